@@ -1,0 +1,307 @@
+/*
+ * rt_cuda.h — C ABI of librt_cuda.so, the GB300 (sm_103a) implementation of the
+ * Tesina-RT hot path: LBVH construction (Morton codes over triangle centroids,
+ * key/value radix sort, hierarchy emit, bottom-up AABB refit), closest-hit BVH
+ * traversal, shadow-ray any-hit, Whitted shading and reflection-ray generation.
+ *
+ * Conventions (the reference's own: every host method returns int32_t 0 / -1):
+ *   - every entry point returns RT_OK (0) or a negative rt_status;
+ *   - rt_last_error() returns a message for the last failure on this thread;
+ *   - "d_" pointers are device pointers, "h_" pointers are host pointers;
+ *   - descriptor structs passed by pointer are caller-owned and copied on entry;
+ *   - a NULL stream means the context's default stream.
+ *
+ * Struct layouts marked "reference layout" are byte-compatible with the device
+ * structs of the reference's OpenCL kernels so that buffers can be exchanged
+ * with code written against the reference's RayBundle / HitBundle.
+ */
+#ifndef RT_CUDA_H
+#define RT_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------------ */
+/* Status codes                                                             */
+/* ------------------------------------------------------------------------ */
+typedef enum rt_status {
+    RT_OK = 0,
+    RT_ERR = -1,              /* generic failure (the reference's -1)          */
+    RT_ERR_INVALID = -2,      /* bad argument / size / descriptor              */
+    RT_ERR_CUDA = -3,         /* CUDA runtime error                            */
+    RT_ERR_OOM = -4,          /* device allocation failed or budget exceeded   */
+    RT_ERR_TIMEOUT = -5,      /* a device-side bounded wait gave up            */
+    RT_ERR_NOT_BUILT = -6,    /* scene has no BVH yet                          */
+    RT_ERR_OVERFLOW = -7,     /* traversal stack or queue overflow             */
+    RT_ERR_REJECTED = -8      /* serving: request refused by admission control */
+} rt_status;
+
+/* Device status bits reported by rt_device_status(). */
+#define RT_DEV_TIMEOUT   0x1u  /* a decoupled look-back spin hit its cap      */
+#define RT_DEV_OVERFLOW  0x2u  /* a traversal stack overflowed                */
+#define RT_DEV_BADINDEX  0x4u  /* an index check failed (checked builds)      */
+
+/* ------------------------------------------------------------------------ */
+/* Scene data model (reference: include/rt/{material,light,camera}.hpp)     */
+/* ------------------------------------------------------------------------ */
+#define RT_MAX_LIGHTS 8
+
+/* Light types: SPOT_L and DIR_L keep the reference's values
+ * (include/rt/light.hpp:69-72); POINT_L is an extension (omni light, no cone,
+ * shadow ray as for a spot light, LD = 1). */
+enum { RT_SPOT_L = 0, RT_DIR_L = 1, RT_POINT_L = 2 };
+
+typedef struct rt_light {        /* 64 B */
+    int32_t type;                /* RT_SPOT_L / RT_DIR_L / RT_POINT_L          */
+    float   radius;              /* spot: unused by the shading math           */
+    float   angle;               /* spot: cosine cutoff                        */
+    float   _pad0;
+    float   pos[4];              /* spot / point position                      */
+    float   dir[4];              /* spot axis or directional light direction   */
+    float   color[4];
+} rt_light;
+
+/* Ambient colour plus 1..RT_MAX_LIGHTS lights.  With count == 1 this is the
+ * reference's lights_cl (include/rt/light.hpp:86-92); more lights are summed in
+ * order, each with its own shadow ray. */
+typedef struct rt_lights {
+    float    ambient[4];
+    int32_t  count;
+    int32_t  _pad[3];
+    rt_light light[RT_MAX_LIGHTS];
+} rt_lights;
+
+/* reference layout: material_cl (include/rt/material.hpp:57-73), 32 B */
+typedef struct rt_material {
+    float   diffuse[4];
+    float   shininess;
+    float   reflectiveness;
+    float   refractive_index;
+    int32_t texture;             /* < 0: untextured (only case supported)      */
+} rt_material;
+
+/* Pinhole camera basis as passed to generate_primary_rays
+ * (src/kernel/primary-ray-generator.cl:27-37): right and up are pre-scaled by
+ * tan(fov/2) and aspect (src/rt/camera.cpp:31-59). */
+typedef struct rt_camera {
+    float pos[4];
+    float dir[4];
+    float right[4];
+    float up[4];
+} rt_camera;
+
+/* Mirror of Camera::set (src/rt/camera.cpp:31-59).  fov is the vertical full
+ * angle in radians, aspect = width / height. */
+int32_t rt_camera_set(rt_camera* cam, const float pos[3], const float dir[3],
+                      const float up[3], float fov, float aspect,
+                      int32_t right_handed);
+
+/* Host scene description.  Vertices may be SoA float4 (stride 16) or the
+ * reference's 80-byte Vertex AoS (stride 80, position at 0, normal at 16). */
+typedef struct rt_scene_desc {
+    const void*        h_vertices;       /* positions (and normals if interleaved) */
+    uint32_t           vertex_count;
+    uint32_t           vertex_stride;    /* bytes between consecutive positions    */
+    uint32_t           position_offset;  /* byte offset of position in a vertex    */
+    uint32_t           normal_offset;    /* byte offset of normal (if h_normals==0)*/
+    const void*        h_normals;        /* optional separate float4 normals       */
+    const uint32_t*    h_indices;        /* 3 per triangle                         */
+    uint32_t           triangle_count;
+    uint32_t           material_count;
+    const rt_material* h_materials;
+    const uint32_t*    h_material_map;   /* material index per triangle            */
+    rt_lights          lights;
+} rt_scene_desc;
+
+/* LBVH configuration: the reference's bvh_depth and bvh_min_leaf_size
+ * (src/rt/bvh-builder.cpp:194-199; clamps depth to [1,32] here, min_leaf to
+ * [1,256]). */
+typedef struct rt_bvh_cfg {
+    int32_t depth;               /* Morton bits, 1..32 (spec: 30)        */
+    int32_t min_leaf_size;       /* 1..256                                     */
+} rt_bvh_cfg;
+
+/* One node of the canonical range tree, emitted in pre-order (left first).
+ * Node numbering of the reference is nondeterministic; the canonical tree is
+ * what parity is defined on. */
+typedef struct rt_canon_node {
+    uint32_t start, end;         /* triangle range [start, end) in sorted order */
+    uint32_t leaf;               /* 1 = leaf                                    */
+    uint32_t depth;              /* tree depth (root = 0)                       */
+    float    lo[4];
+    float    hi[4];
+} rt_canon_node;
+
+/* ------------------------------------------------------------------------ */
+/* Reference-layout ray / sample / hit records (device structs of the .cl)  */
+/* ------------------------------------------------------------------------ */
+typedef struct rt_ray {          /* Ray: float3 ori, dir, invDir; tMin, tMax   */
+    float ori[4];
+    float dir[4];
+    float inv_dir[4];
+    float tmin, tmax;
+    float _pad[2];
+} rt_ray;                        /* 64 B */
+
+typedef struct rt_sample {       /* Sample: Ray ray; int pixel; float contribution */
+    rt_ray  ray;
+    int32_t pixel;
+    float   contribution;
+    int32_t _pad[2];
+} rt_sample;                     /* 80 B */
+
+typedef struct rt_hit {          /* SampleTraceInfo (device layout, bool = 1 B) */
+    uint8_t hit;
+    uint8_t shadow_hit;          /* bit l set: light l occluded (1 light: 0/1) */
+    uint8_t inverse_n;
+    uint8_t reserved;
+    float   t;
+    int32_t id;                  /* triangle index in sorted order             */
+    float   _pad0;
+    float   uv[2];
+    float   _pad1[2];
+    float   n[4];
+    float   hit_point[4];
+} rt_hit;                        /* 64 B */
+
+typedef struct rt_pixel_sample { /* PixelSample: ox, oy, contribution */
+    float ox, oy, contribution;
+} rt_pixel_sample;
+
+/* Per-render counters (reference convention: rays = primary + secondary). */
+typedef struct rt_render_stats {
+    uint64_t primary_rays;
+    uint64_t secondary_rays;
+    uint64_t shadow_rays;
+    uint64_t hits;
+} rt_render_stats;
+
+typedef struct rt_ctx    rt_ctx;
+typedef struct rt_scene  rt_scene;
+typedef void*            rt_stream;   /* a cudaStream_t */
+
+/* ------------------------------------------------------------------------ */
+/* Context, errors, streams, buffers (replaces DeviceInterface/DeviceMemory, */
+/* include/gpu/interface.hpp:20-80, include/gpu/memory.hpp)                 */
+/* ------------------------------------------------------------------------ */
+const char* rt_last_error(void);
+int32_t rt_init(rt_ctx** ctx, int32_t device);
+int32_t rt_shutdown(rt_ctx* ctx);
+/* Reads (and clears) the device status word: RT_DEV_* bits. */
+int32_t rt_device_status(rt_ctx* ctx, uint32_t* bits);
+int32_t rt_stream_create(rt_ctx* ctx, rt_stream* stream);
+int32_t rt_stream_destroy(rt_ctx* ctx, rt_stream stream);
+int32_t rt_stream_sync(rt_ctx* ctx, rt_stream stream);
+int32_t rt_buf_alloc(rt_ctx* ctx, size_t bytes, void** d_ptr);
+int32_t rt_buf_free(rt_ctx* ctx, void* d_ptr);
+int32_t rt_buf_write(rt_ctx* ctx, void* d_dst, const void* h_src, size_t bytes, rt_stream s);
+int32_t rt_buf_read(rt_ctx* ctx, void* h_dst, const void* d_src, size_t bytes, rt_stream s);
+int32_t rt_buf_copy(rt_ctx* ctx, void* d_dst, const void* d_src, size_t bytes, rt_stream s);
+int32_t rt_buf_zero(rt_ctx* ctx, void* d_dst, size_t bytes, rt_stream s);
+
+/* ------------------------------------------------------------------------ */
+/* Scene (replaces Scene::transfer_aggregate_mesh_to_device,                */
+/* src/rt/scene.cpp:236-321, and the buffer accessors scene.hpp:125-133)    */
+/* ------------------------------------------------------------------------ */
+int32_t rt_scene_create(rt_ctx* ctx, rt_scene** scene);
+int32_t rt_scene_destroy(rt_ctx* ctx, rt_scene* scene);
+int32_t rt_scene_upload(rt_ctx* ctx, rt_scene* scene, const rt_scene_desc* desc, rt_stream s);
+/* Replace vertex positions/normals (float4 each, host memory) keeping topology;
+ * analogue of Scene::update_aggregate_mesh_vertices (scene.cpp:967-984). */
+int32_t rt_scene_update_vertices(rt_ctx* ctx, rt_scene* scene, const float* h_pos4,
+                                 const float* h_nrm4, uint32_t vertex_count, rt_stream s);
+/* Same, from device memory. */
+int32_t rt_scene_update_vertices_device(rt_ctx* ctx, rt_scene* scene, const float* d_pos4,
+                                        const float* d_nrm4, uint32_t vertex_count, rt_stream s);
+int32_t rt_scene_set_lights(rt_ctx* ctx, rt_scene* scene, const rt_lights* lights);
+/* Device buffers of the scene (reference: Scene::index_mem(), material_map_mem()).
+ * After a build, indices and material map are permuted into sorted order, as
+ * the reference permutes them in place (bvh-builder.cpp:470-527). */
+int32_t rt_scene_buffers(rt_ctx* ctx, rt_scene* scene, uint32_t** d_indices,
+                         uint32_t** d_material_map, float** d_positions,
+                         float** d_normals, uint32_t* triangle_count);
+/* Host copies of the per-build arrays used for parity:
+ * unsorted Morton keys (per original triangle), the sort permutation
+ * (sorted slot -> original triangle) and the sorted keys.  Any may be NULL. */
+int32_t rt_scene_read_sort(rt_ctx* ctx, rt_scene* scene, uint32_t* h_keys,
+                           uint32_t* h_perm, uint32_t* h_sorted_keys);
+
+/* ------------------------------------------------------------------------ */
+/* LBVH (replaces BVHBuilder, include/rt/bvh-builder.hpp:16-28)             */
+/* ------------------------------------------------------------------------ */
+/* BVHBuilder::build_lbvh (src/rt/bvh-builder.cpp:201-741). */
+int32_t rt_bvh_build_lbvh(rt_ctx* ctx, rt_scene* scene, const rt_bvh_cfg* cfg, rt_stream s);
+/* BVHBuilder::refit_lbvh (src/rt/bvh-builder.cpp:743-850): recompute AABBs on
+ * the existing topology and triangle order. */
+int32_t rt_bvh_refit_lbvh(rt_ctx* ctx, rt_scene* scene, rt_stream s);
+/* Canonical pre-order tree (synchronous).  *count receives the node count;
+ * pass out == NULL to query it. */
+int32_t rt_bvh_export(rt_ctx* ctx, rt_scene* scene, rt_canon_node* out,
+                      uint32_t capacity, uint32_t* count);
+/* Device time of the last build / refit in milliseconds (CUDA events). */
+int32_t rt_bvh_last_time_ms(rt_ctx* ctx, rt_scene* scene, float* ms);
+
+/* ------------------------------------------------------------------------ */
+/* Stage-wise pipeline on reference-layout buffers (drop-in for the         */
+/* reference's PrimaryRayGenerator, Tracer, RayShader,                      */
+/* SecondaryRayGenerator, FrameBuffer)                                      */
+/* ------------------------------------------------------------------------ */
+/* PrimaryRayGenerator::generate (src/rt/primary-ray-generator.cpp:57-165,
+ * kernel primary-ray-generator.cl:27-103). Rays for global ids
+ * [offset, offset+ray_count) of a w*h*spp image, quad_size pixel blocks.
+ * d_pixel_samples may be NULL (one sample {0,0,1}). */
+int32_t rt_gen_primary(rt_ctx* ctx, const rt_camera* cam, int32_t width, int32_t height,
+                       int32_t quad_size, int32_t spp, const rt_pixel_sample* d_pixel_samples,
+                       size_t ray_count, size_t offset, rt_sample* d_samples, rt_stream s);
+/* Tracer::trace (src/rt/tracer.cpp:140-269, kernel trace-bvh.cl:465-481). */
+int32_t rt_trace(rt_ctx* ctx, rt_scene* scene, const rt_sample* d_samples, int32_t ray_count,
+                 rt_hit* d_hits, int32_t secondary, rt_stream s);
+/* Tracer::shadow_trace (src/rt/tracer.cpp:273-352, kernel
+ * shadow-trace-bvh.cl:375-418); one shadow ray per light, result bitmask in
+ * rt_hit.shadow_hit. */
+int32_t rt_shadow_trace(rt_ctx* ctx, rt_scene* scene, const rt_sample* d_samples,
+                        int32_t ray_count, rt_hit* d_hits, int32_t secondary, rt_stream s);
+/* RayShader::shade (src/rt/ray-shader.cpp:32-154, kernel ray-shader.cl:116-459).
+ * d_image_rgb: 3 uint32 per pixel, fixed point x1e6, accumulated with atomics. */
+int32_t rt_shade(rt_ctx* ctx, rt_scene* scene, const rt_sample* d_samples,
+                 const rt_hit* d_hits, int32_t ray_count, uint32_t* d_image_rgb,
+                 int32_t primary, rt_stream s);
+/* SecondaryRayGenerator::generate (src/rt/secondary-ray-generator.cpp:57-244,
+ * kernels secondary-ray-generator.cl:184-326): reflection rays, stable order.
+ * *d_count (device int32) receives the number of rays written (clamped to
+ * max_out).  If h_count != NULL the call synchronises and stores it there. */
+int32_t rt_gen_secondary(rt_ctx* ctx, rt_scene* scene, const rt_sample* d_in, int32_t rays_in,
+                         const rt_hit* d_hits, rt_sample* d_out, int32_t max_out,
+                         int32_t* d_count, int32_t* h_count, rt_stream s);
+/* FrameBuffer::clear / copy (src/rt/framebuffer.cpp:117-165,
+ * framebuffer.cl:20-54): RGBA8 = round-to-nearest-even saturate(255 * v * 1e-6). */
+int32_t rt_fb_clear(rt_ctx* ctx, uint32_t* d_image_rgb, size_t pixels, rt_stream s);
+int32_t rt_fb_copy(rt_ctx* ctx, const uint32_t* d_image_rgb, uint8_t* d_rgba, size_t pixels,
+                   rt_stream s);
+
+/* ------------------------------------------------------------------------ */
+/* Fused plain path: Renderer::render_to_framebuffer (src/rt/renderer.cpp:  */
+/* 113-214) + FrameBuffer::copy in one persistent kernel.                   */
+/* ------------------------------------------------------------------------ */
+/* d_rgba: w*h RGBA8 (required).  d_image_rgb: optional fixed-point
+ * accumulation buffer (3 uint32 per pixel, written, not accumulated).
+ * d_stats: optional device rt_render_stats (accumulated; caller zeroes). */
+int32_t rt_render(rt_ctx* ctx, rt_scene* scene, const rt_camera* cam, int32_t width,
+                  int32_t height, int32_t max_bounces, uint8_t* d_rgba, uint32_t* d_image_rgb,
+                  rt_render_stats* d_stats, rt_stream s);
+
+/* End-to-end convenience: host vertices in, host image out, synchronous:
+ * optional vertex update -> LBVH build -> render -> RGBA8 to host. */
+int32_t rt_render_host(rt_ctx* ctx, rt_scene* scene, const float* h_pos4, const float* h_nrm4,
+                       uint32_t vertex_count, const rt_bvh_cfg* cfg, const rt_camera* cam,
+                       int32_t width, int32_t height, int32_t max_bounces, uint8_t* h_rgba,
+                       rt_render_stats* h_stats, rt_stream s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RT_CUDA_H */

@@ -1,0 +1,199 @@
+"""ctypes bindings of the oracle libraries (test infrastructure only).
+
+``Oracle`` wraps liboracle.so (the CPU restatement); ``RefKernels`` wraps
+oracle/_ref/libref.so (the reference's own kernels compiled for the CPU),
+which exists only where the reference checkout was available at build time.
+"""
+import ctypes as C
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(HERE, "..", "tesina-rt_gb300"))
+from rtgb import abi  # noqa: E402
+
+P = C.c_void_p
+U32, I32, SZ, F = C.c_uint32, C.c_int32, C.c_size_t, C.c_float
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(P)
+
+
+class _Lib:
+    def _bind(self, lib, name, res, args):
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+        return f
+
+
+class Oracle(_Lib):
+    def __init__(self, path=None):
+        self.lib = C.CDLL(path or os.path.join(HERE, "liboracle.so"))
+        b, L = self._bind, self.lib
+        self.scene_new = b(L, "orc_scene_new", P, [P, P, U32, P, U32, P, U32, P, P])
+        self.scene_free = b(L, "orc_scene_free", None, [P])
+        self.set_positions = b(L, "orc_set_positions", C.c_int, [P, P, P])
+        self.morton_keys = b(L, "orc_morton_keys", C.c_int, [P, C.c_int, P, P, P])
+        self.sort_bitonic = b(L, "orc_sort_bitonic", C.c_int, [P, U32, P])
+        self.build = b(L, "orc_build", C.c_int, [P, C.c_int, C.c_int, C.c_int])
+        self.refit = b(L, "orc_refit", C.c_int, [P])
+        self.get_sort = b(L, "orc_get_sort", C.c_int, [P, P, P, P, P])
+        self.get_buffers = b(L, "orc_get_buffers", C.c_int, [P, P, P])
+        self.export = b(L, "orc_export", C.c_int, [P, P, U32, C.POINTER(U32)])
+        self.gen_primary = b(L, "orc_gen_primary", C.c_int,
+                             [P, I32, I32, I32, I32, P, SZ, SZ, P])
+        self.trace = b(L, "orc_trace", C.c_int, [P, P, I32, P, C.c_int])
+        self.shadow = b(L, "orc_shadow", C.c_int, [P, P, I32, P, C.c_int])
+        self.shade = b(L, "orc_shade", C.c_int, [P, P, P, I32, P, C.c_int])
+        self.gen_secondary = b(L, "orc_gen_secondary", C.c_int,
+                               [P, P, I32, P, P, I32, C.POINTER(I32)])
+        self.fb_copy = b(L, "orc_fb_copy", C.c_int, [P, P, SZ])
+        self.render = b(L, "orc_render", C.c_int,
+                        [P, P, I32, I32, I32, SZ, SZ, SZ, P, P, C.c_int])
+        self.fp64_closest = b(L, "orc_fp64_closest", C.c_int, [P, P, I32, P, P, C.c_int])
+        self.fp64_t_of = b(L, "orc_fp64_t_of", C.c_int, [P, P, I32, P, P])
+
+    def new_scene(self, sc):
+        h = self.scene_new(_p(sc.pos4), _p(sc.nrm4), sc.n_verts, _p(sc.idx), sc.n_tris,
+                           _p(sc.mats), sc.mats.shape[0], _p(sc.mat_map), C.byref(sc.lights))
+        return OracleScene(self, h, sc)
+
+
+class OracleScene:
+    def __init__(self, orc, h, sc):
+        self.o, self.h, self.n = orc, h, sc.n_tris
+        self.lights = sc.lights
+
+    def __del__(self):
+        try:
+            self.o.scene_free(self.h)
+        except Exception:
+            pass
+
+    def build(self, depth=30, min_leaf=1, sort_kind=0):
+        r = self.o.build(self.h, depth, min_leaf, sort_kind)
+        if r:
+            raise RuntimeError("oracle build failed")
+
+    def sort_arrays(self):
+        n = self.n
+        keys, perm, sk, orig = (np.zeros(n, np.uint32) for _ in range(4))
+        self.o.get_sort(self.h, _p(keys), _p(perm), _p(sk), _p(orig))
+        return keys, perm, sk, orig
+
+    def buffers(self):
+        idx = np.zeros((self.n, 3), np.uint32)
+        mp = np.zeros(self.n, np.uint32)
+        self.o.get_buffers(self.h, _p(idx), _p(mp))
+        return idx, mp
+
+    def canon(self):
+        cnt = U32(0)
+        self.o.export(self.h, None, 0, C.byref(cnt))
+        out = np.zeros(cnt.value, abi.CANON_DTYPE)
+        self.o.export(self.h, _p(out), cnt.value, C.byref(cnt))
+        return out
+
+    def trace(self, samples, threads=0):
+        hits = np.zeros(samples.shape[0], abi.HIT_DTYPE)
+        self.o.trace(self.h, _p(samples), samples.shape[0], _p(hits), threads or os.cpu_count())
+        return hits
+
+    def shadow(self, samples, hits, threads=0):
+        self.o.shadow(self.h, _p(samples), samples.shape[0], _p(hits), threads or os.cpu_count())
+        return hits
+
+    def shade(self, samples, hits, image, threads=0):
+        self.o.shade(self.h, _p(samples), _p(hits), samples.shape[0], _p(image),
+                     threads or os.cpu_count())
+        return image
+
+    def gen_secondary(self, samples, hits, max_out=None):
+        n = samples.shape[0]
+        max_out = n if max_out is None else max_out
+        out = np.zeros(max_out, abi.SAMPLE_DTYPE)
+        cnt = I32(0)
+        self.o.gen_secondary(self.h, _p(samples), n, _p(hits), _p(out), max_out, C.byref(cnt))
+        return out[:cnt.value]
+
+    def render(self, cam, w, h, max_bounces, offset=0, count=None, tile=1 << 18, threads=0,
+               image=None):
+        count = w * h if count is None else count
+        if image is None:
+            image = np.zeros((h * w, 3), np.uint32)
+        st = abi.RenderStats()
+        r = self.o.render(self.h, C.byref(cam), w, h, max_bounces, offset, count, tile,
+                          _p(image), C.byref(st), threads or os.cpu_count())
+        if r:
+            raise RuntimeError("oracle render failed")
+        return image, st
+
+    def fp64_closest(self, samples, threads=0):
+        n = samples.shape[0]
+        ids = np.zeros(n, np.int32)
+        ts = np.zeros(n, np.float64)
+        self.o.fp64_closest(self.h, _p(samples), n, _p(ids), _p(ts), threads)
+        return ids, ts
+
+    def fp64_t_of(self, samples, tri_orig):
+        n = samples.shape[0]
+        ts = np.zeros(n, np.float64)
+        tri = np.ascontiguousarray(tri_orig, np.int32)
+        self.o.fp64_t_of(self.h, _p(samples), n, _p(tri), _p(ts))
+        return ts
+
+
+def gen_primary(orc, cam, w, h, count=None, offset=0, quad=32):
+    count = w * h if count is None else count
+    out = np.zeros(count, abi.SAMPLE_DTYPE)
+    orc.gen_primary(C.byref(cam), w, h, quad, 1, None, count, offset, _p(out))
+    return out
+
+
+def fb_copy(orc, image):
+    px = image.shape[0]
+    rgba = np.zeros((px, 4), np.uint8)
+    orc.fb_copy(_p(image), _p(rgba), px)
+    return rgba
+
+
+class RefKernels(_Lib):
+    """The reference's kernels compiled for the CPU plus the restated host loops."""
+
+    PATH = os.path.join(HERE, "_ref", "libref.so")
+
+    @classmethod
+    def available(cls):
+        return os.path.exists(cls.PATH)
+
+    def __init__(self):
+        self.lib = C.CDLL(self.PATH)
+        b, L = self._bind, self.lib
+        self.scene_new = b(L, "refd_scene_new", P, [P, P, U32, P, U32, P, U32, P, P])
+        self.scene_free = b(L, "refd_scene_free", None, [P])
+        self.morton = b(L, "refd_morton", C.c_int, [P, C.c_int, P, P, P])
+        self.bitonic = b(L, "refd_bitonic", C.c_int, [P, U32, P])
+        self.apply_perm = b(L, "refd_apply_perm", C.c_int, [P, P])
+        self.get_buffers = b(L, "refd_get_buffers", C.c_int, [P, P, P])
+        self.set_tree = b(L, "refd_set_tree", C.c_int, [P, P, U32])
+        self.get_tree = b(L, "refd_get_tree", C.c_int, [P, P])
+        self.gen_primary = b(L, "refd_gen_primary", C.c_int,
+                             [P, I32, I32, I32, I32, P, SZ, SZ, P])
+        self.trace = b(L, "refd_trace", C.c_int, [P, P, I32, P, C.c_int])
+        self.shadow = b(L, "refd_shadow", C.c_int, [P, P, I32, P, C.c_int])
+        self.shade = b(L, "refd_shade", C.c_int, [P, P, P, I32, P, C.c_int, C.c_int])
+        self.gen_secondary = b(L, "refd_gen_secondary", C.c_int,
+                               [P, P, I32, P, P, I32, C.POINTER(I32)])
+        self.render = b(L, "refd_render", C.c_int,
+                        [P, P, I32, I32, I32, SZ, SZ, SZ, P, P, C.c_int])
+
+    def new_scene(self, sc):
+        h = self.scene_new(_p(sc.pos4), _p(sc.nrm4), sc.n_verts, _p(sc.idx), sc.n_tris,
+                           _p(sc.mats), sc.mats.shape[0], _p(sc.mat_map), C.byref(sc.lights))
+        if not h:
+            raise RuntimeError("reference scene rejected")
+        return h

@@ -1,0 +1,1007 @@
+/*
+ * rt_cpu_ref.cpp — ORACLE (test infrastructure only; never part of the product).
+ *
+ * A CPU restatement of the reference's hot path, used by the tests as the
+ * checker and by bench.py as the timed CPU baseline.  Nothing in the product
+ * library links, loads or calls this file.
+ *
+ * It restates, in the reference's operation order and with IEEE single
+ * precision and no FMA contraction (compile with -ffp-contract=off):
+ *   LBVH build   src/kernel/bvh-builder.cl:100-130 (build_primitive_bbox),
+ *                :318-391 + src/rt/bvh-builder.cpp:289-334 (global bbox),
+ *                :181-252 (morton_encode), bvh-builder-sort.cl:9-232 +
+ *                bvh-builder.cpp:361-454 (bitonic network, exact),
+ *                bvh-builder.cl:49-97 (rearrange_*), :484-671 (process_task /
+ *                find_middle / set_children, as a recursive top-down split),
+ *                :262-311 (build_leaf_bbox / build_node_bbox).
+ *   Trace        src/kernel/trace-bvh.cl:191-417, 465-481 (trace_single).
+ *   Shadow       src/kernel/shadow-trace-bvh.cl:161-315, 375-418.
+ *   Shade        src/kernel/ray-shader.cl:101-333 (untextured, no cubemap).
+ *   Secondary    src/kernel/secondary-ray-generator.cl:184-326 (reflection).
+ *   Primary      src/kernel/primary-ray-generator.cl:27-103.
+ *   Framebuffer  src/kernel/framebuffer.cl:30-54 + RGBA8 UNORM conversion.
+ *   Renderer     src/rt/renderer.cpp:113-214 (tile loop, bounce loop).
+ *
+ * Documented restatement choices (identical in the CUDA path):
+ *   normalize(v) = v * (1 / sqrt(dot(v, v)))  (zero vector stays zero);
+ *   pow(x, 2) = x*x and pow(x, 8) = ((x*x)^2)^2;
+ *   point lights (type 2) and several lights are extensions: each light adds
+ *   the reference's per-light term in order, with its own shadow ray;
+ *   the LBVH sort is stable (std::stable_sort); orc_sort_bitonic restates the
+ *   reference's bitonic network exactly, for tie-order comparisons.
+ *
+ * Parity pin: tests/test_oracle_pin.py checks this file against the
+ * reference's own OpenCL kernels compiled for the CPU (oracle/_ref).
+ */
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <thread>
+#include <vector>
+
+#include "../include/rt_cuda.h"
+
+namespace {
+
+struct v3 {
+    float x, y, z;
+};
+static inline v3 mk(float x, float y, float z) { return v3{x, y, z}; }
+static inline v3 ld3(const float* p) { return v3{p[0], p[1], p[2]}; }
+static inline v3 add(v3 a, v3 b) { return mk(a.x + b.x, a.y + b.y, a.z + b.z); }
+static inline v3 sub(v3 a, v3 b) { return mk(a.x - b.x, a.y - b.y, a.z - b.z); }
+static inline v3 mul(v3 a, v3 b) { return mk(a.x * b.x, a.y * b.y, a.z * b.z); }
+static inline v3 muls(v3 a, float s) { return mk(a.x * s, a.y * s, a.z * s); }
+static inline v3 neg(v3 a) { return mk(-a.x, -a.y, -a.z); }
+static inline float dot(v3 a, v3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+static inline v3 cross(v3 a, v3 b) {
+    return mk(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+static inline v3 normalize(v3 v) {
+    float d = dot(v, v);
+    if (d == 0.0f) return v;
+    float inv = 1.0f / std::sqrt(d);
+    return muls(v, inv);
+}
+static inline float clamp01(float x) { return std::fmin(std::fmax(x, 0.0f), 1.0f); }
+/* OpenCL max/min as specified ("returns y if x < y, otherwise x"), used by
+ * shadow-trace-bvh.cl's bbox_hit. */
+static inline float cl_max(float x, float y) { return (x < y) ? y : x; }
+static inline float cl_min(float x, float y) { return (y < x) ? y : x; }
+
+struct Node {
+    float lo[3], hi[3];
+    uint32_t a, b;  /* leaf: [a, b) triangle range; interior: left, right */
+    uint32_t leaf;
+    uint32_t depth;
+    uint32_t start, end;
+};
+
+unsigned hw_threads() {
+    unsigned n = std::thread::hardware_concurrency();
+    return n ? n : 1;
+}
+
+template <class F>
+void parallel_for(int64_t n, int threads, F f) {
+    if (threads <= 1 || n < 1024) {
+        for (int64_t i = 0; i < n; ++i) f(i);
+        return;
+    }
+    std::atomic<int64_t> next(0);
+    const int64_t chunk = 256;
+    std::vector<std::thread> pool;
+    for (int t = 0; t < threads; ++t) {
+        pool.emplace_back([&]() {
+            for (;;) {
+                int64_t b = next.fetch_add(chunk);
+                if (b >= n) break;
+                int64_t e = std::min(n, b + chunk);
+                for (int64_t i = b; i < e; ++i) f(i);
+            }
+        });
+    }
+    for (auto& th : pool) th.join();
+}
+
+}  // namespace
+
+struct orc_scene {
+    std::vector<float> pos;       /* V*4 */
+    std::vector<float> nrm;       /* V*4 */
+    uint32_t V = 0;
+    std::vector<uint32_t> idx;    /* N*3, permuted into sorted order by a build */
+    std::vector<uint32_t> map;    /* N,   permuted likewise                     */
+    uint32_t N = 0;
+    std::vector<rt_material> mats;
+    rt_lights lights;
+    /* build products */
+    std::vector<uint32_t> keys;        /* per original triangle of this build */
+    std::vector<uint32_t> perm;        /* sorted slot -> triangle id before the build */
+    std::vector<uint32_t> sorted_keys;
+    std::vector<uint32_t> orig_id;     /* sorted slot -> triangle id at upload */
+    std::vector<Node> nodes;           /* pre-order, root = 0 */
+    int depth = 30, min_leaf = 1;
+    bool built = false;
+};
+
+/* ----------------------------------------------------------------------- */
+/* LBVH                                                                     */
+/* ----------------------------------------------------------------------- */
+
+/* bvh-builder.cl:100-130 build_primitive_bbox. */
+static void prim_bbox(const orc_scene* s, uint32_t i, float lo[3], float hi[3]) {
+    const float* p0 = &s->pos[4 * (size_t)s->idx[3 * (size_t)i + 0]];
+    const float* p1 = &s->pos[4 * (size_t)s->idx[3 * (size_t)i + 1]];
+    const float* p2 = &s->pos[4 * (size_t)s->idx[3 * (size_t)i + 2]];
+    for (int c = 0; c < 3; ++c) {
+        float h = p0[c], l = p0[c];
+        h = std::fmax(h, p1[c]);
+        h = std::fmax(h, p2[c]);
+        l = std::fmin(l, p1[c]);
+        l = std::fmin(l, p2[c]);
+        hi[c] = h;
+        lo[c] = l;
+    }
+}
+
+/* bvh-builder.cl:181-252 morton_encode (one triangle). */
+static uint32_t morton_encode(const float lo[3], const float hi[3], const float glo[3],
+                              const float ghi[3], int depth) {
+    float scale = (float)std::pow(2.0, std::ceil(depth / 3.0));
+    uint32_t m[3];
+    for (int c = 0; c < 3; ++c) {
+        float center = (hi[c] + lo[c]) * 0.5f;
+        float inv = 1.0f / (ghi[c] - glo[c]);
+        float slice = (center - glo[c]) * inv;
+        slice = std::fmax(0.0f, std::fmin(1.0f, slice));
+        slice *= scale;
+        m[c] = (uint32_t)slice;
+    }
+    int offset = depth % 3 ? 3 - (depth % 3) : 0;
+    int axis = (offset + 1) % 3;
+    uint32_t code = 0;
+    for (int i = 0; i < depth; ++i) {
+        int src_bit = (i + offset) / 3;
+        code |= ((m[axis] >> src_bit) & 1u) << i;
+        axis = (axis + 1) % 3;
+    }
+    return code;
+}
+
+/* Top-down split of process_task / find_middle / set_children
+ * (bvh-builder.cl:484-580), recursively.  The reference emits the same
+ * ranges level by level with atomics; node numbering differs, the range tree
+ * does not. */
+static void emit(orc_scene* s, uint32_t start, uint32_t end, int level, uint32_t depth_in_tree) {
+    const uint32_t* codes = s->sorted_keys.data();
+    const int max_level = s->depth;
+    uint32_t me = (uint32_t)s->nodes.size();
+    s->nodes.push_back(Node{});
+    Node nd{};
+    nd.start = start;
+    nd.end = end;
+    nd.depth = depth_in_tree;
+    nd.leaf = 1;
+    nd.a = start;
+    nd.b = end;
+
+    uint32_t first = start, last = end - 1;
+    int bit = max_level - 1 - level;
+    bool leaf = false;
+    if ((uint32_t)(last - first - 1) <= (uint32_t)s->min_leaf) leaf = true;  /* unsigned, :501 */
+    if (!leaf && bit < 0) leaf = true;
+    auto codebit = [&](uint32_t x) { return (codes[x] >> bit) & 1u; };
+    if (!leaf) {
+        while (codebit(first) != 0 || codebit(last) == 0) {
+            level++;
+            bit = max_level - 1 - level;
+            if (bit < 0) {
+                leaf = true;
+                break;
+            }
+        }
+    }
+    if (leaf) {
+        s->nodes[me] = nd;
+        return;
+    }
+    while (first + 1 < last) {
+        uint32_t middle = (first + last) / 2;
+        if (codebit(middle) == 0)
+            first = middle;
+        else
+            last = middle;
+    }
+    uint32_t split = last;
+    nd.leaf = 0;
+    s->nodes[me] = nd;
+    uint32_t l = (uint32_t)s->nodes.size();
+    emit(s, start, split, level + 1, depth_in_tree + 1);
+    uint32_t r = (uint32_t)s->nodes.size();
+    emit(s, split, end, level + 1, depth_in_tree + 1);
+    s->nodes[me].a = l;
+    s->nodes[me].b = r;
+}
+
+/* build_leaf_bbox + build_node_bbox (bvh-builder.cl:262-311): leaves merge
+ * their triangles' boxes, interior nodes merge their children (post-order). */
+static void refit(orc_scene* s) {
+    std::vector<float> tlo((size_t)s->N * 3), thi((size_t)s->N * 3);
+    for (uint32_t i = 0; i < s->N; ++i) prim_bbox(s, i, &tlo[3 * (size_t)i], &thi[3 * (size_t)i]);
+    for (int64_t k = (int64_t)s->nodes.size() - 1; k >= 0; --k) {
+        Node& nd = s->nodes[k];
+        if (nd.leaf) {
+            for (int c = 0; c < 3; ++c) {
+                nd.lo[c] = tlo[3 * (size_t)nd.a + c];
+                nd.hi[c] = thi[3 * (size_t)nd.a + c];
+            }
+            for (uint32_t i = nd.a + 1; i < nd.b; ++i)
+                for (int c = 0; c < 3; ++c) {
+                    nd.lo[c] = std::fmin(nd.lo[c], tlo[3 * (size_t)i + c]);
+                    nd.hi[c] = std::fmax(nd.hi[c], thi[3 * (size_t)i + c]);
+                }
+        } else {
+            const Node& l = s->nodes[nd.a];
+            const Node& r = s->nodes[nd.b];
+            for (int c = 0; c < 3; ++c) {
+                nd.lo[c] = std::fmin(l.lo[c], r.lo[c]);
+                nd.hi[c] = std::fmax(l.hi[c], r.hi[c]);
+            }
+        }
+    }
+}
+
+/* Bitonic network of bvh-builder-sort.cl:26-232 driven by the host loop of
+ * bvh-builder.cpp:361-454.  Returns -1 where the reference would exit(1)
+ * (a launch with zero work-items for non-power-of-two N < 16). */
+static int bitonic_sort(const uint32_t* codes, uint32_t n, uint32_t* tri) {
+    for (uint32_t i = 0; i < n; ++i) tri[i] = i;
+    int size = (int)n;
+    int n2 = 1;
+    while (n2 < size) n2 <<= 1;
+    int64_t ms2 = size / 2 + (size % 2);
+    int64_t ms4 = size / 4 + (size - size % 4);
+    int64_t ms8 = size / 8 + (size - size % 8);
+    int64_t ms16 = size / 16 + (size - size % 16);
+    auto smaller = [&](uint32_t a, uint32_t b) { return codes[a] < codes[b]; };
+    for (int len = 1; len < n2; len <<= 1) {
+        int dir = len << 1;
+        int inv = ((size - 1) & dir) == 0 && dir != n2;
+        int last_step = dir == n2;
+        for (int inc = len; inc > 0; inc >>= 1) {
+            int G;
+            int64_t items;
+            if (inc > 4) {
+                inc >>= 3;
+                G = 16;
+                items = ms16;
+            } else if (inc > 2) {
+                inc >>= 2;
+                G = 8;
+                items = ms8;
+            } else if (inc > 1) {
+                inc >>= 1;
+                G = 4;
+                items = ms4;
+            } else {
+                G = 2;
+                items = ms2;
+            }
+            if (items == 0) return -1;
+            int shift = G == 16 ? 4 : G == 8 ? 3 : G == 4 ? 2 : 1;
+            for (int64_t gid = 0; gid < items; ++gid) {
+                int64_t i = gid;
+                int64_t low = i & (inc - 1);
+                if (G == 2)
+                    i = (i << 1) - low;
+                else
+                    i = ((i - low) << shift) + low;
+                if (i + inc >= size) continue;
+                bool order_asc = !(dir & i) && !last_step;
+                if (G == 2) {
+                    bool inc_is_smaller = smaller(tri[i + inc], tri[i]);
+                    bool swap = (inc_is_smaller == order_asc) == (bool)inv;
+                    if (swap) std::swap(tri[i], tri[i + inc]);
+                    continue;
+                }
+                uint32_t t[16], val[16];
+                auto in_range = [&](int64_t X) { return i + X * inc < size; };
+                for (int j = 0; j < G && in_range(j); ++j) {
+                    t[j] = j;
+                    val[j] = tri[i + (int64_t)j * inc];
+                }
+                /* ORDERV / B2V..B16V: recursive half-cleaner on slots [a, a+G). */
+                auto orderv = [&](int a, int b) {
+                    if (in_range(b)) {
+                        bool swap = (smaller(val[t[b]], val[t[a]]) == order_asc) == (bool)inv;
+                        if (swap) std::swap(t[a], t[b]);
+                    }
+                };
+                struct Rec {
+                    static void run(int a, int g, decltype(orderv)& o) {
+                        if (g == 2) {
+                            o(a, a + 1);
+                            return;
+                        }
+                        for (int k = 0; k < g / 2; ++k) o(a + k, a + k + g / 2);
+                        run(a, g / 2, o);
+                        run(a + g / 2, g / 2, o);
+                    }
+                };
+                Rec::run(0, G, orderv);
+                for (int j = 0; j < G && in_range(j) && in_range(t[j]); ++j)
+                    tri[i + (int64_t)j * inc] = val[t[j]];
+            }
+        }
+    }
+    return 0;
+}
+
+/* ----------------------------------------------------------------------- */
+/* Traversal                                                                */
+/* ----------------------------------------------------------------------- */
+struct Ray {
+    v3 ori, dir, inv;
+    float tmin, tmax;
+};
+static inline Ray ray_of(const rt_sample& s) {
+    return Ray{ld3(s.ray.ori), ld3(s.ray.dir), ld3(s.ray.inv_dir), s.ray.tmin, s.ray.tmax};
+}
+
+/* trace-bvh.cl:247-273 bbox_hit (fmin / fmax). */
+static inline bool bbox_hit(const Node& nd, const Ray& r) {
+    float tMin = r.tmin, tMax = r.tmax;
+    float lt[3], ht[3];
+    const float* o = &r.ori.x;
+    const float* iv = &r.inv.x;
+    for (int c = 0; c < 3; ++c) {
+        lt[c] = (nd.lo[c] - o[c]) * iv[c];
+        ht[c] = (nd.hi[c] - o[c]) * iv[c];
+    }
+    for (int c = 0; c < 3; ++c) {
+        if (std::fabs(iv[c]) > 1e-6f) {
+            tMin = std::fmax(tMin, std::fmin(lt[c], ht[c]));
+            tMax = std::fmin(tMax, std::fmax(lt[c], ht[c]));
+        }
+    }
+    return tMin <= tMax;
+}
+
+/* shadow-trace-bvh.cl:160-186 bbox_hit (OpenCL max / min). */
+static inline bool bbox_hit_shadow(const Node& nd, const Ray& r) {
+    float tMin = r.tmin, tMax = r.tmax;
+    float lt[3], ht[3];
+    const float* o = &r.ori.x;
+    const float* iv = &r.inv.x;
+    for (int c = 0; c < 3; ++c) {
+        lt[c] = (nd.lo[c] - o[c]) * iv[c];
+        ht[c] = (nd.hi[c] - o[c]) * iv[c];
+    }
+    for (int c = 0; c < 3; ++c) {
+        if (std::fabs(iv[c]) > 1e-6f) {
+            tMin = cl_max(tMin, cl_min(lt[c], ht[c]));
+            tMax = cl_min(tMax, cl_max(lt[c], ht[c]));
+        }
+    }
+    return tMin <= tMax;
+}
+
+struct Best {
+    int32_t id;
+    float t, u, v;
+};
+
+/* Möller–Trumbore of leaf_hit (trace-bvh.cl:275-328).  Returns 1 on a
+ * candidate and fills t/u/v. */
+static inline bool mt(const orc_scene* s, uint32_t tri, const Ray& r, float* T, float* U, float* V) {
+    v3 v0 = ld3(&s->pos[4 * (size_t)s->idx[3 * (size_t)tri + 0]]);
+    v3 v1 = ld3(&s->pos[4 * (size_t)s->idx[3 * (size_t)tri + 1]]);
+    v3 v2 = ld3(&s->pos[4 * (size_t)s->idx[3 * (size_t)tri + 2]]);
+    v3 e1 = sub(v1, v0), e2 = sub(v2, v0);
+    v3 h = cross(r.dir, e2);
+    float a = dot(e1, h);
+    if (a > -1e-26f && a < 1e-26f) return false;
+    float f = 1.0f / a;
+    v3 sv = sub(r.ori, v0);
+    float u = f * dot(sv, h);
+    if (u < 0.0f || u > 1.0f) return false;
+    v3 q = cross(sv, e1);
+    float v = f * dot(r.dir, q);
+    if (v < 0.0f || u + v > 1.0f) return false;
+    *T = f * dot(e2, q);
+    *U = u;
+    *V = v;
+    return true;
+}
+
+/* trace_ray (trace-bvh.cl:330-417): 32-entry stack, near child first by
+ * dot(dir, right.lo - left.lo) > 0, own box tested when a node is visited. */
+static Best trace_ray(const orc_scene* s, Ray ray) {
+    Best best{-1, ray.tmax, 0.f, 0.f};
+    uint32_t levels[32];
+    uint32_t level = 0, curr = 0;
+    const Node* nodes = s->nodes.data();
+    for (;;) {
+        const Node& nd = nodes[curr];
+        if (!bbox_hit(nd, ray)) {
+            if (level > 0 && level < 32) {
+                curr = levels[--level];
+                continue;
+            }
+            return best;
+        }
+        if (nd.leaf) {
+            for (uint32_t i = nd.a; i < nd.b; ++i) {
+                float t, u, v;
+                if (!mt(s, i, ray, &t, &u, &v)) continue;
+                if (t <= best.t && t >= ray.tmin) best = Best{(int32_t)i, t, u, v};
+            }
+            if (best.id >= 0) ray.tmax = best.t;
+            if (level > 0 && level < 32) {
+                curr = levels[--level];
+                continue;
+            }
+            return best;
+        }
+        const Node& l = nodes[nd.a];
+        const Node& r = nodes[nd.b];
+        v3 dl = sub(ld3(r.lo), ld3(l.lo));
+        bool order = dot(ray.dir, dl) > 0.0f;
+        uint32_t first = order ? nd.a : nd.b, second = order ? nd.b : nd.a;
+        if (level >= 32) return best; /* cannot happen for depth <= 32 */
+        levels[level++] = second;
+        curr = first;
+    }
+}
+
+/* trace_shadow_ray (shadow-trace-bvh.cl:237-315). */
+static bool trace_shadow(const orc_scene* s, const Ray& ray) {
+    uint32_t levels[32];
+    uint32_t level = 0, curr = 0;
+    const Node* nodes = s->nodes.data();
+    for (;;) {
+        const Node& nd = nodes[curr];
+        if (!bbox_hit_shadow(nd, ray)) {
+            if (level > 0 && level < 32) {
+                curr = levels[--level];
+                continue;
+            }
+            return false;
+        }
+        if (nd.leaf) {
+            for (uint32_t i = nd.a; i < nd.b; ++i) {
+                float t, u, v;
+                if (!mt(s, i, ray, &t, &u, &v)) continue;
+                if (t < ray.tmax && t > ray.tmin) return true;
+            }
+            if (level > 0 && level < 32) {
+                curr = levels[--level];
+                continue;
+            }
+            return false;
+        }
+        const Node& l = nodes[nd.a];
+        const Node& r = nodes[nd.b];
+        v3 dl = sub(ld3(r.lo), ld3(l.lo));
+        bool order = dot(ray.dir, dl) > 0.0f;
+        uint32_t first = order ? nd.a : nd.b, second = order ? nd.b : nd.a;
+        if (level >= 32) return false;
+        levels[level++] = second;
+        curr = first;
+    }
+}
+
+/* complete_trace_info (trace-bvh.cl:190-245).  Texture coordinates are not
+ * part of this data model: uv is written as 0. */
+static void complete(const orc_scene* s, const Ray& ray, const Best& b, rt_hit* out) {
+    if (b.id < 0) {
+        out->hit = 0;
+        return;
+    }
+    rt_hit h;
+    std::memset(&h, 0, sizeof(h));
+    h.hit = 1;
+    h.shadow_hit = out->shadow_hit;
+    h.t = b.t;
+    h.id = b.id;
+    v3 hp = add(ray.ori, muls(ray.dir, b.t));
+    const uint32_t* ix = &s->idx[3 * (size_t)b.id];
+    v3 n0 = normalize(ld3(&s->nrm[4 * (size_t)ix[0]]));
+    v3 n1 = normalize(ld3(&s->nrm[4 * (size_t)ix[1]]));
+    v3 n2 = normalize(ld3(&s->nrm[4 * (size_t)ix[2]]));
+    float u = b.u, v = b.v;
+    float w = 1.0f - (u + v);
+    v3 n = normalize(add(add(muls(n0, w), muls(n2, v)), muls(n1, u)));
+    if (dot(n, ray.dir) > 0.0f) {
+        h.inverse_n = 1;
+        n = neg(n);
+    } else {
+        h.inverse_n = 0;
+    }
+    h.n[0] = n.x; h.n[1] = n.y; h.n[2] = n.z;
+    h.hit_point[0] = hp.x; h.hit_point[1] = hp.y; h.hit_point[2] = hp.z;
+    *out = h;
+}
+
+/* Per-light shadow ray setup of shadow_trace_single
+ * (shadow-trace-bvh.cl:375-418), extended to point lights. */
+static bool light_occluded(const orc_scene* s, const rt_light& L, v3 hp) {
+    Ray r;
+    r.ori = hp;
+    if (L.type == RT_DIR_L) {
+        r.dir = neg(ld3(L.dir));
+    } else if (L.type == RT_SPOT_L) {
+        r.dir = normalize(sub(ld3(L.pos), hp));
+        if (dot(neg(r.dir), ld3(L.dir)) < L.angle) return true;
+    } else if (L.type == RT_POINT_L) {
+        r.dir = normalize(sub(ld3(L.pos), hp));
+    } else {
+        return true;
+    }
+    r.inv = mk(1.0f / r.dir.x, 1.0f / r.dir.y, 1.0f / r.dir.z);
+    r.tmin = 0.01f;
+    r.tmax = 1e37f;
+    return trace_shadow(s, r);
+}
+
+/* shade_sample (ray-shader.cl:116-333), untextured, no cubemap. */
+static void shade_one(const orc_scene* s, const rt_sample& smp, const rt_hit& info, uint32_t* image) {
+    if (!info.hit) return;
+    const rt_lights& Ls = s->lights;
+    const rt_material& mat = s->mats[s->map[info.id]];
+    v3 diffuse = ld3(mat.diffuse);
+    v3 valrgb = mul(ld3(Ls.ambient), diffuse);
+    v3 hp = ld3(info.hit_point);
+    for (int l = 0; l < Ls.count; ++l) {
+        const rt_light& L = Ls.light[l];
+        v3 Ld;
+        float LD;
+        v3 dir_rgb;
+        if (L.type == RT_DIR_L) {
+            Ld = ld3(L.dir);
+            dir_rgb = ld3(L.color);
+            LD = 1.0f;
+        } else if (L.type == RT_SPOT_L) {
+            Ld = normalize(sub(hp, ld3(L.pos)));
+            dir_rgb = ld3(L.color);
+            LD = dot(Ld, ld3(L.dir)) - L.angle;
+            LD /= 1.0f - L.angle;
+            LD = clamp01(LD);
+        } else { /* RT_POINT_L */
+            Ld = normalize(sub(hp, ld3(L.pos)));
+            dir_rgb = ld3(L.color);
+            LD = 1.0f;
+        }
+        dir_rgb = muls(dir_rgb, LD);
+        if (!((info.shadow_hit >> l) & 1u)) {
+            v3 d = ld3(smp.ray.dir);
+            v3 n = ld3(info.n);
+            float dn = dot(d, n);
+            v3 r = sub(d, muls(muls(n, 2.0f), dn));
+            float cosL = clamp01(dot(n, neg(Ld)));
+            cosL = cosL * cosL;
+            float spec = clamp01(dot(r, neg(Ld)));
+            spec = spec * spec;
+            spec = spec * spec;
+            spec = spec * spec;
+            spec *= cosL * mat.shininess;
+            valrgb = add(valrgb, muls(mul(dir_rgb, diffuse), cosL));
+            valrgb = add(valrgb, muls(dir_rgb, spec));
+        }
+    }
+    valrgb = muls(valrgb, 1.0f - mat.reflectiveness);
+    v3 f = muls(valrgb, smp.contribution);
+    f = mk(clamp01(f.x), clamp01(f.y), clamp01(f.z));
+    uint32_t* px = image + 3 * (size_t)smp.pixel;
+    px[0] += (uint32_t)std::floor(f.x * 1e6f);
+    px[1] += (uint32_t)std::floor(f.y * 1e6f);
+    px[2] += (uint32_t)std::floor(f.z * 1e6f);
+}
+
+/* Reflection branch of generate_secondary_rays_disc
+ * (secondary-ray-generator.cl:258-270). */
+static void reflect_ray(const rt_sample& in, const rt_hit& info, float refl, rt_sample* out) {
+    v3 d = neg(normalize(ld3(in.ray.dir)));
+    v3 n = normalize(ld3(info.n));
+    d = neg(d);
+    v3 dir = normalize(sub(d, muls(muls(n, 2.0f), dot(d, n))));
+    rt_sample o;
+    std::memset(&o, 0, sizeof(o));
+    o.ray.ori[0] = info.hit_point[0];
+    o.ray.ori[1] = info.hit_point[1];
+    o.ray.ori[2] = info.hit_point[2];
+    o.ray.dir[0] = dir.x; o.ray.dir[1] = dir.y; o.ray.dir[2] = dir.z;
+    o.ray.inv_dir[0] = 1.0f / dir.x;
+    o.ray.inv_dir[1] = 1.0f / dir.y;
+    o.ray.inv_dir[2] = 1.0f / dir.z;
+    o.ray.tmin = 0.0001f;
+    o.ray.tmax = 1e37f;
+    o.pixel = in.pixel;
+    o.contribution = in.contribution * refl * 1.0f;
+    *out = o;
+}
+
+/* ----------------------------------------------------------------------- */
+/* C API                                                                    */
+/* ----------------------------------------------------------------------- */
+extern "C" {
+
+orc_scene* orc_scene_new(const float* pos4, const float* nrm4, uint32_t V, const uint32_t* idx,
+                         uint32_t N, const rt_material* mats, uint32_t M, const uint32_t* map,
+                         const rt_lights* lights) {
+    orc_scene* s = new orc_scene();
+    s->V = V;
+    s->N = N;
+    s->pos.assign(pos4, pos4 + 4 * (size_t)V);
+    s->nrm.assign(nrm4, nrm4 + 4 * (size_t)V);
+    s->idx.assign(idx, idx + 3 * (size_t)N);
+    s->map.assign(map, map + (size_t)N);
+    s->mats.assign(mats, mats + M);
+    s->lights = *lights;
+    s->orig_id.resize(N);
+    for (uint32_t i = 0; i < N; ++i) s->orig_id[i] = i;
+    return s;
+}
+
+void orc_scene_free(orc_scene* s) { delete s; }
+
+int orc_set_positions(orc_scene* s, const float* pos4, const float* nrm4) {
+    std::memcpy(s->pos.data(), pos4, sizeof(float) * 4 * (size_t)s->V);
+    if (nrm4) std::memcpy(s->nrm.data(), nrm4, sizeof(float) * 4 * (size_t)s->V);
+    return 0;
+}
+
+/* Morton keys of the current triangle order (stages a2-a4). */
+int orc_morton_keys(orc_scene* s, int depth, uint32_t* keys, float* glo_out, float* ghi_out) {
+    if (depth < 1 || depth > 32 || s->N == 0) return -1;
+    const uint32_t N = s->N;
+    std::vector<float> lo((size_t)N * 3), hi((size_t)N * 3);
+    float glo[3] = {1e37f, 1e37f, 1e37f}, ghi[3] = {-1e37f, -1e37f, -1e37f};
+    for (uint32_t i = 0; i < N; ++i) {
+        prim_bbox(s, i, &lo[3 * (size_t)i], &hi[3 * (size_t)i]);
+        for (int c = 0; c < 3; ++c) {
+            glo[c] = std::fmin(glo[c], lo[3 * (size_t)i + c]);
+            ghi[c] = std::fmax(ghi[c], hi[3 * (size_t)i + c]);
+        }
+    }
+    for (uint32_t i = 0; i < N; ++i)
+        keys[i] = morton_encode(&lo[3 * (size_t)i], &hi[3 * (size_t)i], glo, ghi, depth);
+    if (glo_out) for (int c = 0; c < 3; ++c) glo_out[c] = glo[c];
+    if (ghi_out) for (int c = 0; c < 3; ++c) ghi_out[c] = ghi[c];
+    return 0;
+}
+
+int orc_sort_bitonic(const uint32_t* keys, uint32_t n, uint32_t* perm) {
+    return bitonic_sort(keys, n, perm);
+}
+
+/* Full build: bbox, bounds, Morton, sort (0 = stable, 1 = the reference's
+ * bitonic network), permute index buffer and material map in place, emit,
+ * refit. */
+int orc_build(orc_scene* s, int depth, int min_leaf, int sort_kind) {
+    if (depth < 1 || depth > 32 || min_leaf < 1 || min_leaf > 256 || s->N == 0) return -1;
+    const uint32_t N = s->N;
+    s->depth = depth;
+    s->min_leaf = min_leaf;
+    s->keys.resize(N);
+    if (orc_morton_keys(s, depth, s->keys.data(), nullptr, nullptr)) return -1;
+    s->perm.resize(N);
+    if (sort_kind == 1) {
+        if (bitonic_sort(s->keys.data(), N, s->perm.data())) return -1;
+    } else {
+        for (uint32_t i = 0; i < N; ++i) s->perm[i] = i;
+        std::stable_sort(s->perm.begin(), s->perm.end(),
+                         [&](uint32_t a, uint32_t b) { return s->keys[a] < s->keys[b]; });
+    }
+    s->sorted_keys.resize(N);
+    std::vector<uint32_t> idx2((size_t)N * 3), map2(N), orig2(N);
+    for (uint32_t i = 0; i < N; ++i) {
+        uint32_t o = s->perm[i];
+        s->sorted_keys[i] = s->keys[o];
+        idx2[3 * (size_t)i + 0] = s->idx[3 * (size_t)o + 0];
+        idx2[3 * (size_t)i + 1] = s->idx[3 * (size_t)o + 1];
+        idx2[3 * (size_t)i + 2] = s->idx[3 * (size_t)o + 2];
+        map2[i] = s->map[o];
+        orig2[i] = s->orig_id[o];
+    }
+    s->idx.swap(idx2);
+    s->map.swap(map2);
+    s->orig_id.swap(orig2);
+    s->nodes.clear();
+    s->nodes.reserve(2 * (size_t)N);
+    emit(s, 0, N, 0, 0);
+    refit(s);
+    s->built = true;
+    return 0;
+}
+
+/* refit_lbvh (bvh-builder.cpp:743-850): new AABBs, same topology and order. */
+int orc_refit(orc_scene* s) {
+    if (!s->built) return -1;
+    refit(s);
+    return 0;
+}
+
+int orc_get_sort(const orc_scene* s, uint32_t* keys, uint32_t* perm, uint32_t* sorted,
+                 uint32_t* orig_id) {
+    if (!s->built) return -1;
+    size_t n = s->N;
+    if (keys) std::memcpy(keys, s->keys.data(), 4 * n);
+    if (perm) std::memcpy(perm, s->perm.data(), 4 * n);
+    if (sorted) std::memcpy(sorted, s->sorted_keys.data(), 4 * n);
+    if (orig_id) std::memcpy(orig_id, s->orig_id.data(), 4 * n);
+    return 0;
+}
+
+int orc_get_buffers(const orc_scene* s, uint32_t* idx, uint32_t* map) {
+    if (idx) std::memcpy(idx, s->idx.data(), 12 * (size_t)s->N);
+    if (map) std::memcpy(map, s->map.data(), 4 * (size_t)s->N);
+    return 0;
+}
+
+int orc_export(const orc_scene* s, rt_canon_node* out, uint32_t cap, uint32_t* count) {
+    if (!s->built) return -1;
+    *count = (uint32_t)s->nodes.size();
+    if (!out) return 0;
+    if (cap < s->nodes.size()) return -1;
+    for (size_t k = 0; k < s->nodes.size(); ++k) {
+        const Node& nd = s->nodes[k];
+        rt_canon_node c;
+        std::memset(&c, 0, sizeof(c));
+        c.start = nd.start;
+        c.end = nd.end;
+        c.leaf = nd.leaf;
+        c.depth = nd.depth;
+        for (int i = 0; i < 3; ++i) {
+            c.lo[i] = nd.lo[i];
+            c.hi[i] = nd.hi[i];
+        }
+        out[k] = c;
+    }
+    return 0;
+}
+
+/* generate_primary_rays (primary-ray-generator.cl:27-103) for global ids
+ * [offset, offset + count). */
+int orc_gen_primary(const rt_camera* cam, int32_t width, int32_t height, int32_t quad_size,
+                    int32_t spp, const rt_pixel_sample* ps, size_t count, size_t offset,
+                    rt_sample* out) {
+    (void)spp;
+    rt_pixel_sample one = {0.f, 0.f, 1.f};
+    const int pixels = width * height;
+    const int bs = quad_size, ba = quad_size * quad_size;
+    const int xb = width / bs, yb = height / bs;
+    const int block_rays = xb * yb * ba;
+    const int right_rays = (width - xb * bs) * height;
+    for (size_t k = 0; k < count; ++k) {
+        int gid = (int)(offset + k);
+        int i = gid % pixels;
+        const rt_pixel_sample p = ps ? ps[gid / pixels] : one;
+        int x, y;
+        if (i < block_rays) {
+            int block = i / ba, yblk = block / xb, xblk = block % xb;
+            int bp = i % ba;
+            x = xblk * bs + bp % bs;
+            y = yblk * bs + bp / bs;
+        } else if (i < block_rays + right_rays) {
+            int sx = xb * bs, slab = width - sx, ri = i - block_rays;
+            x = sx + ri % slab;
+            y = ri / slab;
+        } else {
+            int sy = yb * bs, slab = height - sy, ti = i - (block_rays + right_rays);
+            x = ti / slab;
+            y = sy + ti % slab;
+        }
+        float xn = (0.5f + (float)x + p.ox) / (float)width;
+        float yn = (0.5f + (float)y + p.oy) / (float)height;
+        float a = xn * 2.0f - 1.0f, b = yn * 2.0f - 1.0f;
+        v3 d = add(add(ld3(cam->dir), muls(ld3(cam->right), a)), muls(ld3(cam->up), b));
+        d = normalize(d);
+        rt_sample& o = out[k];
+        std::memset(&o, 0, sizeof(o));
+        o.ray.ori[0] = cam->pos[0]; o.ray.ori[1] = cam->pos[1]; o.ray.ori[2] = cam->pos[2];
+        o.ray.dir[0] = d.x; o.ray.dir[1] = d.y; o.ray.dir[2] = d.z;
+        o.ray.inv_dir[0] = 1.0f / d.x;
+        o.ray.inv_dir[1] = 1.0f / d.y;
+        o.ray.inv_dir[2] = 1.0f / d.z;
+        o.ray.tmin = 0.0f;
+        o.ray.tmax = 1e36f;
+        o.pixel = width * y + x;
+        o.contribution = p.contribution;
+    }
+    return 0;
+}
+
+int orc_trace(const orc_scene* s, const rt_sample* smp, int32_t n, rt_hit* hits, int threads) {
+    if (!s->built) return -1;
+    parallel_for(n, threads, [&](int64_t i) {
+        Ray r = ray_of(smp[i]);
+        Best b = trace_ray(s, r);
+        complete(s, r, b, &hits[i]);
+    });
+    return 0;
+}
+
+int orc_shadow(const orc_scene* s, const rt_sample* smp, int32_t n, rt_hit* hits, int threads) {
+    if (!s->built) return -1;
+    (void)smp;
+    parallel_for(n, threads, [&](int64_t i) {
+        rt_hit& h = hits[i];
+        if (!h.hit) return;
+        v3 hp = ld3(h.hit_point);
+        uint8_t mask = 0;
+        for (int l = 0; l < s->lights.count; ++l)
+            if (light_occluded(s, s->lights.light[l], hp)) mask |= (uint8_t)(1u << l);
+        h.shadow_hit = mask;
+    });
+    return 0;
+}
+
+int orc_shade(const orc_scene* s, const rt_sample* smp, const rt_hit* hits, int32_t n,
+              uint32_t* image, int threads) {
+    /* one sample per pixel per launch, so pixel writes never collide */
+    parallel_for(n, threads, [&](int64_t i) { shade_one(s, smp[i], hits[i], image); });
+    return 0;
+}
+
+/* mark + exclusive scan + emit (reflection rays only), stable order. */
+int orc_gen_secondary(const orc_scene* s, const rt_sample* in, int32_t n, const rt_hit* hits,
+                      rt_sample* out, int32_t max_out, int32_t* count) {
+    int32_t k = 0;
+    for (int32_t i = 0; i < n; ++i) {
+        if (!hits[i].hit) continue;
+        float refl = s->mats[s->map[hits[i].id]].reflectiveness;
+        if (!(refl > 0.0f)) continue;
+        if (k < max_out) reflect_ray(in[i], hits[i], refl, &out[k]);
+        ++k;
+    }
+    *count = std::min(k, max_out);
+    return 0;
+}
+
+/* copy (framebuffer.cl:30-54) + UNORM8 conversion (round to nearest even,
+ * saturate), alpha = 255. */
+int orc_fb_copy(const uint32_t* image, uint8_t* rgba, size_t pixels) {
+    const float inv = 1.0f / 1e6f;
+    for (size_t p = 0; p < pixels; ++p) {
+        for (int c = 0; c < 3; ++c) {
+            float v = (float)image[3 * p + c] * inv;
+            float x = std::nearbyint(clamp01(v) * 255.0f);
+            rgba[4 * p + c] = (uint8_t)x;
+        }
+        rgba[4 * p + 3] = 255;
+    }
+    return 0;
+}
+
+/* Renderer::render_to_framebuffer (renderer.cpp:113-214) restricted to
+ * global sample ids [offset, offset + count) in tiles of tile_size.
+ * image: 3 uint32 per pixel, accumulated.  stats: accumulated. */
+int orc_render(const orc_scene* s, const rt_camera* cam, int32_t width, int32_t height,
+               int32_t max_bounces, size_t offset, size_t count, size_t tile_size,
+               uint32_t* image, rt_render_stats* stats, int threads) {
+    if (!s->built) return -1;
+    if (threads <= 0) threads = (int)hw_threads();
+    if (tile_size == 0) tile_size = 1u << 18;
+    std::vector<rt_sample> a(tile_size), b(tile_size);
+    std::vector<rt_hit> h(tile_size);
+    for (size_t off = offset; off < offset + count; off += tile_size) {
+        size_t cur = std::min(tile_size, offset + count - off);
+        rt_sample* rin = a.data();
+        rt_sample* rout = b.data();
+        orc_gen_primary(cam, width, height, 32, 1, nullptr, cur, off, rin);
+        std::memset(h.data(), 0, sizeof(rt_hit) * cur);
+        orc_trace(s, rin, (int32_t)cur, h.data(), threads);
+        orc_shadow(s, rin, (int32_t)cur, h.data(), threads);
+        orc_shade(s, rin, h.data(), (int32_t)cur, image, threads);
+        if (stats) {
+            stats->primary_rays += cur;
+            for (size_t i = 0; i < cur; ++i)
+                if (h[i].hit) {
+                    stats->hits++;
+                    stats->shadow_rays += (uint64_t)s->lights.count;
+                }
+        }
+        int32_t sec = (int32_t)cur;
+        for (int bounce = 0; bounce < max_bounces; ++bounce) {
+            int32_t nout = 0;
+            orc_gen_secondary(s, rin, sec, h.data(), rout, (int32_t)tile_size, &nout);
+            std::swap(rin, rout);
+            sec = nout;
+            if (!sec) break;
+            std::memset(h.data(), 0, sizeof(rt_hit) * (size_t)sec);
+            orc_trace(s, rin, sec, h.data(), threads);
+            orc_shadow(s, rin, sec, h.data(), threads);
+            orc_shade(s, rin, h.data(), sec, image, threads);
+            if (stats) {
+                stats->secondary_rays += (uint64_t)sec;
+                for (int32_t i = 0; i < sec; ++i)
+                    if (h[i].hit) {
+                        stats->hits++;
+                        stats->shadow_rays += (uint64_t)s->lights.count;
+                    }
+            }
+        }
+    }
+    return 0;
+}
+
+/* FP64 brute-force closest hit over all triangles (ray subset); returns the
+ * triangle id at upload (orig_id) or -1, and t. */
+int orc_fp64_closest(const orc_scene* s, const rt_sample* smp, int32_t n, int32_t* id_out,
+                     double* t_out, int threads) {
+    if (threads <= 0) threads = (int)hw_threads();
+    const uint32_t N = s->N;
+    parallel_for(n, threads, [&](int64_t k) {
+        const rt_sample& sm = smp[k];
+        double o[3] = {sm.ray.ori[0], sm.ray.ori[1], sm.ray.ori[2]};
+        double d[3] = {sm.ray.dir[0], sm.ray.dir[1], sm.ray.dir[2]};
+        double best = (double)sm.ray.tmax;
+        int32_t bid = -1;
+        for (uint32_t i = 0; i < N; ++i) {
+            const uint32_t* ix = &s->idx[3 * (size_t)i];
+            double v0[3], e1[3], e2[3];
+            for (int c = 0; c < 3; ++c) {
+                v0[c] = s->pos[4 * (size_t)ix[0] + c];
+                e1[c] = (double)s->pos[4 * (size_t)ix[1] + c] - v0[c];
+                e2[c] = (double)s->pos[4 * (size_t)ix[2] + c] - v0[c];
+            }
+            double h[3] = {d[1] * e2[2] - d[2] * e2[1], d[2] * e2[0] - d[0] * e2[2],
+                           d[0] * e2[1] - d[1] * e2[0]};
+            double a = e1[0] * h[0] + e1[1] * h[1] + e1[2] * h[2];
+            if (a == 0.0) continue;
+            double f = 1.0 / a;
+            double sv[3] = {o[0] - v0[0], o[1] - v0[1], o[2] - v0[2]};
+            double u = f * (sv[0] * h[0] + sv[1] * h[1] + sv[2] * h[2]);
+            if (u < 0.0 || u > 1.0) continue;
+            double q[3] = {sv[1] * e1[2] - sv[2] * e1[1], sv[2] * e1[0] - sv[0] * e1[2],
+                           sv[0] * e1[1] - sv[1] * e1[0]};
+            double v = f * (d[0] * q[0] + d[1] * q[1] + d[2] * q[2]);
+            if (v < 0.0 || u + v > 1.0) continue;
+            double t = f * (e2[0] * q[0] + e2[1] * q[1] + e2[2] * q[2]);
+            if (t >= (double)sm.ray.tmin && t <= best) {
+                best = t;
+                bid = (int32_t)s->orig_id[i];
+            }
+        }
+        id_out[k] = bid;
+        t_out[k] = best;
+    });
+    return 0;
+}
+
+/* FP64 t of a given triangle (id at upload) along a ray, or NaN on a miss. */
+int orc_fp64_t_of(const orc_scene* s, const rt_sample* smp, int32_t n, const int32_t* tri_orig,
+                  double* t_out) {
+    std::vector<uint32_t> slot(s->N);
+    for (uint32_t i = 0; i < s->N; ++i) slot[s->orig_id[i]] = i;
+    for (int32_t k = 0; k < n; ++k) {
+        t_out[k] = NAN;
+        if (tri_orig[k] < 0) continue;
+        const uint32_t* ix = &s->idx[3 * (size_t)slot[tri_orig[k]]];
+        const rt_sample& sm = smp[k];
+        double o[3] = {sm.ray.ori[0], sm.ray.ori[1], sm.ray.ori[2]};
+        double d[3] = {sm.ray.dir[0], sm.ray.dir[1], sm.ray.dir[2]};
+        double v0[3], e1[3], e2[3];
+        for (int c = 0; c < 3; ++c) {
+            v0[c] = s->pos[4 * (size_t)ix[0] + c];
+            e1[c] = (double)s->pos[4 * (size_t)ix[1] + c] - v0[c];
+            e2[c] = (double)s->pos[4 * (size_t)ix[2] + c] - v0[c];
+        }
+        double h[3] = {d[1] * e2[2] - d[2] * e2[1], d[2] * e2[0] - d[0] * e2[2],
+                       d[0] * e2[1] - d[1] * e2[0]};
+        double a = e1[0] * h[0] + e1[1] * h[1] + e1[2] * h[2];
+        if (a == 0.0) continue;
+        double f = 1.0 / a;
+        double sv[3] = {o[0] - v0[0], o[1] - v0[1], o[2] - v0[2]};
+        double q[3] = {sv[1] * e1[2] - sv[2] * e1[1], sv[2] * e1[0] - sv[0] * e1[2],
+                       sv[0] * e1[1] - sv[1] * e1[0]};
+        t_out[k] = f * (e2[0] * q[0] + e2[1] * q[1] + e2[2] * q[2]);
+    }
+    return 0;
+}
+
+}  /* extern "C" */

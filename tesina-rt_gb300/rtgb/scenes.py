@@ -1,0 +1,304 @@
+"""Seeded synthetic scenes for the Whitted-ray-tracer workloads.
+
+The reference's own benchmark scenes are OBJ files that are not part of its
+repository; these generators stand in for them with the shapes, sizes and
+value distributions of the five workloads:
+
+- ``soup``: random triangle soup (10,000 triangles, centroids U[-1,1]^3,
+  vertex offsets N(0, 0.03) per axis, 20% mirrors with reflectance 0.5, the
+  rest Lambertian with albedo U[0.2, 0.9]^3, one point light at (0, 4, -2)).
+- ``terrain``: an fBm value-noise heightfield (4 octaves, amplitude 1,
+  lacunarity 2, gain 0.5) with mirror UV spheres (32 x 16 segments, 960
+  triangles each) scattered above it; heights animated per frame by
+  0.1 * sin(x + t) with t = 0.1 * frame.
+
+All geometry is float32; the vertex normal of a soup triangle is its face
+normal, terrain normals come from central differences of the height field,
+sphere normals are radial.
+"""
+import math
+
+import numpy as np
+
+from . import abi
+
+MAT_MIRROR_SOUP = dict(diffuse=(0.0, 0.0, 0.0), reflectiveness=0.5)
+
+
+class Scene:
+    """Host scene in the C ABI's data model (see rt_scene_desc)."""
+
+    def __init__(self, pos4, nrm4, idx, mats, mat_map, lights):
+        self.pos4 = np.ascontiguousarray(pos4, dtype=np.float32)
+        self.nrm4 = np.ascontiguousarray(nrm4, dtype=np.float32)
+        self.idx = np.ascontiguousarray(idx, dtype=np.uint32).reshape(-1, 3)
+        self.mats = np.ascontiguousarray(mats)
+        self.mat_map = np.ascontiguousarray(mat_map, dtype=np.uint32)
+        self.lights = lights
+        assert self.mats.dtype == abi.MATERIAL_DTYPE
+        assert self.pos4.shape == self.nrm4.shape and self.pos4.shape[1] == 4
+        assert self.mat_map.shape[0] == self.idx.shape[0]
+
+    @property
+    def n_tris(self):
+        return self.idx.shape[0]
+
+    @property
+    def n_verts(self):
+        return self.pos4.shape[0]
+
+
+def _materials(n):
+    m = np.zeros(n, dtype=abi.MATERIAL_DTYPE)
+    m["texture"] = -1
+    return m
+
+
+def _normalize(v):
+    v = v.astype(np.float32)
+    n = np.sqrt((v * v).sum(axis=-1, keepdims=True)).astype(np.float32)
+    n[n == 0] = 1
+    return (v / n).astype(np.float32)
+
+
+def _f4(v3):
+    out = np.zeros((v3.shape[0], 4), dtype=np.float32)
+    out[:, :3] = v3
+    return out
+
+
+def soup(n_tris=10000, seed=0, mirror_frac=0.2, offset_sigma=0.03,
+         light_pos=(0.0, 4.0, -2.0), ambient=0.1):
+    """Random triangle soup (the small plain workload and the batched scenes)."""
+    rng = np.random.default_rng(seed)
+    c = rng.uniform(-1.0, 1.0, size=(n_tris, 1, 3)).astype(np.float32)
+    off = rng.normal(0.0, offset_sigma, size=(n_tris, 3, 3)).astype(np.float32)
+    v = (c + off).astype(np.float32)                         # (N, 3 verts, 3)
+    fn = _normalize(np.cross(v[:, 1] - v[:, 0], v[:, 2] - v[:, 0]))
+    pos = _f4(v.reshape(-1, 3))
+    nrm = _f4(np.repeat(fn, 3, axis=0))
+    idx = np.arange(3 * n_tris, dtype=np.uint32).reshape(-1, 3)
+    mirror = rng.random(n_tris) < mirror_frac
+    albedo = rng.uniform(0.2, 0.9, size=(n_tris, 3)).astype(np.float32)
+    mats = _materials(n_tris + 1)
+    mats["reflectiveness"][0] = MAT_MIRROR_SOUP["reflectiveness"]
+    mats["diffuse"][1:, :3] = albedo
+    mat_map = np.where(mirror, 0, np.arange(1, n_tris + 1)).astype(np.uint32)
+    lights = abi.make_lights((ambient,) * 3, [dict(type=abi.RT_POINT_L, pos=light_pos,
+                                                   color=(1.0, 1.0, 1.0))])
+    return Scene(pos, nrm, idx, mats, mat_map, lights)
+
+
+# ---------------------------------------------------------------------------
+# value-noise fBm
+# ---------------------------------------------------------------------------
+def _hash(ix, iz, octave, seed):
+    """32-bit integer hash of a lattice point -> float32 in [-1, 1)."""
+    h = (ix.astype(np.uint32) * np.uint32(0x8DA6B343)) ^ \
+        (iz.astype(np.uint32) * np.uint32(0xD8163841)) ^ \
+        np.uint32((octave * 0x2545F491 + seed * 0x9E3779B9) & 0xFFFFFFFF)
+    h ^= h >> np.uint32(16)
+    h *= np.uint32(0x7FEB352D)
+    h ^= h >> np.uint32(15)
+    h *= np.uint32(0x846CA68B)
+    h ^= h >> np.uint32(16)
+    return (h >> np.uint32(8)).astype(np.float32) * np.float32(2.0 / (1 << 24)) - np.float32(1.0)
+
+
+def _value_noise(x, z, octave, seed):
+    fx, fz = np.floor(x), np.floor(z)
+    ix, iz = fx.astype(np.int64), fz.astype(np.int64)
+    tx, tz = (x - fx).astype(np.float32), (z - fz).astype(np.float32)
+    sx = tx * tx * (3 - 2 * tx)
+    sz = tz * tz * (3 - 2 * tz)
+    a = _hash(ix, iz, octave, seed)
+    b = _hash(ix + 1, iz, octave, seed)
+    c = _hash(ix, iz + 1, octave, seed)
+    d = _hash(ix + 1, iz + 1, octave, seed)
+    return (a + (b - a) * sx) * (1 - sz) + (c + (d - c) * sx) * sz
+
+
+def fbm(x, z, seed=0, octaves=4, amplitude=1.0, lacunarity=2.0, gain=0.5, base_freq=0.5):
+    """fBm of value noise; base_freq lattice cells per unit (documented choice)."""
+    h = np.zeros(np.broadcast(x, z).shape, dtype=np.float32)
+    amp, freq = amplitude, base_freq
+    for o in range(octaves):
+        h += np.float32(amp) * _value_noise(x * freq, z * freq, o, seed)
+        amp *= gain
+        freq *= lacunarity
+    return h.astype(np.float32)
+
+
+def _uv_sphere(center, radius, seg=32, rings=16):
+    """UV sphere without degenerate pole triangles: seg*(2*(rings-1)) tris."""
+    cx, cy, cz = center
+    verts = [(0.0, 1.0, 0.0)]
+    for r in range(1, rings):
+        th = math.pi * r / rings
+        for s in range(seg):
+            ph = 2 * math.pi * s / seg
+            verts.append((math.sin(th) * math.cos(ph), math.cos(th), math.sin(th) * math.sin(ph)))
+    verts.append((0.0, -1.0, 0.0))
+    unit = np.array(verts, dtype=np.float32)
+    tris = []
+    for s in range(seg):                                   # top cap
+        tris.append((0, 1 + s, 1 + (s + 1) % seg))
+    for r in range(rings - 2):                             # bands
+        a0, b0 = 1 + r * seg, 1 + (r + 1) * seg
+        for s in range(seg):
+            s1 = (s + 1) % seg
+            tris.append((a0 + s, b0 + s, b0 + s1))
+            tris.append((a0 + s, b0 + s1, a0 + s1))
+    last = len(verts) - 1                                  # bottom cap
+    base = 1 + (rings - 2) * seg
+    for s in range(seg):
+        tris.append((base + s, last, base + (s + 1) % seg))
+    pos = (unit * np.float32(radius) + np.array(center, dtype=np.float32)).astype(np.float32)
+    return pos, unit, np.array(tris, dtype=np.uint32)
+
+
+SPHERE_TEMPLATE = {}
+
+
+def _sphere_template(seg, rings):
+    key = (seg, rings)
+    if key not in SPHERE_TEMPLATE:
+        _, unit, tris = _uv_sphere((0, 0, 0), 1.0, seg, rings)
+        SPHERE_TEMPLATE[key] = (unit, tris)
+    return SPHERE_TEMPLATE[key]
+
+
+class Terrain:
+    """fBm heightfield plus mirror spheres; ``frame(f)`` gives animated vertices."""
+
+    def __init__(self, nx=1024, nz=512, extent=(-8.0, 8.0, -4.0, 4.0), n_spheres=200,
+                 seed=1, lights=None, ambient=0.1, sphere_seg=(32, 16)):
+        self.nx, self.nz = nx, nz
+        x0, x1, z0, z1 = extent
+        xs = np.linspace(x0, x1, nx + 1, dtype=np.float32)
+        zs = np.linspace(z0, z1, nz + 1, dtype=np.float32)
+        self.gx, self.gz = np.meshgrid(xs, zs)               # (nz+1, nx+1)
+        self.h0 = fbm(self.gx, self.gz, seed=seed)
+        self.dx = (x1 - x0) / nx
+        self.dz = (z1 - z0) / nz
+        # grid triangles, 2 per cell
+        j, i = np.meshgrid(np.arange(nz, dtype=np.uint32), np.arange(nx, dtype=np.uint32),
+                           indexing="ij")
+        v00 = (j * (nx + 1) + i).ravel()
+        v10 = v00 + 1
+        v01 = v00 + (nx + 1)
+        v11 = v01 + 1
+        grid_tris = np.empty((2 * nx * nz, 3), dtype=np.uint32)
+        grid_tris[0::2] = np.stack([v00, v10, v11], axis=1)
+        grid_tris[1::2] = np.stack([v00, v11, v01], axis=1)
+        self.n_grid_verts = (nx + 1) * (nz + 1)
+        # spheres
+        rng = np.random.default_rng(seed + 1000)
+        unit, stris = _sphere_template(*sphere_seg)
+        radii = rng.uniform(0.1, 0.5, n_spheres).astype(np.float32)
+        cx = rng.uniform(x0 + 0.5, x1 - 0.5, n_spheres).astype(np.float32)
+        cz = rng.uniform(z0 + 0.5, z1 - 0.5, n_spheres).astype(np.float32)
+        lift = rng.uniform(0.2, 1.0, n_spheres).astype(np.float32)
+        cy = fbm(cx, cz, seed=seed) + radii + np.float32(0.1) + lift
+        centers = np.stack([cx, cy, cz], axis=1).astype(np.float32)
+        nv = unit.shape[0]
+        sp_pos = (unit[None] * radii[:, None, None] + centers[:, None, :]).reshape(-1, 3)
+        sp_nrm = np.broadcast_to(unit[None], (n_spheres, nv, 3)).reshape(-1, 3)
+        sp_tris = (stris[None] + (self.n_grid_verts + nv * np.arange(n_spheres,
+                                                                    dtype=np.uint32))[:, None, None])
+        self.sp_pos = _f4(sp_pos.astype(np.float32))
+        self.sp_nrm = _f4(sp_nrm.astype(np.float32))
+        self.idx = np.concatenate([grid_tris, sp_tris.reshape(-1, 3)]).astype(np.uint32)
+        n_grid_tris = grid_tris.shape[0]
+        mats = _materials(2)
+        mats["diffuse"][0, :3] = (0.55, 0.5, 0.4)          # terrain, Lambertian
+        mats["diffuse"][1, :3] = (0.1, 0.1, 0.1)           # mirror spheres
+        mats["reflectiveness"][1] = 0.8
+        self.mats = mats
+        self.mat_map = np.concatenate([np.zeros(n_grid_tris, np.uint32),
+                                       np.ones(self.idx.shape[0] - n_grid_tris, np.uint32)])
+        if lights is None:
+            lights = [dict(type=abi.RT_POINT_L, pos=(-4.0, 6.0, -3.0), color=(0.7, 0.7, 0.7)),
+                      dict(type=abi.RT_POINT_L, pos=(5.0, 5.0, 2.0), color=(0.5, 0.5, 0.6))]
+        self.lights = abi.make_lights((ambient,) * 3, lights)
+
+    @property
+    def n_tris(self):
+        return self.idx.shape[0]
+
+    def heights(self, f):
+        t = np.float32(0.1 * f)
+        return (self.h0 + np.float32(0.1) * np.sin(self.gx + t)).astype(np.float32)
+
+    def frame_vertices(self, f):
+        """(pos4, nrm4) of frame f: terrain heights animated, spheres fixed."""
+        h = self.heights(f)
+        gxs = np.gradient(h, self.dx, axis=1).astype(np.float32)
+        gzs = np.gradient(h, self.dz, axis=0).astype(np.float32)
+        n = _normalize(np.stack([-gxs, np.ones_like(h), -gzs], axis=-1).reshape(-1, 3))
+        gp = np.stack([self.gx, h, self.gz], axis=-1).reshape(-1, 3)
+        pos = np.concatenate([_f4(gp), self.sp_pos])
+        nrm = np.concatenate([_f4(n), self.sp_nrm])
+        return pos, nrm
+
+    def scene(self, f=0):
+        pos, nrm = self.frame_vertices(f)
+        return Scene(pos, nrm, self.idx, self.mats, self.mat_map, self.lights)
+
+
+def camera(pos, target, up=(0.0, 1.0, 0.0), fov_deg=60.0, aspect=1.0, right_handed=False):
+    """Camera::set (src/rt/camera.cpp:31-59) in float32: returns abi.Camera."""
+    f32 = np.float32
+    p = np.array(pos, dtype=f32)
+    d = np.array(target, dtype=f32) - p
+    d = (d / np.sqrt(f32((d * d).sum()))).astype(f32)
+    u = np.array(up, dtype=f32)
+    right = np.cross(d, u) if right_handed else np.cross(u, d)
+    upv = np.cross(right, d) if right_handed else np.cross(d, right)
+    ph = f32(math.tan(math.radians(fov_deg) * 0.5))
+    right = (right * (ph * f32(aspect)) / np.sqrt(f32((right * right).sum()))).astype(f32)
+    upv = (upv * ph / np.sqrt(f32((upv * upv).sum()))).astype(f32)
+    cam = abi.Camera()
+    cam.pos[:3] = [float(v) for v in p]
+    cam.dir[:3] = [float(v) for v in d]
+    cam.right[:3] = [float(v) for v in right]
+    cam.up[:3] = [float(v) for v in upv]
+    return cam
+
+
+# ---------------------------------------------------------------------------
+# named workloads
+# ---------------------------------------------------------------------------
+def workload_small(seed=0):
+    """Plain method, small: 10k-triangle soup, 512x512, depth 3, 1 point light."""
+    sc = soup(10000, seed=seed)
+    cam = camera((0.0, 0.0, -4.0), (0.0, 0.0, 0.0), fov_deg=60.0, aspect=1.0)
+    return dict(name="soup10k_512x512_d3", scene=sc, camera=cam, width=512, height=512,
+                max_bounces=3, depth=30, min_leaf=1)
+
+
+def workload_mid(seed=1):
+    """Plain method, mid scale: 1024x512-cell fBm field + 200 mirror spheres,
+    1920x1080, 2 point lights, depth 4, full LBVH rebuild per frame."""
+    ter = Terrain(1024, 512, n_spheres=200, seed=seed)
+    cam = camera((0.0, 4.0, -10.0), (0.0, 0.0, 0.0), fov_deg=60.0, aspect=1920 / 1080)
+    return dict(name="terrain1M_1920x1080_d4", terrain=ter, camera=cam, width=1920,
+                height=1080, max_bounces=4, depth=30, min_leaf=1)
+
+
+def workload_stress(seed=2):
+    """Plain method, stress: 4096x2048-cell field + 1000 spheres, 3840x2160,
+    3 point lights, depth 6, 8 camera poses on a radius-10 sphere."""
+    lights = [dict(type=abi.RT_POINT_L, pos=(-4.0, 6.0, -3.0), color=(0.6, 0.6, 0.6)),
+              dict(type=abi.RT_POINT_L, pos=(5.0, 5.0, 2.0), color=(0.4, 0.4, 0.5)),
+              dict(type=abi.RT_POINT_L, pos=(0.0, 8.0, 6.0), color=(0.3, 0.3, 0.3))]
+    ter = Terrain(4096, 2048, n_spheres=1000, seed=seed, lights=lights)
+    rng = np.random.default_rng(seed + 7)
+    poses = []
+    for _ in range(8):
+        v = rng.normal(size=3)
+        v[1] = abs(v[1]) + 0.2          # above the field
+        v = v / np.linalg.norm(v) * 10.0
+        poses.append(camera(tuple(v), (0.0, 0.0, 0.0), fov_deg=60.0, aspect=3840 / 2160))
+    return dict(name="terrain17M_3840x2160_d6", terrain=ter, cameras=poses, width=3840,
+                height=2160, max_bounces=6, depth=30, min_leaf=1)
