@@ -21,6 +21,12 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#if defined(__GNUC__)
+#define RT_API __attribute__((visibility("default")))
+#else
+#define RT_API
+#endif
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -96,7 +102,7 @@ typedef struct rt_camera {
 
 /* Mirror of Camera::set (src/rt/camera.cpp:31-59).  fov is the vertical full
  * angle in radians, aspect = width / height. */
-int32_t rt_camera_set(rt_camera* cam, const float pos[3], const float dir[3],
+RT_API int32_t rt_camera_set(rt_camera* cam, const float pos[3], const float dir[3],
                       const float up[3], float fov, float aspect,
                       int32_t right_handed);
 
@@ -188,62 +194,65 @@ typedef void*            rt_stream;   /* a cudaStream_t */
 /* Context, errors, streams, buffers (replaces DeviceInterface/DeviceMemory, */
 /* include/gpu/interface.hpp:20-80, include/gpu/memory.hpp)                 */
 /* ------------------------------------------------------------------------ */
-const char* rt_last_error(void);
-int32_t rt_init(rt_ctx** ctx, int32_t device);
-int32_t rt_shutdown(rt_ctx* ctx);
+RT_API const char* rt_last_error(void);
+RT_API int32_t rt_init(rt_ctx** ctx, int32_t device);
+RT_API int32_t rt_shutdown(rt_ctx* ctx);
 /* Reads (and clears) the device status word: RT_DEV_* bits. */
-int32_t rt_device_status(rt_ctx* ctx, uint32_t* bits);
-int32_t rt_stream_create(rt_ctx* ctx, rt_stream* stream);
-int32_t rt_stream_destroy(rt_ctx* ctx, rt_stream stream);
-int32_t rt_stream_sync(rt_ctx* ctx, rt_stream stream);
-int32_t rt_buf_alloc(rt_ctx* ctx, size_t bytes, void** d_ptr);
-int32_t rt_buf_free(rt_ctx* ctx, void* d_ptr);
-int32_t rt_buf_write(rt_ctx* ctx, void* d_dst, const void* h_src, size_t bytes, rt_stream s);
-int32_t rt_buf_read(rt_ctx* ctx, void* h_dst, const void* d_src, size_t bytes, rt_stream s);
-int32_t rt_buf_copy(rt_ctx* ctx, void* d_dst, const void* d_src, size_t bytes, rt_stream s);
-int32_t rt_buf_zero(rt_ctx* ctx, void* d_dst, size_t bytes, rt_stream s);
+RT_API int32_t rt_device_status(rt_ctx* ctx, uint32_t* bits);
+RT_API int32_t rt_stream_create(rt_ctx* ctx, rt_stream* stream);
+RT_API int32_t rt_stream_destroy(rt_ctx* ctx, rt_stream stream);
+RT_API int32_t rt_stream_sync(rt_ctx* ctx, rt_stream stream);
+RT_API int32_t rt_buf_alloc(rt_ctx* ctx, size_t bytes, void** d_ptr);
+RT_API int32_t rt_buf_free(rt_ctx* ctx, void* d_ptr);
+RT_API int32_t rt_buf_write(rt_ctx* ctx, void* d_dst, const void* h_src, size_t bytes, rt_stream s);
+RT_API int32_t rt_buf_read(rt_ctx* ctx, void* h_dst, const void* d_src, size_t bytes, rt_stream s);
+RT_API int32_t rt_buf_copy(rt_ctx* ctx, void* d_dst, const void* d_src, size_t bytes, rt_stream s);
+RT_API int32_t rt_buf_zero(rt_ctx* ctx, void* d_dst, size_t bytes, rt_stream s);
 
 /* ------------------------------------------------------------------------ */
 /* Scene (replaces Scene::transfer_aggregate_mesh_to_device,                */
 /* src/rt/scene.cpp:236-321, and the buffer accessors scene.hpp:125-133)    */
 /* ------------------------------------------------------------------------ */
-int32_t rt_scene_create(rt_ctx* ctx, rt_scene** scene);
-int32_t rt_scene_destroy(rt_ctx* ctx, rt_scene* scene);
-int32_t rt_scene_upload(rt_ctx* ctx, rt_scene* scene, const rt_scene_desc* desc, rt_stream s);
+RT_API int32_t rt_scene_create(rt_ctx* ctx, rt_scene** scene);
+RT_API int32_t rt_scene_destroy(rt_ctx* ctx, rt_scene* scene);
+RT_API int32_t rt_scene_upload(rt_ctx* ctx, rt_scene* scene, const rt_scene_desc* desc, rt_stream s);
 /* Replace vertex positions/normals (float4 each, host memory) keeping topology;
  * analogue of Scene::update_aggregate_mesh_vertices (scene.cpp:967-984). */
-int32_t rt_scene_update_vertices(rt_ctx* ctx, rt_scene* scene, const float* h_pos4,
+RT_API int32_t rt_scene_update_vertices(rt_ctx* ctx, rt_scene* scene, const float* h_pos4,
                                  const float* h_nrm4, uint32_t vertex_count, rt_stream s);
 /* Same, from device memory. */
-int32_t rt_scene_update_vertices_device(rt_ctx* ctx, rt_scene* scene, const float* d_pos4,
+RT_API int32_t rt_scene_update_vertices_device(rt_ctx* ctx, rt_scene* scene, const float* d_pos4,
                                         const float* d_nrm4, uint32_t vertex_count, rt_stream s);
-int32_t rt_scene_set_lights(rt_ctx* ctx, rt_scene* scene, const rt_lights* lights);
+RT_API int32_t rt_scene_set_lights(rt_ctx* ctx, rt_scene* scene, const rt_lights* lights);
 /* Device buffers of the scene (reference: Scene::index_mem(), material_map_mem()).
  * After a build, indices and material map are permuted into sorted order, as
  * the reference permutes them in place (bvh-builder.cpp:470-527). */
-int32_t rt_scene_buffers(rt_ctx* ctx, rt_scene* scene, uint32_t** d_indices,
+RT_API int32_t rt_scene_buffers(rt_ctx* ctx, rt_scene* scene, uint32_t** d_indices,
                          uint32_t** d_material_map, float** d_positions,
                          float** d_normals, uint32_t* triangle_count);
 /* Host copies of the per-build arrays used for parity:
  * unsorted Morton keys (per original triangle), the sort permutation
  * (sorted slot -> original triangle) and the sorted keys.  Any may be NULL. */
-int32_t rt_scene_read_sort(rt_ctx* ctx, rt_scene* scene, uint32_t* h_keys,
+RT_API int32_t rt_scene_read_sort(rt_ctx* ctx, rt_scene* scene, uint32_t* h_keys,
                            uint32_t* h_perm, uint32_t* h_sorted_keys);
+/* Triangle id at upload of each triangle in the current order (maps the
+ * sorted-order ids of rt_hit.id back to the caller's triangles). */
+RT_API int32_t rt_scene_read_orig(rt_ctx* ctx, rt_scene* scene, uint32_t* h_orig);
 
 /* ------------------------------------------------------------------------ */
 /* LBVH (replaces BVHBuilder, include/rt/bvh-builder.hpp:16-28)             */
 /* ------------------------------------------------------------------------ */
 /* BVHBuilder::build_lbvh (src/rt/bvh-builder.cpp:201-741). */
-int32_t rt_bvh_build_lbvh(rt_ctx* ctx, rt_scene* scene, const rt_bvh_cfg* cfg, rt_stream s);
+RT_API int32_t rt_bvh_build_lbvh(rt_ctx* ctx, rt_scene* scene, const rt_bvh_cfg* cfg, rt_stream s);
 /* BVHBuilder::refit_lbvh (src/rt/bvh-builder.cpp:743-850): recompute AABBs on
  * the existing topology and triangle order. */
-int32_t rt_bvh_refit_lbvh(rt_ctx* ctx, rt_scene* scene, rt_stream s);
+RT_API int32_t rt_bvh_refit_lbvh(rt_ctx* ctx, rt_scene* scene, rt_stream s);
 /* Canonical pre-order tree (synchronous).  *count receives the node count;
  * pass out == NULL to query it. */
-int32_t rt_bvh_export(rt_ctx* ctx, rt_scene* scene, rt_canon_node* out,
+RT_API int32_t rt_bvh_export(rt_ctx* ctx, rt_scene* scene, rt_canon_node* out,
                       uint32_t capacity, uint32_t* count);
 /* Device time of the last build / refit in milliseconds (CUDA events). */
-int32_t rt_bvh_last_time_ms(rt_ctx* ctx, rt_scene* scene, float* ms);
+RT_API int32_t rt_bvh_last_time_ms(rt_ctx* ctx, rt_scene* scene, float* ms);
 
 /* ------------------------------------------------------------------------ */
 /* Stage-wise pipeline on reference-layout buffers (drop-in for the         */
@@ -254,33 +263,33 @@ int32_t rt_bvh_last_time_ms(rt_ctx* ctx, rt_scene* scene, float* ms);
  * kernel primary-ray-generator.cl:27-103). Rays for global ids
  * [offset, offset+ray_count) of a w*h*spp image, quad_size pixel blocks.
  * d_pixel_samples may be NULL (one sample {0,0,1}). */
-int32_t rt_gen_primary(rt_ctx* ctx, const rt_camera* cam, int32_t width, int32_t height,
+RT_API int32_t rt_gen_primary(rt_ctx* ctx, const rt_camera* cam, int32_t width, int32_t height,
                        int32_t quad_size, int32_t spp, const rt_pixel_sample* d_pixel_samples,
                        size_t ray_count, size_t offset, rt_sample* d_samples, rt_stream s);
 /* Tracer::trace (src/rt/tracer.cpp:140-269, kernel trace-bvh.cl:465-481). */
-int32_t rt_trace(rt_ctx* ctx, rt_scene* scene, const rt_sample* d_samples, int32_t ray_count,
+RT_API int32_t rt_trace(rt_ctx* ctx, rt_scene* scene, const rt_sample* d_samples, int32_t ray_count,
                  rt_hit* d_hits, int32_t secondary, rt_stream s);
 /* Tracer::shadow_trace (src/rt/tracer.cpp:273-352, kernel
  * shadow-trace-bvh.cl:375-418); one shadow ray per light, result bitmask in
  * rt_hit.shadow_hit. */
-int32_t rt_shadow_trace(rt_ctx* ctx, rt_scene* scene, const rt_sample* d_samples,
+RT_API int32_t rt_shadow_trace(rt_ctx* ctx, rt_scene* scene, const rt_sample* d_samples,
                         int32_t ray_count, rt_hit* d_hits, int32_t secondary, rt_stream s);
 /* RayShader::shade (src/rt/ray-shader.cpp:32-154, kernel ray-shader.cl:116-459).
  * d_image_rgb: 3 uint32 per pixel, fixed point x1e6, accumulated with atomics. */
-int32_t rt_shade(rt_ctx* ctx, rt_scene* scene, const rt_sample* d_samples,
+RT_API int32_t rt_shade(rt_ctx* ctx, rt_scene* scene, const rt_sample* d_samples,
                  const rt_hit* d_hits, int32_t ray_count, uint32_t* d_image_rgb,
                  int32_t primary, rt_stream s);
 /* SecondaryRayGenerator::generate (src/rt/secondary-ray-generator.cpp:57-244,
  * kernels secondary-ray-generator.cl:184-326): reflection rays, stable order.
  * *d_count (device int32) receives the number of rays written (clamped to
  * max_out).  If h_count != NULL the call synchronises and stores it there. */
-int32_t rt_gen_secondary(rt_ctx* ctx, rt_scene* scene, const rt_sample* d_in, int32_t rays_in,
+RT_API int32_t rt_gen_secondary(rt_ctx* ctx, rt_scene* scene, const rt_sample* d_in, int32_t rays_in,
                          const rt_hit* d_hits, rt_sample* d_out, int32_t max_out,
                          int32_t* d_count, int32_t* h_count, rt_stream s);
 /* FrameBuffer::clear / copy (src/rt/framebuffer.cpp:117-165,
  * framebuffer.cl:20-54): RGBA8 = round-to-nearest-even saturate(255 * v * 1e-6). */
-int32_t rt_fb_clear(rt_ctx* ctx, uint32_t* d_image_rgb, size_t pixels, rt_stream s);
-int32_t rt_fb_copy(rt_ctx* ctx, const uint32_t* d_image_rgb, uint8_t* d_rgba, size_t pixels,
+RT_API int32_t rt_fb_clear(rt_ctx* ctx, uint32_t* d_image_rgb, size_t pixels, rt_stream s);
+RT_API int32_t rt_fb_copy(rt_ctx* ctx, const uint32_t* d_image_rgb, uint8_t* d_rgba, size_t pixels,
                    rt_stream s);
 
 /* ------------------------------------------------------------------------ */
@@ -290,13 +299,13 @@ int32_t rt_fb_copy(rt_ctx* ctx, const uint32_t* d_image_rgb, uint8_t* d_rgba, si
 /* d_rgba: w*h RGBA8 (required).  d_image_rgb: optional fixed-point
  * accumulation buffer (3 uint32 per pixel, written, not accumulated).
  * d_stats: optional device rt_render_stats (accumulated; caller zeroes). */
-int32_t rt_render(rt_ctx* ctx, rt_scene* scene, const rt_camera* cam, int32_t width,
+RT_API int32_t rt_render(rt_ctx* ctx, rt_scene* scene, const rt_camera* cam, int32_t width,
                   int32_t height, int32_t max_bounces, uint8_t* d_rgba, uint32_t* d_image_rgb,
                   rt_render_stats* d_stats, rt_stream s);
 
 /* End-to-end convenience: host vertices in, host image out, synchronous:
  * optional vertex update -> LBVH build -> render -> RGBA8 to host. */
-int32_t rt_render_host(rt_ctx* ctx, rt_scene* scene, const float* h_pos4, const float* h_nrm4,
+RT_API int32_t rt_render_host(rt_ctx* ctx, rt_scene* scene, const float* h_pos4, const float* h_nrm4,
                        uint32_t vertex_count, const rt_bvh_cfg* cfg, const rt_camera* cam,
                        int32_t width, int32_t height, int32_t max_bounces, uint8_t* h_rgba,
                        rt_render_stats* h_stats, rt_stream s);

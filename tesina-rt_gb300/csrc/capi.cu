@@ -1,0 +1,818 @@
+// capi.cu — the extern "C" boundary of librt_cuda.so (include/rt_cuda.h).
+//
+// Replaces the reference's DeviceInterface / DeviceMemory handle tables
+// (include/gpu/interface.hpp:20-80, src/gpu/memory.cpp) with plain device
+// pointers owned by a context, and its Scene / BVHBuilder / Tracer /
+// RayShader / SecondaryRayGenerator / FrameBuffer methods with the entry
+// points below.  Every entry point returns 0 or a negative rt_status and never
+// throws; rt_last_error() holds the message of the last failure on the
+// calling thread.  There is no CPU fallback: without a CUDA device every
+// compute entry point fails with RT_ERR_CUDA.
+#include <cuda_runtime.h>
+#include <stdarg.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <cmath>
+#include <new>
+#include <vector>
+
+#include "../../include/rt_cuda.h"
+#include "lbvh.cuh"
+#include "rt_internal.cuh"
+#include "trace.cuh"
+
+namespace {
+
+thread_local char g_err[512] = "";
+
+int32_t fail(int32_t code, const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+#define CU(call)                                                                              \
+    do {                                                                                      \
+        cudaError_t e_ = (call);                                                              \
+        if (e_ != cudaSuccess)                                                                \
+            return fail(RT_ERR_CUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_),  \
+                        __FILE__, __LINE__);                                                  \
+    } while (0)
+
+template <class T>
+cudaError_t dalloc(T** p, size_t count) {
+    if (count == 0) count = 1;
+    return cudaMalloc(reinterpret_cast<void**>(p), sizeof(T) * count);
+}
+
+template <class T>
+void dfree(T*& p) {
+    if (p) cudaFree(p);
+    p = nullptr;
+}
+
+}  // namespace
+
+struct rt_ctx {
+    int device = 0;
+    int num_sms = 0;
+    int render_blocks_per_sm = 1;
+    cudaStream_t stream = nullptr;
+    uint32_t* d_status = nullptr;
+    uint32_t* d_work = nullptr;
+    uint32_t* d_sec_scratch = nullptr;
+    size_t sec_scratch_bytes = 0;
+    uint8_t* d_out = nullptr;            // rt_render_host image staging
+    size_t d_out_cap = 0;
+    rt_render_stats* d_stats = nullptr;  // rt_render_host counters
+    float inv1e6 = 1.0f / 1e6f;
+};
+
+struct rt_scene {
+    uint32_t V = 0, N = 0, M = 0;
+    uint32_t capV = 0, capN = 0, capM = 0;
+    float4* d_pos = nullptr;
+    float4* d_nrm = nullptr;
+    uint32_t* d_idx[2] = {nullptr, nullptr};
+    uint32_t* d_map[2] = {nullptr, nullptr};
+    uint32_t* d_orig[2] = {nullptr, nullptr};
+    int cur = 0;                     // which of the [2] buffers holds the current order
+    rt_material* d_mats = nullptr;
+    rt_lights lights;
+    // build products
+    uint32_t* d_keys_unsorted = nullptr;
+    uint32_t* d_vals0 = nullptr;
+    uint32_t* d_keys1 = nullptr;
+    uint32_t* d_vals1 = nullptr;
+    uint32_t* d_keys_sorted = nullptr;
+    uint32_t* d_vals_sorted = nullptr;
+    float4* d_tris = nullptr;
+    float4* d_leafbox = nullptr;
+    float4* d_nodes = nullptr;
+    uint32_t* d_flags = nullptr;
+    uint32_t* d_rangeL = nullptr;
+    uint32_t* d_rangeR = nullptr;
+    rt::BvhHeader* d_hdr = nullptr;
+    uint32_t* d_scratch = nullptr;
+    size_t scratch_bytes = 0;
+    uint32_t buildN = 0;             // capacity of the build buffers
+    bool built = false;
+    int depth = 30, min_leaf = 1;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+namespace {
+
+void free_build(rt_scene* s) {
+    dfree(s->d_keys_unsorted);
+    dfree(s->d_vals0);
+    dfree(s->d_keys1);
+    dfree(s->d_vals1);
+    dfree(s->d_keys_sorted);
+    dfree(s->d_vals_sorted);
+    dfree(s->d_tris);
+    dfree(s->d_leafbox);
+    dfree(s->d_nodes);
+    dfree(s->d_flags);
+    dfree(s->d_rangeL);
+    dfree(s->d_rangeR);
+    dfree(s->d_hdr);
+    dfree(s->d_scratch);
+    s->buildN = 0;
+    s->scratch_bytes = 0;
+}
+
+void free_geometry(rt_scene* s) {
+    dfree(s->d_pos);
+    dfree(s->d_nrm);
+    for (int i = 0; i < 2; ++i) {
+        dfree(s->d_idx[i]);
+        dfree(s->d_map[i]);
+        dfree(s->d_orig[i]);
+    }
+    dfree(s->d_mats);
+    s->capV = s->capN = s->capM = 0;
+}
+
+int32_t ensure_build(rt_scene* s, int passes) {
+    const uint32_t n = s->N;
+    const size_t need_scratch = rt::lbvh_scratch_bytes(n, 4);
+    (void)passes;
+    if (s->buildN >= n && s->scratch_bytes >= need_scratch && s->d_hdr) return RT_OK;
+    free_build(s);
+    const size_t nn = n > 1 ? n - 1 : 1;
+    if (dalloc(&s->d_keys_unsorted, n) || dalloc(&s->d_vals0, n) || dalloc(&s->d_keys1, n) ||
+        dalloc(&s->d_vals1, n) || dalloc(&s->d_keys_sorted, n) || dalloc(&s->d_vals_sorted, n) ||
+        dalloc(&s->d_tris, 3 * (size_t)n) || dalloc(&s->d_leafbox, 2 * (size_t)n) ||
+        dalloc(&s->d_nodes, 4 * nn) || dalloc(&s->d_flags, nn) || dalloc(&s->d_rangeL, nn) ||
+        dalloc(&s->d_rangeR, nn) || dalloc(&s->d_hdr, 1) ||
+        cudaMalloc(reinterpret_cast<void**>(&s->d_scratch), need_scratch)) {
+        cudaGetLastError();
+        free_build(s);
+        return fail(RT_ERR_OOM, "device allocation of LBVH buffers for %u triangles failed", n);
+    }
+    s->buildN = n;
+    s->scratch_bytes = need_scratch;
+    return RT_OK;
+}
+
+rt::SceneView view_of(const rt_scene* s) {
+    rt::SceneView v;
+    v.nodes = s->d_nodes;
+    v.tris = s->d_tris;
+    v.idx = s->d_idx[s->cur];
+    v.nrm = s->d_nrm;
+    v.map = s->d_map[s->cur];
+    v.mats = s->d_mats;
+    v.hdr = s->d_hdr;
+    return v;
+}
+
+int32_t check_lights(const rt_lights* L) {
+    if (L->count < 1 || L->count > RT_MAX_LIGHTS)
+        return fail(RT_ERR_INVALID, "light count %d outside [1, %d]", L->count, RT_MAX_LIGHTS);
+    for (int i = 0; i < L->count; ++i) {
+        const int t = L->light[i].type;
+        if (t != RT_SPOT_L && t != RT_DIR_L && t != RT_POINT_L)
+            return fail(RT_ERR_INVALID, "light %d has unknown type %d", i, t);
+    }
+    return RT_OK;
+}
+
+cudaStream_t st(rt_ctx* c, rt_stream s) { return s ? (cudaStream_t)s : c->stream; }
+
+}  // namespace
+
+extern "C" {
+
+const char* rt_last_error(void) { return g_err; }
+
+int32_t rt_camera_set(rt_camera* cam, const float pos[3], const float dir[3], const float up[3],
+                      float fov, float aspect, int32_t right_handed) {
+    if (!cam || !pos || !dir || !up) return fail(RT_ERR_INVALID, "rt_camera_set: null argument");
+    float dn = std::sqrt(dir[0] * dir[0] + dir[1] * dir[1] + dir[2] * dir[2]);
+    if (!(dn > 0.f)) return fail(RT_ERR_INVALID, "rt_camera_set: zero direction");
+    float d[3] = {dir[0] / dn, dir[1] / dn, dir[2] / dn};
+    auto cross = [](const float* a, const float* b, float* o) {
+        o[0] = a[1] * b[2] - a[2] * b[1];
+        o[1] = a[2] * b[0] - a[0] * b[2];
+        o[2] = a[0] * b[1] - a[1] * b[0];
+    };
+    float r[3], u[3];
+    if (right_handed) {
+        cross(d, up, r);
+        cross(r, d, u);
+    } else {
+        cross(up, d, r);
+        cross(d, r, u);
+    }
+    const float ph = std::tan(fov * 0.5f);
+    const float rn = std::sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+    const float un = std::sqrt(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
+    if (!(rn > 0.f) || !(un > 0.f)) return fail(RT_ERR_INVALID, "rt_camera_set: up parallel to dir");
+    memset(cam, 0, sizeof(*cam));
+    for (int i = 0; i < 3; ++i) {
+        cam->pos[i] = pos[i];
+        cam->dir[i] = d[i];
+        cam->right[i] = r[i] * ((ph * aspect) / rn);
+        cam->up[i] = u[i] * (ph / un);
+    }
+    return RT_OK;
+}
+
+int32_t rt_init(rt_ctx** out, int32_t device) {
+    if (!out) return fail(RT_ERR_INVALID, "rt_init: null output");
+    *out = nullptr;
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count == 0) {
+        cudaGetLastError();
+        return fail(RT_ERR_CUDA, "rt_init: no CUDA device (%s)", cudaGetErrorString(e));
+    }
+    if (device < 0 || device >= count) return fail(RT_ERR_INVALID, "rt_init: bad device %d", device);
+    CU(cudaSetDevice(device));
+    rt_ctx* c = new (std::nothrow) rt_ctx();
+    if (!c) return fail(RT_ERR_OOM, "rt_init: host allocation failed");
+    c->device = device;
+    cudaDeviceProp prop;
+    CU(cudaGetDeviceProperties(&prop, device));
+    c->num_sms = prop.multiProcessorCount;
+    CU(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    CU(cudaMalloc(&c->d_status, sizeof(uint32_t)));
+    CU(cudaMemset(c->d_status, 0, sizeof(uint32_t)));
+    CU(cudaMalloc(&c->d_work, 64 * sizeof(uint32_t)));
+    int bps = 0;
+    CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, rt::launch_render_kernel_ptr(),
+                                                     rt::RENDER_THREADS, 0));
+    c->render_blocks_per_sm = bps > 0 ? bps : 1;
+    volatile float one = 1.0f, m = 1e6f;
+    c->inv1e6 = one / m;
+    *out = c;
+    return RT_OK;
+}
+
+int32_t rt_shutdown(rt_ctx* c) {
+    if (!c) return RT_OK;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    dfree(c->d_status);
+    dfree(c->d_work);
+    dfree(c->d_sec_scratch);
+    dfree(c->d_out);
+    dfree(c->d_stats);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return RT_OK;
+}
+
+int32_t rt_device_status(rt_ctx* c, uint32_t* bits) {
+    if (!c || !bits) return fail(RT_ERR_INVALID, "rt_device_status: null argument");
+    CU(cudaStreamSynchronize(c->stream));
+    CU(cudaMemcpy(bits, c->d_status, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    CU(cudaMemset(c->d_status, 0, sizeof(uint32_t)));
+    return RT_OK;
+}
+
+int32_t rt_stream_create(rt_ctx* c, rt_stream* s) {
+    if (!c || !s) return fail(RT_ERR_INVALID, "rt_stream_create: null argument");
+    cudaStream_t x;
+    CU(cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking));
+    *s = (rt_stream)x;
+    return RT_OK;
+}
+
+int32_t rt_stream_destroy(rt_ctx* c, rt_stream s) {
+    (void)c;
+    if (s) CU(cudaStreamDestroy((cudaStream_t)s));
+    return RT_OK;
+}
+
+int32_t rt_stream_sync(rt_ctx* c, rt_stream s) {
+    if (!c) return fail(RT_ERR_INVALID, "rt_stream_sync: null context");
+    CU(cudaStreamSynchronize(st(c, s)));
+    return RT_OK;
+}
+
+int32_t rt_buf_alloc(rt_ctx* c, size_t bytes, void** p) {
+    if (!c || !p) return fail(RT_ERR_INVALID, "rt_buf_alloc: null argument");
+    cudaError_t e = cudaMalloc(p, bytes ? bytes : 1);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        *p = nullptr;
+        return fail(RT_ERR_OOM, "rt_buf_alloc(%zu): %s", bytes, cudaGetErrorString(e));
+    }
+    return RT_OK;
+}
+
+int32_t rt_buf_free(rt_ctx* c, void* p) {
+    (void)c;
+    if (p) CU(cudaFree(p));
+    return RT_OK;
+}
+
+int32_t rt_buf_write(rt_ctx* c, void* d, const void* h, size_t bytes, rt_stream s) {
+    if (!c) return fail(RT_ERR_INVALID, "rt_buf_write: null context");
+    CU(cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, st(c, s)));
+    return RT_OK;
+}
+
+int32_t rt_buf_read(rt_ctx* c, void* h, const void* d, size_t bytes, rt_stream s) {
+    if (!c) return fail(RT_ERR_INVALID, "rt_buf_read: null context");
+    CU(cudaMemcpyAsync(h, d, bytes, cudaMemcpyDeviceToHost, st(c, s)));
+    CU(cudaStreamSynchronize(st(c, s)));
+    return RT_OK;
+}
+
+int32_t rt_buf_copy(rt_ctx* c, void* d, const void* src, size_t bytes, rt_stream s) {
+    if (!c) return fail(RT_ERR_INVALID, "rt_buf_copy: null context");
+    CU(cudaMemcpyAsync(d, src, bytes, cudaMemcpyDeviceToDevice, st(c, s)));
+    return RT_OK;
+}
+
+int32_t rt_buf_zero(rt_ctx* c, void* d, size_t bytes, rt_stream s) {
+    if (!c) return fail(RT_ERR_INVALID, "rt_buf_zero: null context");
+    CU(cudaMemsetAsync(d, 0, bytes, st(c, s)));
+    return RT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// scene
+// ---------------------------------------------------------------------------
+int32_t rt_scene_create(rt_ctx* c, rt_scene** out) {
+    if (!c || !out) return fail(RT_ERR_INVALID, "rt_scene_create: null argument");
+    rt_scene* s = new (std::nothrow) rt_scene();
+    if (!s) return fail(RT_ERR_OOM, "rt_scene_create: host allocation failed");
+    memset(&s->lights, 0, sizeof(s->lights));
+    CU(cudaEventCreate(&s->ev0));
+    CU(cudaEventCreate(&s->ev1));
+    *out = s;
+    return RT_OK;
+}
+
+int32_t rt_scene_destroy(rt_ctx* c, rt_scene* s) {
+    if (!s) return RT_OK;
+    if (c) cudaStreamSynchronize(c->stream);
+    free_build(s);
+    free_geometry(s);
+    if (s->ev0) cudaEventDestroy(s->ev0);
+    if (s->ev1) cudaEventDestroy(s->ev1);
+    delete s;
+    return RT_OK;
+}
+
+int32_t rt_scene_upload(rt_ctx* c, rt_scene* s, const rt_scene_desc* d, rt_stream stream) {
+    if (!c || !s || !d) return fail(RT_ERR_INVALID, "rt_scene_upload: null argument");
+    if (!d->h_vertices || !d->h_indices || !d->h_materials || !d->h_material_map)
+        return fail(RT_ERR_INVALID, "rt_scene_upload: missing vertex, index or material data");
+    if (d->triangle_count == 0 || d->vertex_count == 0 || d->material_count == 0)
+        return fail(RT_ERR_INVALID, "rt_scene_upload: empty scene (%u tris, %u verts, %u mats)",
+                    d->triangle_count, d->vertex_count, d->material_count);
+    if (d->triangle_count >= (1u << 30))
+        return fail(RT_ERR_INVALID, "rt_scene_upload: %u triangles exceed 2^30", d->triangle_count);
+    if (d->vertex_stride < 12 || (!d->h_normals && d->vertex_stride < d->normal_offset + 12))
+        return fail(RT_ERR_INVALID, "rt_scene_upload: bad vertex stride %u", d->vertex_stride);
+    int32_t r = check_lights(&d->lights);
+    if (r) return r;
+    const uint32_t V = d->vertex_count, N = d->triangle_count, M = d->material_count;
+    for (size_t i = 0; i < 3 * (size_t)N; ++i)
+        if (d->h_indices[i] >= V)
+            return fail(RT_ERR_INVALID, "rt_scene_upload: index %u of triangle %zu >= %u vertices",
+                        d->h_indices[i], i / 3, V);
+    for (uint32_t i = 0; i < N; ++i)
+        if (d->h_material_map[i] >= M)
+            return fail(RT_ERR_INVALID, "rt_scene_upload: material %u of triangle %u >= %u",
+                        d->h_material_map[i], i, M);
+    for (uint32_t i = 0; i < M; ++i) {
+        if (d->h_materials[i].texture >= 0)
+            return fail(RT_ERR_INVALID, "rt_scene_upload: material %u is textured (unsupported)", i);
+        if (d->h_materials[i].refractive_index > 0.f)
+            return fail(RT_ERR_INVALID, "rt_scene_upload: material %u refracts (unsupported)", i);
+    }
+    CU(cudaSetDevice(c->device));
+    cudaStream_t cs = st(c, stream);
+    CU(cudaStreamSynchronize(cs));
+    if (s->capV < V || s->capN < N || s->capM < M) {
+        free_geometry(s);
+        if (dalloc(&s->d_pos, V) || dalloc(&s->d_nrm, V) || dalloc(&s->d_idx[0], 3 * (size_t)N) ||
+            dalloc(&s->d_idx[1], 3 * (size_t)N) || dalloc(&s->d_map[0], N) ||
+            dalloc(&s->d_map[1], N) || dalloc(&s->d_orig[0], N) || dalloc(&s->d_orig[1], N) ||
+            dalloc(&s->d_mats, M)) {
+            cudaGetLastError();
+            free_geometry(s);
+            return fail(RT_ERR_OOM, "rt_scene_upload: device allocation failed");
+        }
+        s->capV = V;
+        s->capN = N;
+        s->capM = M;
+    }
+    s->V = V;
+    s->N = N;
+    s->M = M;
+    s->cur = 0;
+    const char* vb = (const char*)d->h_vertices;
+    if (d->vertex_stride == 16 && d->position_offset == 0) {
+        CU(cudaMemcpyAsync(s->d_pos, vb, 16 * (size_t)V, cudaMemcpyHostToDevice, cs));
+    } else {
+        std::vector<float> tmp(4 * (size_t)V, 0.f);
+        for (size_t i = 0; i < V; ++i)
+            memcpy(&tmp[4 * i], vb + i * d->vertex_stride + d->position_offset, 12);
+        CU(cudaMemcpyAsync(s->d_pos, tmp.data(), 16 * (size_t)V, cudaMemcpyHostToDevice, cs));
+        CU(cudaStreamSynchronize(cs));
+    }
+    if (d->h_normals) {
+        CU(cudaMemcpyAsync(s->d_nrm, d->h_normals, 16 * (size_t)V, cudaMemcpyHostToDevice, cs));
+    } else {
+        std::vector<float> tmp(4 * (size_t)V, 0.f);
+        for (size_t i = 0; i < V; ++i)
+            memcpy(&tmp[4 * i], vb + i * d->vertex_stride + d->normal_offset, 12);
+        CU(cudaMemcpyAsync(s->d_nrm, tmp.data(), 16 * (size_t)V, cudaMemcpyHostToDevice, cs));
+        CU(cudaStreamSynchronize(cs));
+    }
+    CU(cudaMemcpyAsync(s->d_idx[0], d->h_indices, 12 * (size_t)N, cudaMemcpyHostToDevice, cs));
+    CU(cudaMemcpyAsync(s->d_map[0], d->h_material_map, 4 * (size_t)N, cudaMemcpyHostToDevice, cs));
+    CU(cudaMemcpyAsync(s->d_mats, d->h_materials, sizeof(rt_material) * M, cudaMemcpyHostToDevice,
+                       cs));
+    {
+        std::vector<uint32_t> iota(N);
+        for (uint32_t i = 0; i < N; ++i) iota[i] = i;
+        CU(cudaMemcpyAsync(s->d_orig[0], iota.data(), 4 * (size_t)N, cudaMemcpyHostToDevice, cs));
+        CU(cudaStreamSynchronize(cs));
+    }
+    s->lights = d->lights;
+    s->built = false;
+    return RT_OK;
+}
+
+int32_t rt_scene_update_vertices(rt_ctx* c, rt_scene* s, const float* pos4, const float* nrm4,
+                                 uint32_t V, rt_stream stream) {
+    if (!c || !s || !pos4) return fail(RT_ERR_INVALID, "rt_scene_update_vertices: null argument");
+    if (V != s->V) return fail(RT_ERR_INVALID, "vertex count %u != scene's %u", V, s->V);
+    cudaStream_t cs = st(c, stream);
+    CU(cudaMemcpyAsync(s->d_pos, pos4, 16 * (size_t)V, cudaMemcpyHostToDevice, cs));
+    if (nrm4) CU(cudaMemcpyAsync(s->d_nrm, nrm4, 16 * (size_t)V, cudaMemcpyHostToDevice, cs));
+    return RT_OK;
+}
+
+int32_t rt_scene_update_vertices_device(rt_ctx* c, rt_scene* s, const float* pos4,
+                                        const float* nrm4, uint32_t V, rt_stream stream) {
+    if (!c || !s || !pos4) return fail(RT_ERR_INVALID, "rt_scene_update_vertices: null argument");
+    if (V != s->V) return fail(RT_ERR_INVALID, "vertex count %u != scene's %u", V, s->V);
+    cudaStream_t cs = st(c, stream);
+    CU(cudaMemcpyAsync(s->d_pos, pos4, 16 * (size_t)V, cudaMemcpyDeviceToDevice, cs));
+    if (nrm4) CU(cudaMemcpyAsync(s->d_nrm, nrm4, 16 * (size_t)V, cudaMemcpyDeviceToDevice, cs));
+    return RT_OK;
+}
+
+int32_t rt_scene_set_lights(rt_ctx* c, rt_scene* s, const rt_lights* L) {
+    if (!c || !s || !L) return fail(RT_ERR_INVALID, "rt_scene_set_lights: null argument");
+    int32_t r = check_lights(L);
+    if (r) return r;
+    s->lights = *L;
+    return RT_OK;
+}
+
+int32_t rt_scene_buffers(rt_ctx* c, rt_scene* s, uint32_t** idx, uint32_t** map, float** pos,
+                         float** nrm, uint32_t* n) {
+    if (!c || !s) return fail(RT_ERR_INVALID, "rt_scene_buffers: null argument");
+    if (idx) *idx = s->d_idx[s->cur];
+    if (map) *map = s->d_map[s->cur];
+    if (pos) *pos = reinterpret_cast<float*>(s->d_pos);
+    if (nrm) *nrm = reinterpret_cast<float*>(s->d_nrm);
+    if (n) *n = s->N;
+    return RT_OK;
+}
+
+int32_t rt_scene_read_sort(rt_ctx* c, rt_scene* s, uint32_t* keys, uint32_t* perm,
+                           uint32_t* sorted) {
+    if (!c || !s) return fail(RT_ERR_INVALID, "rt_scene_read_sort: null argument");
+    if (!s->built) return fail(RT_ERR_NOT_BUILT, "rt_scene_read_sort: no BVH built");
+    CU(cudaStreamSynchronize(c->stream));
+    const size_t b = 4 * (size_t)s->N;
+    if (keys) CU(cudaMemcpy(keys, s->d_keys_unsorted, b, cudaMemcpyDeviceToHost));
+    if (perm) CU(cudaMemcpy(perm, s->d_vals_sorted, b, cudaMemcpyDeviceToHost));
+    if (sorted) CU(cudaMemcpy(sorted, s->d_keys_sorted, b, cudaMemcpyDeviceToHost));
+    return RT_OK;
+}
+
+int32_t rt_scene_read_orig(rt_ctx* c, rt_scene* s, uint32_t* orig) {
+    if (!c || !s || !orig) return fail(RT_ERR_INVALID, "rt_scene_read_orig: null argument");
+    CU(cudaStreamSynchronize(c->stream));
+    CU(cudaMemcpy(orig, s->d_orig[s->cur], 4 * (size_t)s->N, cudaMemcpyDeviceToHost));
+    return RT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// LBVH
+// ---------------------------------------------------------------------------
+static rt::LbvhArgs lbvh_args(rt_ctx* c, rt_scene* s) {
+    rt::LbvhArgs a;
+    a.n = s->N;
+    a.depth = s->depth;
+    a.min_leaf = s->min_leaf;
+    a.num_sms = c->num_sms;
+    a.pos = s->d_pos;
+    a.idx_in = s->d_idx[s->cur];
+    a.map_in = s->d_map[s->cur];
+    a.orig_in = s->d_orig[s->cur];
+    a.idx_out = s->d_idx[s->cur ^ 1];
+    a.map_out = s->d_map[s->cur ^ 1];
+    a.orig_out = s->d_orig[s->cur ^ 1];
+    a.keys_unsorted = s->d_keys_unsorted;
+    a.vals0 = s->d_vals0;
+    a.keys1 = s->d_keys1;
+    a.vals1 = s->d_vals1;
+    a.keys_sorted = s->d_keys_sorted;
+    a.vals_sorted = s->d_vals_sorted;
+    a.tris = s->d_tris;
+    a.leafbox = s->d_leafbox;
+    a.nodes = s->d_nodes;
+    a.flags = s->d_flags;
+    a.rangeL = s->d_rangeL;
+    a.rangeR = s->d_rangeR;
+    a.hdr = s->d_hdr;
+    a.scratch = s->d_scratch;
+    a.status = c->d_status;
+    return a;
+}
+
+int32_t rt_bvh_build_lbvh(rt_ctx* c, rt_scene* s, const rt_bvh_cfg* cfg, rt_stream stream) {
+    if (!c || !s) return fail(RT_ERR_INVALID, "rt_bvh_build_lbvh: null argument");
+    if (s->N == 0) return fail(RT_ERR_INVALID, "rt_bvh_build_lbvh: scene has no triangles");
+    int depth = cfg ? cfg->depth : 30, min_leaf = cfg ? cfg->min_leaf_size : 1;
+    if (depth > 32) return fail(RT_ERR_INVALID, "bvh depth %d > 32 is not supported", depth);
+    if (depth < 1) depth = 1;
+    if (min_leaf < 1) min_leaf = 1;
+    if (min_leaf > 256) min_leaf = 256;
+    s->depth = depth;
+    s->min_leaf = min_leaf;
+    int32_t r = ensure_build(s, (depth + 7) / 8);
+    if (r) return r;
+    cudaStream_t cs = st(c, stream);
+    CU(cudaEventRecord(s->ev0, cs));
+    rt::LbvhArgs a = lbvh_args(c, s);
+    CU(rt::lbvh_build(a, cs));
+    CU(cudaEventRecord(s->ev1, cs));
+    s->cur ^= 1;   // the sorted index buffer / material map are now current
+    s->built = true;
+    return RT_OK;
+}
+
+int32_t rt_bvh_refit_lbvh(rt_ctx* c, rt_scene* s, rt_stream stream) {
+    if (!c || !s) return fail(RT_ERR_INVALID, "rt_bvh_refit_lbvh: null argument");
+    if (!s->built) return fail(RT_ERR_NOT_BUILT, "rt_bvh_refit_lbvh: no BVH built");
+    cudaStream_t cs = st(c, stream);
+    CU(cudaEventRecord(s->ev0, cs));
+    rt::LbvhArgs a = lbvh_args(c, s);
+    a.idx_out = s->d_idx[s->cur];   // refit keeps the current (sorted) order
+    CU(rt::lbvh_refit(a, cs));
+    CU(cudaEventRecord(s->ev1, cs));
+    return RT_OK;
+}
+
+int32_t rt_bvh_last_time_ms(rt_ctx* c, rt_scene* s, float* ms) {
+    if (!c || !s || !ms) return fail(RT_ERR_INVALID, "rt_bvh_last_time_ms: null argument");
+    CU(cudaEventSynchronize(s->ev1));
+    CU(cudaEventElapsedTime(ms, s->ev0, s->ev1));
+    return RT_OK;
+}
+
+int32_t rt_bvh_export(rt_ctx* c, rt_scene* s, rt_canon_node* out, uint32_t cap, uint32_t* count) {
+    if (!c || !s || !count) return fail(RT_ERR_INVALID, "rt_bvh_export: null argument");
+    if (!s->built) return fail(RT_ERR_NOT_BUILT, "rt_bvh_export: no BVH built");
+    CU(cudaStreamSynchronize(c->stream));
+    rt::BvhHeader h;
+    CU(cudaMemcpy(&h, s->d_hdr, sizeof(h), cudaMemcpyDeviceToHost));
+    const size_t nn = s->N > 1 ? s->N - 1 : 0;
+    std::vector<float4> nodes(4 * nn + 4);
+    if (nn) CU(cudaMemcpy(nodes.data(), s->d_nodes, sizeof(float4) * 4 * nn, cudaMemcpyDeviceToHost));
+    std::vector<rt_canon_node> res;
+    res.reserve(2 * (size_t)s->N);
+    struct Item {
+        int32_t ref, cnt;
+        uint32_t depth;
+        float lo[3], hi[3];
+        int64_t slot;
+    };
+    // iterative pre-order; interior ranges patched after their subtrees
+    std::vector<Item> todo;
+    std::vector<std::pair<int64_t, int64_t>> pending;   // (slot, right child slot)
+    todo.push_back(Item{h.root_ref, h.root_cnt, 0, {h.root_lo.x, h.root_lo.y, h.root_lo.z},
+                        {h.root_hi.x, h.root_hi.y, h.root_hi.z}, -1});
+    std::vector<int64_t> left_of, right_of;
+    while (!todo.empty()) {
+        Item it = todo.back();
+        todo.pop_back();
+        rt_canon_node cn;
+        memset(&cn, 0, sizeof(cn));
+        cn.depth = it.depth;
+        for (int k = 0; k < 3; ++k) {
+            cn.lo[k] = it.lo[k];
+            cn.hi[k] = it.hi[k];
+        }
+        const int64_t me = (int64_t)res.size();
+        if (it.cnt > 0) {
+            cn.leaf = 1;
+            cn.start = (uint32_t)it.ref;
+            cn.end = (uint32_t)(it.ref + it.cnt);
+        } else {
+            if (it.ref < 0 || (size_t)it.ref >= nn)
+                return fail(RT_ERR, "rt_bvh_export: corrupt node reference %d", it.ref);
+            const float4* q = &nodes[4 * (size_t)it.ref];
+            const int* qi = reinterpret_cast<const int*>(&q[3]);
+            Item L{qi[0], qi[2], it.depth + 1, {q[0].x, q[0].y, q[0].z}, {q[0].w, q[1].x, q[1].y}, me};
+            Item R{qi[1], qi[3], it.depth + 1, {q[1].z, q[1].w, q[2].x}, {q[2].y, q[2].z, q[2].w}, me};
+            todo.push_back(R);
+            todo.push_back(L);
+        }
+        res.push_back(cn);
+        left_of.push_back(-1);
+        right_of.push_back(-1);
+        if (it.slot >= 0) {
+            if (left_of[it.slot] < 0)
+                left_of[it.slot] = me;
+            else
+                right_of[it.slot] = me;
+        }
+        if (res.size() > 2 * (size_t)s->N) return fail(RT_ERR, "rt_bvh_export: tree has a cycle");
+    }
+    // ranges of interior nodes from their children (post-order = reverse pre-order)
+    for (int64_t k = (int64_t)res.size() - 1; k >= 0; --k)
+        if (!res[k].leaf) {
+            res[k].start = res[left_of[k]].start;
+            res[k].end = res[right_of[k]].end;
+        }
+    *count = (uint32_t)res.size();
+    if (!out) return RT_OK;
+    if (cap < res.size()) return fail(RT_ERR_INVALID, "rt_bvh_export: capacity %u < %zu", cap, res.size());
+    memcpy(out, res.data(), sizeof(rt_canon_node) * res.size());
+    return RT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// stage-wise pipeline
+// ---------------------------------------------------------------------------
+int32_t rt_gen_primary(rt_ctx* c, const rt_camera* cam, int32_t w, int32_t h, int32_t quad,
+                       int32_t spp, const rt_pixel_sample* ps, size_t count, size_t offset,
+                       rt_sample* out, rt_stream s) {
+    if (!c || !cam || !out) return fail(RT_ERR_INVALID, "rt_gen_primary: null argument");
+    if (w <= 0 || h <= 0 || quad <= 0 || spp <= 0)
+        return fail(RT_ERR_INVALID, "rt_gen_primary: bad size %dx%d quad %d spp %d", w, h, quad, spp);
+    if (offset + count > (size_t)w * h * spp)
+        return fail(RT_ERR_INVALID, "rt_gen_primary: ids beyond w*h*spp");
+    CU(rt::launch_gen_primary(*cam, w, h, quad, ps, count, offset, out, st(c, s)));
+    return RT_OK;
+}
+
+static int32_t need_built(rt_scene* s, const char* who) {
+    if (!s) return fail(RT_ERR_INVALID, "%s: null scene", who);
+    if (!s->built) return fail(RT_ERR_NOT_BUILT, "%s: no BVH built", who);
+    return RT_OK;
+}
+
+int32_t rt_trace(rt_ctx* c, rt_scene* s, const rt_sample* smp, int32_t n, rt_hit* hits,
+                 int32_t secondary, rt_stream stream) {
+    (void)secondary;
+    if (!c || !smp || !hits) return fail(RT_ERR_INVALID, "rt_trace: null argument");
+    int32_t r = need_built(s, "rt_trace");
+    if (r) return r;
+    CU(rt::launch_trace(view_of(s), smp, n, hits, c->d_status, st(c, stream)));
+    return RT_OK;
+}
+
+int32_t rt_shadow_trace(rt_ctx* c, rt_scene* s, const rt_sample* smp, int32_t n, rt_hit* hits,
+                        int32_t secondary, rt_stream stream) {
+    (void)secondary;
+    (void)smp;
+    if (!c || !hits) return fail(RT_ERR_INVALID, "rt_shadow_trace: null argument");
+    int32_t r = need_built(s, "rt_shadow_trace");
+    if (r) return r;
+    CU(rt::launch_shadow(view_of(s), s->lights, n, hits, c->d_status, st(c, stream)));
+    return RT_OK;
+}
+
+int32_t rt_shade(rt_ctx* c, rt_scene* s, const rt_sample* smp, const rt_hit* hits, int32_t n,
+                 uint32_t* img, int32_t primary, rt_stream stream) {
+    (void)primary;
+    if (!c || !smp || !hits || !img) return fail(RT_ERR_INVALID, "rt_shade: null argument");
+    int32_t r = need_built(s, "rt_shade");
+    if (r) return r;
+    CU(rt::launch_shade(view_of(s), s->lights, smp, hits, n, img, st(c, stream)));
+    return RT_OK;
+}
+
+int32_t rt_gen_secondary(rt_ctx* c, rt_scene* s, const rt_sample* in, int32_t n, const rt_hit* hits,
+                         rt_sample* out, int32_t max_out, int32_t* d_count, int32_t* h_count,
+                         rt_stream stream) {
+    if (!c || !in || !hits || !out || !d_count)
+        return fail(RT_ERR_INVALID, "rt_gen_secondary: null argument");
+    int32_t r = need_built(s, "rt_gen_secondary");
+    if (r) return r;
+    const size_t need = rt::gen_secondary_scratch_bytes(n);
+    if (c->sec_scratch_bytes < need) {
+        dfree(c->d_sec_scratch);
+        if (cudaMalloc(&c->d_sec_scratch, need)) {
+            cudaGetLastError();
+            c->sec_scratch_bytes = 0;
+            return fail(RT_ERR_OOM, "rt_gen_secondary: scratch allocation failed");
+        }
+        c->sec_scratch_bytes = need;
+    }
+    cudaStream_t cs = st(c, stream);
+    CU(rt::launch_gen_secondary(view_of(s), in, n, hits, out, max_out, d_count, c->d_sec_scratch, cs));
+    if (h_count) {
+        CU(cudaMemcpyAsync(h_count, d_count, sizeof(int32_t), cudaMemcpyDeviceToHost, cs));
+        CU(cudaStreamSynchronize(cs));
+    }
+    return RT_OK;
+}
+
+int32_t rt_fb_clear(rt_ctx* c, uint32_t* img, size_t px, rt_stream s) {
+    if (!c || !img) return fail(RT_ERR_INVALID, "rt_fb_clear: null argument");
+    CU(cudaMemsetAsync(img, 0, 12 * px, st(c, s)));
+    return RT_OK;
+}
+
+int32_t rt_fb_copy(rt_ctx* c, const uint32_t* img, uint8_t* rgba, size_t px, rt_stream s) {
+    if (!c || !img || !rgba) return fail(RT_ERR_INVALID, "rt_fb_copy: null argument");
+    CU(rt::launch_fb_copy(img, rgba, px, c->inv1e6, st(c, s)));
+    return RT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// fused path
+// ---------------------------------------------------------------------------
+int32_t rt_render(rt_ctx* c, rt_scene* s, const rt_camera* cam, int32_t w, int32_t h,
+                  int32_t max_bounces, uint8_t* rgba, uint32_t* img, rt_render_stats* stats,
+                  rt_stream stream) {
+    if (!c || !cam || !rgba) return fail(RT_ERR_INVALID, "rt_render: null argument");
+    int32_t r = need_built(s, "rt_render");
+    if (r) return r;
+    if (w <= 0 || h <= 0 || (int64_t)w * h > (1ll << 30))
+        return fail(RT_ERR_INVALID, "rt_render: bad size %dx%d", w, h);
+    if (max_bounces < 0 || max_bounces > 64)
+        return fail(RT_ERR_INVALID, "rt_render: bad max_bounces %d", max_bounces);
+    cudaStream_t cs = st(c, stream);
+    CU(cudaMemsetAsync(c->d_work, 0, sizeof(uint32_t), cs));
+    rt::RenderArgs a;
+    a.scene = view_of(s);
+    a.lights = s->lights;
+    a.cam = *cam;
+    a.width = w;
+    a.height = h;
+    a.max_bounces = max_bounces;
+    a.inv1e6 = c->inv1e6;
+    a.rgba = rgba;
+    a.image_rgb = img;
+    a.stats = stats;
+    a.work_counter = c->d_work;
+    a.status = c->d_status;
+    const int64_t warps_needed = ((int64_t)w * h + 31) / 32;
+    int64_t grid = (int64_t)c->num_sms * c->render_blocks_per_sm;
+    const int64_t max_useful = (warps_needed + (rt::RENDER_THREADS / 32) - 1) / (rt::RENDER_THREADS / 32);
+    if (grid > max_useful) grid = max_useful;
+    CU(rt::launch_render(a, (int)grid, cs));
+    return RT_OK;
+}
+
+int32_t rt_render_host(rt_ctx* c, rt_scene* s, const float* pos4, const float* nrm4, uint32_t V,
+                       const rt_bvh_cfg* cfg, const rt_camera* cam, int32_t w, int32_t h,
+                       int32_t max_bounces, uint8_t* h_rgba, rt_render_stats* h_stats,
+                       rt_stream stream) {
+    if (!c || !s || !cam || !h_rgba) return fail(RT_ERR_INVALID, "rt_render_host: null argument");
+    cudaStream_t cs = st(c, stream);
+    int32_t r;
+    if (pos4) {
+        r = rt_scene_update_vertices(c, s, pos4, nrm4, V, stream);
+        if (r) return r;
+    }
+    r = rt_bvh_build_lbvh(c, s, cfg, stream);
+    if (r) return r;
+    const size_t bytes = 4 * (size_t)w * h;
+    if (c->d_out_cap < bytes) {
+        dfree(c->d_out);
+        if (cudaMalloc(&c->d_out, bytes)) {
+            cudaGetLastError();
+            c->d_out_cap = 0;
+            return fail(RT_ERR_OOM, "rt_render_host: image allocation failed");
+        }
+        c->d_out_cap = bytes;
+    }
+    if (!c->d_stats) CU(cudaMalloc(&c->d_stats, sizeof(rt_render_stats)));
+    CU(cudaMemsetAsync(c->d_stats, 0, sizeof(rt_render_stats), cs));
+    r = rt_render(c, s, cam, w, h, max_bounces, c->d_out, nullptr, c->d_stats, stream);
+    if (r) return r;
+    CU(cudaMemcpyAsync(h_rgba, c->d_out, bytes, cudaMemcpyDeviceToHost, cs));
+    if (h_stats) CU(cudaMemcpyAsync(h_stats, c->d_stats, sizeof(*h_stats), cudaMemcpyDeviceToHost, cs));
+    CU(cudaStreamSynchronize(cs));
+    uint32_t bits = 0;
+    CU(cudaMemcpy(&bits, c->d_status, sizeof(bits), cudaMemcpyDeviceToHost));
+    if (bits & RT_DEV_TIMEOUT) return fail(RT_ERR_TIMEOUT, "rt_render_host: device wait timed out");
+    if (bits & RT_DEV_OVERFLOW) return fail(RT_ERR_OVERFLOW, "rt_render_host: stack overflow");
+    return RT_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,46 @@
+// lbvh.cuh — host interface of the LBVH builder kernels (lbvh.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "rt_internal.cuh"
+
+namespace rt {
+
+struct LbvhArgs {
+    uint32_t n;               // triangles
+    int depth;                // Morton bits (1..32)
+    int min_leaf;             // reference bvh_min_leaf_size
+    int num_sms;
+    const float4* pos;        // vertex positions
+    // triangle data in the order before this build, and its sorted copy
+    const uint32_t* idx_in;
+    const uint32_t* map_in;
+    const uint32_t* orig_in;
+    uint32_t* idx_out;
+    uint32_t* map_out;
+    uint32_t* orig_out;
+    // sort buffers
+    uint32_t* keys_unsorted;  // Morton key per triangle (order before the build)
+    uint32_t* vals0;          // 0..n-1
+    uint32_t* keys1;
+    uint32_t* vals1;
+    uint32_t* keys_sorted;
+    uint32_t* vals_sorted;    // sorted slot -> triangle (order before the build)
+    // outputs
+    float4* tris;             // 3 float4 per sorted triangle
+    float4* leafbox;          // 2 float4 per sorted triangle
+    float4* nodes;            // 4 float4 per radix-tree node (n - 1)
+    uint32_t* flags;          // n - 1 arrival counters
+    uint32_t* rangeL;         // n - 1
+    uint32_t* rangeR;         // n - 1
+    BvhHeader* hdr;
+    uint32_t* scratch;        // lbvh_scratch_bytes(n, passes)
+    uint32_t* status;         // device status word (RT_DEV_* bits)
+};
+
+size_t lbvh_scratch_bytes(uint32_t n, int passes);
+cudaError_t lbvh_build(const LbvhArgs& a, cudaStream_t s);
+cudaError_t lbvh_refit(const LbvhArgs& a, cudaStream_t s);
+
+}  // namespace rt

@@ -1,0 +1,42 @@
+// trace.cuh — host interface of the traversal / shading kernels (trace.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "rt_internal.cuh"
+
+namespace rt {
+
+constexpr int RENDER_THREADS = 128;
+
+struct RenderArgs {
+    SceneView scene;
+    rt_lights lights;
+    rt_camera cam;
+    int width, height, max_bounces;
+    float inv1e6;                 // 1.0f / 1e6f, the framebuffer's cint_max_inv
+    uint8_t* rgba;                // width * height RGBA8
+    uint32_t* image_rgb;          // optional fixed-point accumulation (3 per pixel)
+    rt_render_stats* stats;       // optional, accumulated
+    uint32_t* work_counter;       // zeroed before launch
+    uint32_t* status;
+};
+
+cudaError_t launch_render(const RenderArgs& a, int grid, cudaStream_t s);
+const void* launch_render_kernel_ptr();
+cudaError_t launch_gen_primary(const rt_camera& cam, int w, int h, int q, const rt_pixel_sample* ps,
+                               size_t count, size_t offset, rt_sample* out, cudaStream_t s);
+cudaError_t launch_trace(const SceneView& S, const rt_sample* smp, int n, rt_hit* hits,
+                         uint32_t* status, cudaStream_t s);
+cudaError_t launch_shadow(const SceneView& S, const rt_lights& L, int n, rt_hit* hits,
+                          uint32_t* status, cudaStream_t s);
+cudaError_t launch_shade(const SceneView& S, const rt_lights& L, const rt_sample* smp,
+                         const rt_hit* hits, int n, uint32_t* image, cudaStream_t s);
+cudaError_t launch_gen_secondary(const SceneView& S, const rt_sample* in, int n, const rt_hit* hits,
+                                 rt_sample* out, int max_out, int32_t* d_count,
+                                 uint32_t* block_scratch, cudaStream_t s);
+cudaError_t launch_fb_copy(const uint32_t* img, uint8_t* rgba, size_t px, float inv1e6,
+                           cudaStream_t s);
+size_t gen_secondary_scratch_bytes(int n);
+
+}  // namespace rt

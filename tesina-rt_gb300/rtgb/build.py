@@ -1,0 +1,68 @@
+"""In-tree build of librt_cuda.so for sm_103a (nvcc, no cmake).
+
+All CUDA translation units are compiled with ``--fmad=false`` so that the
+single-precision math follows the reference kernels' operation order without
+fused multiply-adds; division and square root keep nvcc's IEEE defaults.
+"""
+import os
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))   # tesina-rt_gb300/
+CSRC = os.path.join(PKG, "csrc")
+LIB = os.path.join(PKG, "librt_cuda.so")
+OBJDIR = os.path.join(PKG, "_build")
+NVCC = os.environ.get("NVCC", "nvcc")
+UNITS = ["lbvh", "trace", "capi"]
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+FLAGS = ARCH + ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
+                "-Xcompiler", "-fvisibility=hidden"]
+
+
+def _run(cmd):
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("command failed: %s\n%s%s" % (" ".join(cmd), r.stdout[-3000:],
+                                                         r.stderr[-6000:]))
+    return r
+
+
+def _sources():
+    out = []
+    for root, _, files in os.walk(CSRC):
+        out += [os.path.join(root, f) for f in files if f.endswith((".cu", ".cuh", ".h"))]
+    out.append(os.path.join(PKG, "..", "include", "rt_cuda.h"))
+    return out
+
+
+def stale():
+    if not os.path.exists(LIB):
+        return True
+    t = os.path.getmtime(LIB)
+    return any(os.path.getmtime(s) > t for s in _sources())
+
+
+def build(force=False, verbose=False):
+    if not force and not stale():
+        return LIB
+    os.makedirs(OBJDIR, exist_ok=True)
+
+    def one(u):
+        obj = os.path.join(OBJDIR, u + ".o")
+        extra = ["-Xptxas", "-v"] if verbose else []
+        r = _run([NVCC] + FLAGS + extra + ["-c", os.path.join(CSRC, u + ".cu"), "-o", obj])
+        if verbose:
+            sys.stderr.write(r.stderr)
+        return obj
+
+    with ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
+        objs = list(ex.map(one, UNITS))
+    tmp = LIB + ".tmp"
+    _run([NVCC] + ARCH + ["-shared", "-o", tmp] + objs)
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="-f" in sys.argv, verbose="-v" in sys.argv))

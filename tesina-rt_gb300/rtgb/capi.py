@@ -1,0 +1,309 @@
+"""ctypes binding of librt_cuda.so (include/rt_cuda.h) and thin Python helpers.
+
+Every call goes through the C ABI; there is no Python or CPU implementation
+of any compute entry point.  ``load()`` raises if the library is missing, and
+compute calls raise ``RtError`` when the library reports a failure (for
+example RT_ERR_CUDA when no GPU is present).
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+
+PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(PKG, "librt_cuda.so")
+
+P, I32, U32, SZ, F = C.c_void_p, C.c_int32, C.c_uint32, C.c_size_t, C.c_float
+
+# name -> (restype, argtypes); the list of every exported entry point
+SIGNATURES = {
+    "rt_last_error": (C.c_char_p, []),
+    "rt_camera_set": (I32, [P, P, P, P, F, F, I32]),
+    "rt_init": (I32, [C.POINTER(P), I32]),
+    "rt_shutdown": (I32, [P]),
+    "rt_device_status": (I32, [P, C.POINTER(U32)]),
+    "rt_stream_create": (I32, [P, C.POINTER(P)]),
+    "rt_stream_destroy": (I32, [P, P]),
+    "rt_stream_sync": (I32, [P, P]),
+    "rt_buf_alloc": (I32, [P, SZ, C.POINTER(P)]),
+    "rt_buf_free": (I32, [P, P]),
+    "rt_buf_write": (I32, [P, P, P, SZ, P]),
+    "rt_buf_read": (I32, [P, P, P, SZ, P]),
+    "rt_buf_copy": (I32, [P, P, P, SZ, P]),
+    "rt_buf_zero": (I32, [P, P, SZ, P]),
+    "rt_scene_create": (I32, [P, C.POINTER(P)]),
+    "rt_scene_destroy": (I32, [P, P]),
+    "rt_scene_upload": (I32, [P, P, P, P]),
+    "rt_scene_update_vertices": (I32, [P, P, P, P, U32, P]),
+    "rt_scene_update_vertices_device": (I32, [P, P, P, P, U32, P]),
+    "rt_scene_set_lights": (I32, [P, P, P]),
+    "rt_scene_buffers": (I32, [P, P, P, P, P, P, P]),
+    "rt_scene_read_sort": (I32, [P, P, P, P, P]),
+    "rt_scene_read_orig": (I32, [P, P, P]),
+    "rt_bvh_build_lbvh": (I32, [P, P, P, P]),
+    "rt_bvh_refit_lbvh": (I32, [P, P, P]),
+    "rt_bvh_export": (I32, [P, P, P, U32, C.POINTER(U32)]),
+    "rt_bvh_last_time_ms": (I32, [P, P, C.POINTER(F)]),
+    "rt_gen_primary": (I32, [P, P, I32, I32, I32, I32, P, SZ, SZ, P, P]),
+    "rt_trace": (I32, [P, P, P, I32, P, I32, P]),
+    "rt_shadow_trace": (I32, [P, P, P, I32, P, I32, P]),
+    "rt_shade": (I32, [P, P, P, P, I32, P, I32, P]),
+    "rt_gen_secondary": (I32, [P, P, P, I32, P, P, I32, P, P, P]),
+    "rt_fb_clear": (I32, [P, P, SZ, P]),
+    "rt_fb_copy": (I32, [P, P, P, SZ, P]),
+    "rt_render": (I32, [P, P, P, I32, I32, I32, P, P, P, P]),
+    "rt_render_host": (I32, [P, P, P, P, U32, P, P, I32, I32, I32, P, P, P]),
+}
+
+
+class RtError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("rt error %d: %s" % (code, msg))
+        self.code = code
+
+
+_LIB = None
+
+
+def load(path=None):
+    """Load librt_cuda.so (fails loudly if it has not been built)."""
+    global _LIB
+    if _LIB is not None and path is None:
+        return _LIB
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise RuntimeError("librt_cuda.so not built (%s): run __graft_entry__.build()" % p)
+    lib = C.CDLL(p)
+    for name, (res, args) in SIGNATURES.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    if path is None:
+        _LIB = lib
+    return lib
+
+
+def check(lib, code):
+    if code != 0:
+        raise RtError(code, lib.rt_last_error().decode(errors="replace"))
+    return code
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(P)
+
+
+class Context:
+    """An rt_ctx on one GPU."""
+
+    def __init__(self, device=0):
+        self.lib = load()
+        h = P()
+        check(self.lib, self.lib.rt_init(C.byref(h), device))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.lib.rt_shutdown(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # device buffers ------------------------------------------------------
+    def alloc(self, nbytes):
+        d = P()
+        check(self.lib, self.lib.rt_buf_alloc(self.h, nbytes, C.byref(d)))
+        return DeviceBuffer(self, d, nbytes)
+
+    def to_device(self, arr, stream=None):
+        arr = np.ascontiguousarray(arr)
+        b = self.alloc(arr.nbytes)
+        check(self.lib, self.lib.rt_buf_write(self.h, b.ptr, _p(arr), arr.nbytes, stream))
+        return b
+
+    def sync(self, stream=None):
+        check(self.lib, self.lib.rt_stream_sync(self.h, stream))
+
+    def device_status(self):
+        bits = U32(0)
+        check(self.lib, self.lib.rt_device_status(self.h, C.byref(bits)))
+        return bits.value
+
+    # stage-wise pipeline ---------------------------------------------------
+    def gen_primary(self, cam, w, h, out_buf, count=None, offset=0, quad=32, stream=None):
+        count = w * h if count is None else count
+        check(self.lib, self.lib.rt_gen_primary(self.h, C.byref(cam), w, h, quad, 1, None, count,
+                                                offset, out_buf.ptr, stream))
+
+    def fb_copy(self, img_buf, rgba_buf, pixels, stream=None):
+        check(self.lib, self.lib.rt_fb_copy(self.h, img_buf.ptr, rgba_buf.ptr, pixels, stream))
+
+
+class DeviceBuffer:
+    def __init__(self, ctx, ptr, nbytes):
+        self.ctx, self.ptr, self.nbytes = ctx, ptr, nbytes
+
+    def read(self, dtype, count=None, stream=None):
+        dtype = np.dtype(dtype)
+        count = self.nbytes // dtype.itemsize if count is None else count
+        out = np.empty(count, dtype)
+        check(self.ctx.lib, self.ctx.lib.rt_buf_read(self.ctx.h, _p(out), self.ptr,
+                                                     out.nbytes, stream))
+        return out
+
+    def write(self, arr, stream=None):
+        arr = np.ascontiguousarray(arr)
+        assert arr.nbytes <= self.nbytes
+        check(self.ctx.lib, self.ctx.lib.rt_buf_write(self.ctx.h, self.ptr, _p(arr), arr.nbytes,
+                                                      stream))
+
+    def zero(self, stream=None):
+        check(self.ctx.lib, self.ctx.lib.rt_buf_zero(self.ctx.h, self.ptr, self.nbytes, stream))
+
+    def free(self):
+        if self.ptr:
+            self.ctx.lib.rt_buf_free(self.ctx.h, self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            if self.ctx.h:
+                self.free()
+        except Exception:
+            pass
+
+
+def scene_desc(sc):
+    d = abi.SceneDesc()
+    d.h_vertices = _p(sc.pos4)
+    d.vertex_count = sc.n_verts
+    d.vertex_stride = 16
+    d.position_offset = 0
+    d.normal_offset = 0
+    d.h_normals = _p(sc.nrm4)
+    d.h_indices = _p(sc.idx)
+    d.triangle_count = sc.n_tris
+    d.material_count = sc.mats.shape[0]
+    d.h_materials = _p(sc.mats)
+    d.h_material_map = _p(sc.mat_map)
+    d.lights = sc.lights
+    return d
+
+
+class Scene:
+    """An rt_scene: upload, LBVH build, render, parity read-outs."""
+
+    def __init__(self, ctx, sc=None, stream=None):
+        self.ctx, self.lib = ctx, ctx.lib
+        h = P()
+        check(self.lib, self.lib.rt_scene_create(ctx.h, C.byref(h)))
+        self.h = h
+        self.n = 0
+        if sc is not None:
+            self.upload(sc, stream)
+
+    def upload(self, sc, stream=None):
+        self._keep = sc
+        d = scene_desc(sc)
+        check(self.lib, self.lib.rt_scene_upload(self.ctx.h, self.h, C.byref(d), stream))
+        self.n = sc.n_tris
+
+    def update_vertices(self, pos4, nrm4=None, stream=None):
+        check(self.lib, self.lib.rt_scene_update_vertices(self.ctx.h, self.h, _p(pos4), _p(nrm4),
+                                                          pos4.shape[0], stream))
+
+    def build(self, depth=30, min_leaf=1, stream=None):
+        cfg = abi.BvhCfg(depth, min_leaf)
+        check(self.lib, self.lib.rt_bvh_build_lbvh(self.ctx.h, self.h, C.byref(cfg), stream))
+
+    def refit(self, stream=None):
+        check(self.lib, self.lib.rt_bvh_refit_lbvh(self.ctx.h, self.h, stream))
+
+    def last_build_ms(self):
+        ms = F(0)
+        check(self.lib, self.lib.rt_bvh_last_time_ms(self.ctx.h, self.h, C.byref(ms)))
+        return ms.value
+
+    def sort_arrays(self):
+        n = self.n
+        keys, perm, sk, orig = (np.zeros(n, np.uint32) for _ in range(4))
+        check(self.lib, self.lib.rt_scene_read_sort(self.ctx.h, self.h, _p(keys), _p(perm), _p(sk)))
+        check(self.lib, self.lib.rt_scene_read_orig(self.ctx.h, self.h, _p(orig)))
+        return keys, perm, sk, orig
+
+    def canon(self):
+        cnt = U32(0)
+        check(self.lib, self.lib.rt_bvh_export(self.ctx.h, self.h, None, 0, C.byref(cnt)))
+        out = np.zeros(cnt.value, abi.CANON_DTYPE)
+        check(self.lib, self.lib.rt_bvh_export(self.ctx.h, self.h, _p(out), cnt.value, C.byref(cnt)))
+        return out
+
+    def buffers(self):
+        idx, mp, pos, nrm = P(), P(), P(), P()
+        n = U32(0)
+        check(self.lib, self.lib.rt_scene_buffers(self.ctx.h, self.h, C.byref(idx), C.byref(mp),
+                                                  C.byref(pos), C.byref(nrm), C.byref(n)))
+        return idx, mp, pos, nrm, n.value
+
+    def read_sorted_buffers(self):
+        idx, mp, _, _, n = self.buffers()
+        a = np.zeros((n, 3), np.uint32)
+        m = np.zeros(n, np.uint32)
+        check(self.lib, self.lib.rt_buf_read(self.ctx.h, _p(a), idx, a.nbytes, None))
+        check(self.lib, self.lib.rt_buf_read(self.ctx.h, _p(m), mp, m.nbytes, None))
+        return a, m
+
+    # stage-wise --------------------------------------------------------------
+    def trace(self, smp_buf, n, hit_buf, stream=None):
+        check(self.lib, self.lib.rt_trace(self.ctx.h, self.h, smp_buf.ptr, n, hit_buf.ptr, 0, stream))
+
+    def shadow(self, smp_buf, n, hit_buf, stream=None):
+        check(self.lib, self.lib.rt_shadow_trace(self.ctx.h, self.h, smp_buf.ptr, n, hit_buf.ptr, 0,
+                                                 stream))
+
+    def shade(self, smp_buf, hit_buf, n, img_buf, primary=1, stream=None):
+        check(self.lib, self.lib.rt_shade(self.ctx.h, self.h, smp_buf.ptr, hit_buf.ptr, n,
+                                          img_buf.ptr, primary, stream))
+
+    def gen_secondary(self, in_buf, n, hit_buf, out_buf, max_out, count_buf, stream=None):
+        hc = I32(0)
+        check(self.lib, self.lib.rt_gen_secondary(self.ctx.h, self.h, in_buf.ptr, n, hit_buf.ptr,
+                                                  out_buf.ptr, max_out, count_buf.ptr,
+                                                  C.byref(hc), stream))
+        return hc.value
+
+    # fused ----------------------------------------------------------------
+    def render(self, cam, w, h, max_bounces, rgba_buf, img_buf=None, stats_buf=None, stream=None):
+        check(self.lib, self.lib.rt_render(self.ctx.h, self.h, C.byref(cam), w, h, max_bounces,
+                                           rgba_buf.ptr, img_buf.ptr if img_buf else None,
+                                           stats_buf.ptr if stats_buf else None, stream))
+
+    def render_host(self, cam, w, h, max_bounces, pos4=None, nrm4=None, depth=30, min_leaf=1,
+                    rgba=None, stream=None):
+        if rgba is None:
+            rgba = np.zeros((h * w, 4), np.uint8)
+        st = abi.RenderStats()
+        cfg = abi.BvhCfg(depth, min_leaf)
+        V = pos4.shape[0] if pos4 is not None else 0
+        check(self.lib, self.lib.rt_render_host(self.ctx.h, self.h, _p(pos4), _p(nrm4), V,
+                                                C.byref(cfg), C.byref(cam), w, h, max_bounces,
+                                                _p(rgba), C.byref(st), stream))
+        return rgba, st
+
+    def close(self):
+        if self.h:
+            self.lib.rt_scene_destroy(self.ctx.h, self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            if self.ctx.h:
+                self.close()
+        except Exception:
+            pass

@@ -281,7 +281,7 @@ def workload_mid(seed=1):
     """Plain method, mid scale: 1024x512-cell fBm field + 200 mirror spheres,
     1920x1080, 2 point lights, depth 4, full LBVH rebuild per frame."""
     ter = Terrain(1024, 512, n_spheres=200, seed=seed)
-    cam = camera((0.0, 4.0, -10.0), (0.0, 0.0, 0.0), fov_deg=60.0, aspect=1920 / 1080)
+    cam = camera((0.0, 9.0, -2.5), (0.0, 0.0, 2.0), fov_deg=60.0, aspect=1920 / 1080)
     return dict(name="terrain1M_1920x1080_d4", terrain=ter, camera=cam, width=1920,
                 height=1080, max_bounces=4, depth=30, min_leaf=1)
 

@@ -1,0 +1,180 @@
+"""GPU parity of traversal, shading and the fused render (bit-exact against
+the oracle; closest-hit ids against an FP64 brute-force intersector)."""
+import numpy as np
+import pytest
+
+import pyoracle
+from helpers import camera_small, single_light, tiny_terrain
+from rtgb import abi, capi, scenes
+
+pytestmark = pytest.mark.gpu
+
+
+def _pair(ctx, orc, sc, depth=30):
+    g = capi.Scene(ctx, sc)
+    g.build(depth, 1)
+    o = orc.new_scene(sc)
+    o.build(depth, 1, 0)
+    return g, o
+
+
+def _primary(ctx, orc, cam, w, h):
+    n = w * h
+    d = ctx.alloc(80 * n)
+    ctx.gen_primary(cam, w, h, d)
+    ctx.sync()
+    return d, pyoracle.gen_primary(orc, cam, w, h)
+
+
+def test_primary_rays(ctx, orc):
+    cam = camera_small()
+    for (w, h) in [(512, 512), (100, 70), (33, 65)]:
+        d, ref = _primary(ctx, orc, cam, w, h)
+        got = d.read(abi.SAMPLE_DTYPE)
+        assert got.tobytes() == ref.tobytes()
+
+
+@pytest.mark.parametrize("light", ["point", "spot", "dir"])
+def test_stages_match_oracle(ctx, orc, light):
+    sc = scenes.soup(10000, seed=2)
+    sc.lights = single_light(light)
+    g, o = _pair(ctx, orc, sc)
+    cam = camera_small()
+    w = h = 256
+    n = w * h
+    smp_d, smp = _primary(ctx, orc, cam, w, h)
+    hit_d = ctx.alloc(64 * n)
+    hit_d.zero()
+    g.trace(smp_d, n, hit_d)
+    g.shadow(smp_d, n, hit_d)
+    ctx.sync()
+    got = hit_d.read(abi.HIT_DTYPE)
+    ref = o.trace(smp)
+    o.shadow(smp, ref)
+    m = ref["hit"] == 1
+    assert np.array_equal(got["hit"], ref["hit"])
+    for f in ("id", "t", "inverse_n", "shadow_hit"):
+        assert np.array_equal(got[f][m], ref[f][m]), f
+    for f in ("n", "hit_point"):
+        assert np.array_equal(got[f][m][:, :3], ref[f][m][:, :3]), f
+    img_d = ctx.alloc(12 * n)
+    img_d.zero()
+    g.shade(smp_d, hit_d, n, img_d)
+    ctx.sync()
+    img = img_d.read(np.uint32).reshape(-1, 3)
+    rimg = np.zeros((n, 3), np.uint32)
+    o.shade(smp, ref, rimg)
+    assert np.array_equal(img, rimg)
+    out_d = ctx.alloc(80 * n)
+    cnt_d = ctx.alloc(4)
+    k = g.gen_secondary(smp_d, n, hit_d, out_d, n, cnt_d)
+    ref_sec = o.gen_secondary(smp, ref)
+    assert k == ref_sec.shape[0] and k > 0
+    assert out_d.read(abi.SAMPLE_DTYPE, k).tobytes() == ref_sec.tobytes()
+    rgba_d = ctx.alloc(4 * n)
+    ctx.fb_copy(img_d, rgba_d, n)
+    ctx.sync()
+    assert np.array_equal(rgba_d.read(np.uint8).reshape(-1, 4), pyoracle.fb_copy(orc, rimg))
+
+
+def _render_both(ctx, orc, sc, cam, w, h, bounces):
+    g, o = _pair(ctx, orc, sc)
+    n = w * h
+    rgba_d, img_d = ctx.alloc(4 * n), ctx.alloc(12 * n)
+    st_d = ctx.alloc(32)
+    st_d.zero()
+    g.render(cam, w, h, bounces, rgba_d, img_d, st_d)
+    ctx.sync()
+    img = img_d.read(np.uint32).reshape(-1, 3)
+    rgba = rgba_d.read(np.uint8).reshape(-1, 4)
+    st = st_d.read(np.uint64)
+    rimg, rst = o.render(cam, w, h, bounces)
+    return img, rgba, st, rimg, rst, g, o
+
+
+def test_render_small_workload_bit_exact(ctx, orc):
+    """512x512 soup, depth 3, one point light: identical fixed-point image."""
+    wl = scenes.workload_small()
+    img, rgba, st, rimg, rst, _, _ = _render_both(ctx, orc, wl["scene"], wl["camera"], 512, 512, 3)
+    assert np.array_equal(img, rimg)
+    assert np.array_equal(rgba, pyoracle.fb_copy(orc, rimg))
+    assert st[0] == rst.primary_rays and st[1] == rst.secondary_rays
+    assert st[2] == rst.shadow_rays and st[3] == rst.hits
+    assert ctx.device_status() == 0
+
+
+@pytest.mark.parametrize("bounces", [0, 1, 4])
+def test_render_terrain_two_lights(ctx, orc, bounces):
+    ter = tiny_terrain(96, 48, 12)
+    sc = ter.scene(3)
+    cam = scenes.camera((0.0, 4.0, -10.0), (0.0, 0.0, 0.0), aspect=160 / 90)
+    img, rgba, st, rimg, rst, _, _ = _render_both(ctx, orc, sc, cam, 160, 90, bounces)
+    assert np.array_equal(img, rimg)
+    assert st[1] == rst.secondary_rays
+
+
+def test_render_mid_scale_tile(ctx, orc):
+    """1920x1080 terrain (1.24M triangles, 2 lights, depth 4): the oracle
+    renders the first 64K samples in the reference's tile order; those
+    pixels must match the GPU image exactly."""
+    wl = scenes.workload_mid()
+    sc = wl["terrain"].scene(0)
+    g = capi.Scene(ctx, sc)
+    g.build(30, 1)
+    w, h = wl["width"], wl["height"]
+    n = w * h
+    rgba_d, img_d = ctx.alloc(4 * n), ctx.alloc(12 * n)
+    g.render(wl["camera"], w, h, wl["max_bounces"], rgba_d, img_d)
+    ctx.sync()
+    img = img_d.read(np.uint32).reshape(-1, 3)
+    o = orc.new_scene(sc)
+    o.build(30, 1, 0)
+    count = 65536
+    rimg, _ = o.render(wl["camera"], w, h, wl["max_bounces"], offset=0, count=count)
+    smp = pyoracle.gen_primary(orc, wl["camera"], w, h, count=count)
+    px = smp["pixel"]
+    assert np.array_equal(img[px], rimg[px])
+
+
+def test_closest_hit_vs_fp64(ctx, orc):
+    """Closest-hit ids vs an FP64 brute-force intersector: >= 99.99% equal,
+    every mismatch a tie within 1e-6 relative t; hit t within 1e-5 relative."""
+    sc = scenes.soup(10000, seed=4)
+    g, o = _pair(ctx, orc, sc)
+    cam = camera_small()
+    w = h = 256
+    n = w * h
+    smp_d, smp = _primary(ctx, orc, cam, w, h)
+    hit_d = ctx.alloc(64 * n)
+    hit_d.zero()
+    g.trace(smp_d, n, hit_d)
+    ctx.sync()
+    hits = hit_d.read(abi.HIT_DTYPE)
+    _, _, _, orig = g.sort_arrays()
+    gid = np.where(hits["hit"] == 1, orig.astype(np.int64)[np.clip(hits["id"], 0, None)], -1)
+    gid = gid.astype(np.int32)
+    fid, ft = o.fp64_closest(smp)
+    match = gid == fid
+    assert match.mean() >= 0.9999
+    mism = np.nonzero(~match)[0]
+    if mism.size:
+        t_g = o.fp64_t_of(smp[mism], gid[mism])
+        assert np.all(np.abs(t_g - ft[mism]) <= 1e-6 * np.abs(ft[mism]))
+    hm = (gid >= 0) & match
+    rel = np.abs(hits["t"][hm].astype(np.float64) - ft[hm]) / np.abs(ft[hm])
+    assert rel.max() <= 1e-5
+
+
+def test_render_host_e2e(ctx, orc):
+    """rt_render_host: host vertices in, host RGBA8 out (upload + build + render)."""
+    ter = tiny_terrain(64, 32, 6)
+    sc = ter.scene(0)
+    g = capi.Scene(ctx, sc)
+    cam = scenes.camera((0.0, 4.0, -10.0), (0.0, 0.0, 0.0), aspect=1.0)
+    pos, nrm = ter.frame_vertices(2)
+    rgba, st = g.render_host(cam, 128, 128, 2, pos, nrm)
+    o = orc.new_scene(ter.scene(2))
+    o.build(30, 1, 0)
+    rimg, rst = o.render(cam, 128, 128, 2)
+    assert np.array_equal(rgba, pyoracle.fb_copy(orc, rimg))
+    assert st.primary_rays == 128 * 128
