@@ -22,18 +22,25 @@
 #include "lbvh.cuh"
 #include "rt_internal.cuh"
 #include "trace.cuh"
+#include "ctx_internal.h"
 
 namespace {
-
 thread_local char g_err[512] = "";
+}  // namespace
 
-int32_t fail(int32_t code, const char* fmt, ...) {
+namespace rt {
+int32_t set_error(int32_t code, const char* fmt, ...) {
     va_list ap;
     va_start(ap, fmt);
     vsnprintf(g_err, sizeof(g_err), fmt, ap);
     va_end(ap);
     return code;
 }
+}  // namespace rt
+
+namespace {
+
+#define fail rt::set_error
 
 #define CU(call)                                                                              \
     do {                                                                                      \
@@ -56,21 +63,6 @@ void dfree(T*& p) {
 }
 
 }  // namespace
-
-struct rt_ctx {
-    int device = 0;
-    int num_sms = 0;
-    int render_blocks_per_sm = 1;
-    cudaStream_t stream = nullptr;
-    uint32_t* d_status = nullptr;
-    uint32_t* d_work = nullptr;
-    uint32_t* d_sec_scratch = nullptr;
-    size_t sec_scratch_bytes = 0;
-    uint8_t* d_out = nullptr;            // rt_render_host image staging
-    size_t d_out_cap = 0;
-    rt_render_stats* d_stats = nullptr;  // rt_render_host counters
-    float inv1e6 = 1.0f / 1e6f;
-};
 
 struct rt_scene {
     uint32_t V = 0, N = 0, M = 0;
