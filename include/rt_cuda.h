@@ -310,6 +310,30 @@ RT_API int32_t rt_render_host(rt_ctx* ctx, rt_scene* scene, const float* h_pos4,
                        int32_t width, int32_t height, int32_t max_bounces, uint8_t* h_rgba,
                        rt_render_stats* h_stats, rt_stream s);
 
+/* ------------------------------------------------------------------------ */
+/* Sort without allocation (no counterpart in the reference)                */
+/* ------------------------------------------------------------------------ */
+/* Largest n accepted by rt_sort_pairs_noalloc. */
+#define RT_NOALLOC_MAX_PAIRS (1u << 20)
+
+/* Stable LSD radix sort of n (key, value) uint32 pairs on the low key_bits
+ * bits (1..32), the same passes the LBVH builder runs on Morton codes, for
+ * callers that cannot allocate device memory when they sort (their HBM is
+ * already handed to their own pool, or a cudaMalloc's implicit
+ * synchronisation is not acceptable in their loop).  No counterpart in the
+ * reference.  Allocates nothing: its scratch is a fixed ~9 MiB array in
+ * device memory that every GPU loading this library keeps until exit.
+ *   - n > RT_NOALLOC_MAX_PAIRS is rejected with RT_ERR_INVALID;
+ *   - inputs are not modified; outputs must not alias them;
+ *   - every call on a device shares the one scratch array: calls that
+ *     overlap on the GPU race; order them on one stream;
+ *   - the first call on a device looks up the array's device address; make
+ *     that call before any stream capture. */
+RT_API int32_t rt_sort_pairs_noalloc(rt_ctx* ctx, const uint32_t* d_keys_in,
+                                     const uint32_t* d_vals_in, uint32_t* d_keys_out,
+                                     uint32_t* d_vals_out, uint32_t n, int32_t key_bits,
+                                     rt_stream s);
+
 #ifdef __cplusplus
 }
 #endif

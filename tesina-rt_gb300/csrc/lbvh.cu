@@ -151,6 +151,24 @@ __global__ void __launch_bounds__(256) k_morton_hist(const float4* __restrict__ 
     }
 }
 
+// Digit histograms of every radix pass over plain keys (the sort without the
+// fused Morton stage).
+__global__ void __launch_bounds__(256) k_radix_hist(const uint32_t* __restrict__ keys, uint32_t n,
+                                                    int passes, uint32_t* __restrict__ hist) {
+    __shared__ uint32_t sh[4][256];
+    for (int i = threadIdx.x; i < 4 * 256; i += blockDim.x) (&sh[0][0])[i] = 0;
+    __syncthreads();
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t code = __ldg(&keys[i]);
+        for (int p = 0; p < passes; ++p) atomicAdd(&sh[p][(code >> (8 * p)) & 255u], 1u);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < passes * 256; i += blockDim.x) {
+        const uint32_t v = (&sh[0][0])[i];
+        if (v) atomicAdd(&hist[i], v);
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Onesweep radix pass
 // ---------------------------------------------------------------------------
@@ -517,6 +535,41 @@ cudaError_t lbvh_build(const LbvhArgs& a, cudaStream_t s) {
     }
     k_emit_refit<<<(n + 255) / 256, 256, 0, s>>>(n, a.keys_sorted, a.leafbox, a.nodes, a.flags,
                                                  a.rangeL, a.rangeR, a.min_leaf, a.hdr);
+    return cudaGetLastError();
+}
+
+size_t radix_scratch_words(uint32_t n, int passes) {
+    const size_t tiles = ((size_t)n + SORT_TILE - 1) / SORT_TILE;
+    return 4 * 256 + 4 + (size_t)passes * tiles * 256;
+}
+
+int radix_tile_size() { return SORT_TILE; }
+
+cudaError_t radix_sort_pairs(const uint32_t* kin, const uint32_t* vin, uint32_t* kout,
+                             uint32_t* vout, uint32_t* ktmp, uint32_t* vtmp, uint32_t n,
+                             int key_bits, uint32_t* scratch, uint32_t* status, int num_sms,
+                             cudaStream_t s) {
+    const int passes = (key_bits + 7) / 8;
+    const size_t tiles = ((size_t)n + SORT_TILE - 1) / SORT_TILE;
+    uint32_t* hist = scratch;
+    uint32_t* tile_ctr = hist + 4 * 256;
+    uint32_t* lookback = tile_ctr + 4;
+    cudaError_t e = cudaMemsetAsync(scratch, 0, sizeof(uint32_t) * radix_scratch_words(n, passes), s);
+    if (e) return e;
+    if (n == 0) return cudaSuccess;
+    k_radix_hist<<<grid_for(n, 256, num_sms * 8), 256, 0, s>>>(kin, n, passes, hist);
+    const uint32_t* ki = kin;
+    const uint32_t* vi = vin;
+    for (int p = 0; p < passes; ++p) {
+        const bool to_out = ((passes - 1 - p) & 1) == 0;
+        uint32_t* ko = to_out ? kout : ktmp;
+        uint32_t* vo = to_out ? vout : vtmp;
+        k_onesweep<<<(unsigned)tiles, SORT_THREADS, 0, s>>>(ki, vi, ko, vo, n, 8 * p, hist + 256 * p,
+                                                          lookback + (size_t)p * tiles * 256,
+                                                          tile_ctr + p, status);
+        ki = ko;
+        vi = vo;
+    }
     return cudaGetLastError();
 }
 

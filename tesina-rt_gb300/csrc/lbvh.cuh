@@ -43,4 +43,14 @@ size_t lbvh_scratch_bytes(uint32_t n, int passes);
 cudaError_t lbvh_build(const LbvhArgs& a, cudaStream_t s);
 cudaError_t lbvh_refit(const LbvhArgs& a, cudaStream_t s);
 
+// Stable LSD radix sort of (key, value) pairs on the low key_bits bits with
+// caller-provided scratch (radix_scratch_words words) and temporaries of n
+// pairs; passes alternate between out and tmp so that the last lands in out.
+size_t radix_scratch_words(uint32_t n, int passes);
+int radix_tile_size();
+cudaError_t radix_sort_pairs(const uint32_t* kin, const uint32_t* vin, uint32_t* kout,
+                             uint32_t* vout, uint32_t* ktmp, uint32_t* vtmp, uint32_t n,
+                             int key_bits, uint32_t* scratch, uint32_t* status, int num_sms,
+                             cudaStream_t s);
+
 }  // namespace rt

@@ -55,6 +55,7 @@ SIGNATURES = {
     "rt_fb_copy": (I32, [P, P, P, SZ, P]),
     "rt_render": (I32, [P, P, P, I32, I32, I32, P, P, P, P]),
     "rt_render_host": (I32, [P, P, P, P, U32, P, P, I32, I32, I32, P, P, P]),
+    "rt_sort_pairs_noalloc": (I32, [P, P, P, P, P, U32, I32, P]),
 }
 
 
