@@ -56,6 +56,17 @@ class Oracle(_Lib):
                         [P, P, I32, I32, I32, SZ, SZ, SZ, P, P, C.c_int])
         self.fp64_closest = b(L, "orc_fp64_closest", C.c_int, [P, P, I32, P, P, C.c_int])
         self.fp64_t_of = b(L, "orc_fp64_t_of", C.c_int, [P, P, I32, P, P])
+        self.emit_keys_raw = b(L, "orc_emit_keys", C.c_int, [P, U32, C.c_int, C.c_int, P, U32,
+                                                              C.POINTER(U32)])
+
+    def emit_keys(self, sorted_keys, depth=30, min_leaf=1):
+        k = np.ascontiguousarray(sorted_keys, np.uint32)
+        cnt = U32(0)
+        if self.emit_keys_raw(_p(k), k.shape[0], depth, min_leaf, None, 0, C.byref(cnt)):
+            raise RuntimeError("emit failed")
+        out = np.zeros(cnt.value, abi.CANON_DTYPE)
+        self.emit_keys_raw(_p(k), k.shape[0], depth, min_leaf, _p(out), cnt.value, C.byref(cnt))
+        return out
 
     def new_scene(self, sc):
         h = self.scene_new(_p(sc.pos4), _p(sc.nrm4), sc.n_verts, _p(sc.idx), sc.n_tris,

@@ -718,6 +718,31 @@ int orc_build(orc_scene* s, int depth, int min_leaf, int sort_kind) {
     return 0;
 }
 
+/* The emit rule alone on given sorted keys (ranges only; AABBs zero). */
+int orc_emit_keys(const uint32_t* sorted_keys, uint32_t n, int depth, int min_leaf,
+                  rt_canon_node* out, uint32_t cap, uint32_t* count) {
+    if (n == 0 || depth < 1 || depth > 32) return -1;
+    orc_scene s;
+    s.N = n;
+    s.depth = depth;
+    s.min_leaf = min_leaf;
+    s.sorted_keys.assign(sorted_keys, sorted_keys + n);
+    emit(&s, 0, n, 0, 0);
+    *count = (uint32_t)s.nodes.size();
+    if (!out) return 0;
+    if (cap < s.nodes.size()) return -1;
+    for (size_t k = 0; k < s.nodes.size(); ++k) {
+        rt_canon_node c;
+        std::memset(&c, 0, sizeof(c));
+        c.start = s.nodes[k].start;
+        c.end = s.nodes[k].end;
+        c.leaf = s.nodes[k].leaf;
+        c.depth = s.nodes[k].depth;
+        out[k] = c;
+    }
+    return 0;
+}
+
 /* refit_lbvh (bvh-builder.cpp:743-850): new AABBs, same topology and order. */
 int orc_refit(orc_scene* s) {
     if (!s->built) return -1;

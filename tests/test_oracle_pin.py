@@ -1,0 +1,138 @@
+"""Live pin of the oracle against the reference's kernels compiled for the
+CPU (oracle/_ref, built where the reference checkout exists)."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import pyoracle
+from helpers import camera_small, single_light, tiny_terrain
+from rtgb import abi, scenes
+
+pytestmark = pytest.mark.skipif(not pyoracle.RefKernels.available(),
+                                reason="reference kernels not built (no reference checkout)")
+_p = pyoracle._p
+
+
+@pytest.fixture(scope="module")
+def ref():
+    return pyoracle.RefKernels()
+
+
+def _pair(orc, ref, sc):
+    s = orc.new_scene(sc)
+    s.build(30, 1, 1)
+    rh = ref.new_scene(sc)
+    return s, rh
+
+
+@pytest.mark.parametrize("light", ["point", "spot", "dir"])
+def test_pin_soup_10k(orc, ref, light):
+    sc = scenes.soup(10000, seed=1)
+    sc.lights = single_light(light)
+    s, rh = _pair(orc, ref, sc)
+    n = sc.n_tris
+    kr = np.zeros(n, np.uint32)
+    assert ref.morton(rh, 30, _p(kr), None, None) == 0
+    keys, perm, _, _ = s.sort_arrays()
+    assert np.array_equal(kr, keys)
+    pr = np.zeros(n, np.uint32)
+    assert ref.bitonic(_p(kr), n, _p(pr)) == 0
+    assert np.array_equal(pr, perm)
+    ref.apply_perm(rh, _p(pr))
+    ir, mr = np.zeros((n, 3), np.uint32), np.zeros(n, np.uint32)
+    ref.get_buffers(rh, _p(ir), _p(mr))
+    io, mo = s.buffers()
+    assert np.array_equal(ir, io) and np.array_equal(mr, mo)
+    canon = s.canon()
+    assert ref.set_tree(rh, _p(canon), canon.shape[0]) == 0
+    tr = canon.copy()
+    ref.get_tree(rh, _p(tr))
+    assert np.array_equal(tr["lo"], canon["lo"]) and np.array_equal(tr["hi"], canon["hi"])
+    cam = camera_small()
+    w = h = 256
+    so = pyoracle.gen_primary(orc, cam, w, h)
+    sr = np.zeros(w * h, abi.SAMPLE_DTYPE)
+    ref.gen_primary(C.byref(cam), w, h, 32, 1, None, w * h, 0, _p(sr))
+    assert so.tobytes() == sr.tobytes()
+    ho = s.trace(so)
+    s.shadow(so, ho)
+    hr = np.zeros(w * h, abi.HIT_DTYPE)
+    ref.trace(rh, _p(sr), w * h, _p(hr), 4)
+    ref.shadow(rh, _p(sr), w * h, _p(hr), 4)
+    m = ho["hit"] == 1
+    assert np.array_equal(ho["hit"], hr["hit"])
+    for f in ("id", "t", "inverse_n", "shadow_hit"):
+        assert np.array_equal(ho[f][m], hr[f][m]), f
+    for f in ("n", "hit_point"):
+        assert np.array_equal(ho[f][m], hr[f][m]), f
+    io_, ir_ = np.zeros((w * h, 3), np.uint32), np.zeros((w * h, 3), np.uint32)
+    s.shade(so, ho, io_)
+    ref.shade(rh, _p(sr), _p(hr), w * h, _p(ir_), 1, 4)
+    assert np.array_equal(io_, ir_)
+    s2 = s.gen_secondary(so, ho)
+    out = np.zeros(w * h, abi.SAMPLE_DTYPE)
+    cnt = C.c_int32(0)
+    ref.gen_secondary(rh, _p(sr), w * h, _p(hr), _p(out), w * h, C.byref(cnt))
+    assert cnt.value == s2.shape[0] and s2.tobytes() == out[:cnt.value].tobytes()
+    ref.scene_free(rh)
+
+
+def test_pin_full_render_small_workload(orc, ref):
+    """The 512x512, depth-3 soup rendered end to end by the reference's own
+    kernels (one point light, expressed as a cone-less spot light) and by the
+    oracle: identical fixed-point images."""
+    wl = scenes.workload_small()
+    sc = wl["scene"]
+    s, rh = _pair(orc, ref, sc)
+    keys, perm, _, _ = s.sort_arrays()
+    ref.apply_perm(rh, _p(perm))
+    canon = s.canon()
+    ref.set_tree(rh, _p(canon), canon.shape[0])
+    img_o, st_o = s.render(wl["camera"], 512, 512, 3)
+    img_r = np.zeros((512 * 512, 3), np.uint32)
+    st_r = abi.RenderStats()
+    ref.render(rh, C.byref(wl["camera"]), 512, 512, 3, 0, 512 * 512, 1 << 18, _p(img_r),
+               C.byref(st_r), 8)
+    assert np.array_equal(img_o, img_r)
+    assert st_o.secondary_rays == st_r.secondary_rays
+    ref.scene_free(rh)
+
+
+@pytest.mark.parametrize("depth", [30, 10, 1])
+def test_pin_terrain_duplicates(orc, ref, depth):
+    """Equal keys: the oracle's bitonic restatement reproduces the reference's
+    (unstable) tie order exactly."""
+    sc = tiny_terrain().scene(1)
+    s = orc.new_scene(sc)
+    s.build(depth, 1, 1)
+    rh = ref.new_scene(sc)
+    kr = np.zeros(sc.n_tris, np.uint32)
+    ref.morton(rh, depth, _p(kr), None, None)
+    pr = np.zeros(sc.n_tris, np.uint32)
+    assert ref.bitonic(_p(kr), sc.n_tris, _p(pr)) == 0
+    keys, perm, _, _ = s.sort_arrays()
+    assert np.array_equal(kr, keys) and np.array_equal(pr, perm)
+    ref.scene_free(rh)
+
+
+@pytest.mark.parametrize("n", [1, 2, 4, 8, 16, 17, 31, 33, 1000])
+def test_pin_bitonic_sizes(orc, ref, n):
+    rng = np.random.default_rng(n)
+    keys = rng.integers(0, 64, size=n).astype(np.uint32)    # many duplicates
+    pr, po = np.zeros(n, np.uint32), np.zeros(n, np.uint32)
+    rr = ref.bitonic(_p(keys), n, _p(pr))
+    ro = orc.sort_bitonic(_p(keys), n, _p(po))
+    assert rr == ro == 0
+    assert np.array_equal(pr, po)
+    assert (np.diff(keys[pr].astype(np.int64)) >= 0).all()
+
+
+@pytest.mark.parametrize("n", [3, 5, 6, 7, 9, 12, 15])
+def test_pin_bitonic_aborts_like_reference(orc, ref, n):
+    """Non-power-of-two N < 16 make the reference launch zero work-items and
+    exit(1) (bvh-builder.cpp:403-406); both report it as -1."""
+    keys = np.arange(n, dtype=np.uint32)[::-1].copy()
+    p = np.zeros(n, np.uint32)
+    assert ref.bitonic(_p(keys), n, _p(p)) == -1
+    assert orc.sort_bitonic(_p(keys), n, _p(p)) == -1
