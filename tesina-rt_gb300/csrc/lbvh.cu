@@ -44,6 +44,15 @@ __device__ __forceinline__ uint32_t ld_acquire(const uint32_t* p) {
 __device__ __forceinline__ void st_release(uint32_t* p, uint32_t v) {
     asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
+// atomicAdd with acquire-release ordering at GPU scope: the caller's earlier
+// writes are visible to whoever reads the counter's new value, and the
+// caller sees everything released by earlier adders.
+__device__ __forceinline__ uint32_t atomic_add_acq_rel(uint32_t* p, uint32_t v) {
+    uint32_t old;
+    asm volatile("atom.add.acq_rel.gpu.global.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v)
+                 : "memory");
+    return old;
+}
 
 // ---------------------------------------------------------------------------
 // scene AABB
@@ -441,9 +450,7 @@ __global__ void __launch_bounds__(256) k_emit_refit(uint32_t n, const uint32_t* 
             rec_i[3] = cnt;
             rangeR[p] = r;
         }
-        __threadfence();
-        if (atomicAdd(&flags[p], 1u) == 0) return;   // first to arrive: the sibling finishes p
-        __threadfence();
+        if (atomic_add_acq_rel(&flags[p], 1u) == 0) return;   // the sibling finishes p
         // second arrival: both children of p are in its record
         const float4 n0 = __ldcg(&nodes[4 * (size_t)p]);
         const float4 n1 = __ldcg(&nodes[4 * (size_t)p + 1]);

@@ -100,20 +100,30 @@ __device__ __forceinline__ TRay make_tray(f3 o, f3 d, f3 inv, float tmin) {
     return r;
 }
 
+// Three-operand min / max (sm_100+): exact selections with the same NaN
+// rule as fminf / fmaxf (a NaN operand is dropped), so chaining them gives the
+// same value as the reference's two-operand sequence.
+__device__ __forceinline__ float max3f(float a, float b, float c) {
+    float d;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+__device__ __forceinline__ float min3f(float a, float b, float c) {
+    float d;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+
 // Slab test of bbox_hit (trace-bvh.cl:247-273).  Returns the entry distance A
-// = max(tMin, per-axis near) and whether A <= min(tMax, per-axis far).
+// = max(tMin, per-axis near) and whether A <= min(tMax, per-axis far).  The
+// per-axis selections are exact, so their grouping does not change A.
 __device__ __forceinline__ bool slab(const TRay& r, float tmax, float lox, float loy, float loz,
                                      float hix, float hiy, float hiz, float& A) {
     float ltx = (lox - r.o.x) * r.inv.x, htx = (hix - r.o.x) * r.inv.x;
     float lty = (loy - r.o.y) * r.inv.y, hty = (hiy - r.o.y) * r.inv.y;
     float ltz = (loz - r.o.z) * r.inv.z, htz = (hiz - r.o.z) * r.inv.z;
-    float tmin = r.tmin;
-    tmin = fmaxf(tmin, fminf(ltx, htx));
-    tmax = fminf(tmax, fmaxf(ltx, htx));
-    tmin = fmaxf(tmin, fminf(lty, hty));
-    tmax = fminf(tmax, fmaxf(lty, hty));
-    tmin = fmaxf(tmin, fminf(ltz, htz));
-    tmax = fminf(tmax, fmaxf(ltz, htz));
+    const float tmin = fmaxf(max3f(r.tmin, fminf(ltx, htx), fminf(lty, hty)), fminf(ltz, htz));
+    tmax = fminf(min3f(tmax, fmaxf(ltx, htx), fmaxf(lty, hty)), fmaxf(ltz, htz));
     A = tmin;
     return tmin <= tmax;
 }
