@@ -303,6 +303,34 @@ RT_API int32_t rt_render(rt_ctx* ctx, rt_scene* scene, const rt_camera* cam, int
                   int32_t height, int32_t max_bounces, uint8_t* d_rgba, uint32_t* d_image_rgb,
                   rt_render_stats* d_stats, rt_stream s);
 
+/* ------------------------------------------------------------------------ */
+/* Render kernel configuration and autotuning                               */
+/* ------------------------------------------------------------------------ */
+/* All variants produce identical images; they differ in block size and in
+ * the register budget (minimum resident blocks per SM), the number of
+ * resident blocks launched, and the pixels a warp takes per work fetch. */
+typedef struct rt_render_config {
+    int32_t variant;         /* kernel variant, 0 .. rt_render_variants() - 1           */
+    int32_t blocks_per_sm;   /* resident blocks per SM to launch; 0 = occupancy maximum */
+    int32_t chunk;           /* pixels per warp work fetch: 32, 64, 128 or 256          */
+    int32_t stack_depth;     /* traversal stack entries (fixed: 32, enough for depth <= 31) */
+} rt_render_config;
+
+RT_API int32_t rt_render_variants(int32_t* count);
+/* threads per block, minimum blocks per SM it was compiled for, and the
+ * blocks per SM the occupancy calculator allows on this context's GPU. */
+RT_API int32_t rt_render_variant_info(rt_ctx* ctx, int32_t variant, int32_t* threads,
+                                      int32_t* min_blocks, int32_t* occupancy_blocks);
+RT_API int32_t rt_set_render_config(rt_ctx* ctx, const rt_render_config* cfg);
+RT_API int32_t rt_get_render_config(rt_ctx* ctx, rt_render_config* cfg);
+/* Times every variant x resident-block count x chunk on this scene and
+ * camera (trials timed launches each, best kept), installs the fastest
+ * configuration in the context and returns it.  Results are cached per
+ * (image size, triangle count, bounces) class in the context. */
+RT_API int32_t rt_autotune_render(rt_ctx* ctx, rt_scene* scene, const rt_camera* cam,
+                                  int32_t width, int32_t height, int32_t max_bounces,
+                                  int32_t trials, rt_render_config* best, float* best_ms);
+
 /* End-to-end convenience: host vertices in, host image out, synchronous:
  * optional vertex update -> LBVH build -> render -> RGBA8 to host. */
 RT_API int32_t rt_render_host(rt_ctx* ctx, rt_scene* scene, const float* h_pos4, const float* h_nrm4,

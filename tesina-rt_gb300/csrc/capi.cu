@@ -14,6 +14,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <algorithm>
 #include <cmath>
 #include <new>
 #include <vector>
@@ -237,10 +238,13 @@ int32_t rt_init(rt_ctx** out, int32_t device) {
     CU(cudaMalloc(&c->d_status, sizeof(uint32_t)));
     CU(cudaMemset(c->d_status, 0, sizeof(uint32_t)));
     CU(cudaMalloc(&c->d_work, 64 * sizeof(uint32_t)));
-    int bps = 0;
-    CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, rt::launch_render_kernel_ptr(),
-                                                     rt::RENDER_THREADS, 0));
-    c->render_blocks_per_sm = bps > 0 ? bps : 1;
+    for (int v = 0; v < rt::render_variant_count() && v < 16; ++v) {
+        int threads = 0, minb = 0, bps = 0;
+        const void* fn = nullptr;
+        rt::render_variant_info(v, &threads, &minb, &fn);
+        CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fn, threads, 0));
+        c->variant_occupancy[v] = bps > 0 ? bps : 1;
+    }
     volatile float one = 1.0f, m = 1e6f;
     c->inv1e6 = one / m;
     *out = c;
@@ -737,6 +741,58 @@ int32_t rt_fb_copy(rt_ctx* c, const uint32_t* img, uint8_t* rgba, size_t px, rt_
 // ---------------------------------------------------------------------------
 // fused path
 // ---------------------------------------------------------------------------
+static cudaError_t launch_render_cfg(rt_ctx* c, rt::RenderArgs a, const rt_render_config& cfg,
+                                     cudaStream_t cs) {
+    int threads = 0, minb = 0;
+    rt::render_variant_info(cfg.variant, &threads, &minb, nullptr);
+    int bps = cfg.blocks_per_sm > 0 ? cfg.blocks_per_sm : c->variant_occupancy[cfg.variant];
+    if (bps > c->variant_occupancy[cfg.variant]) bps = c->variant_occupancy[cfg.variant];
+    const int64_t pixels = (int64_t)a.width * a.height;
+    const int64_t warps_needed = (pixels + cfg.chunk - 1) / cfg.chunk;
+    int64_t grid = (int64_t)c->num_sms * bps;
+    const int64_t max_useful = (warps_needed + threads / 32 - 1) / (threads / 32);
+    if (grid > max_useful) grid = max_useful;
+    if (grid < 1) grid = 1;
+    a.chunk = cfg.chunk;
+    return rt::launch_render(a, cfg.variant, (int)grid, cs);
+}
+
+static bool valid_cfg(const rt_render_config& cfg) {
+    return cfg.variant >= 0 && cfg.variant < rt::render_variant_count() && cfg.blocks_per_sm >= 0 &&
+           (cfg.chunk == 32 || cfg.chunk == 64 || cfg.chunk == 128 || cfg.chunk == 256);
+}
+
+int32_t rt_render_variants(int32_t* count) {
+    if (!count) return fail(RT_ERR_INVALID, "rt_render_variants: null argument");
+    *count = rt::render_variant_count();
+    return RT_OK;
+}
+
+int32_t rt_render_variant_info(rt_ctx* c, int32_t v, int32_t* threads, int32_t* min_blocks,
+                               int32_t* occ) {
+    if (!c) return fail(RT_ERR_INVALID, "rt_render_variant_info: null context");
+    int t = 0, m = 0;
+    if (rt::render_variant_info(v, &t, &m, nullptr))
+        return fail(RT_ERR_INVALID, "rt_render_variant_info: no variant %d", v);
+    if (threads) *threads = t;
+    if (min_blocks) *min_blocks = m;
+    if (occ) *occ = c->variant_occupancy[v];
+    return RT_OK;
+}
+
+int32_t rt_set_render_config(rt_ctx* c, const rt_render_config* cfg) {
+    if (!c || !cfg) return fail(RT_ERR_INVALID, "rt_set_render_config: null argument");
+    if (!valid_cfg(*cfg)) return fail(RT_ERR_INVALID, "rt_set_render_config: invalid configuration");
+    c->render_cfg = *cfg;
+    c->render_cfg.stack_depth = 32;
+    return RT_OK;
+}
+
+int32_t rt_get_render_config(rt_ctx* c, rt_render_config* cfg) {
+    if (!c || !cfg) return fail(RT_ERR_INVALID, "rt_get_render_config: null argument");
+    *cfg = c->render_cfg;
+    return RT_OK;
+}
 int32_t rt_render(rt_ctx* c, rt_scene* s, const rt_camera* cam, int32_t w, int32_t h,
                   int32_t max_bounces, uint8_t* rgba, uint32_t* img, rt_render_stats* stats,
                   rt_stream stream) {
@@ -762,11 +818,99 @@ int32_t rt_render(rt_ctx* c, rt_scene* s, const rt_camera* cam, int32_t w, int32
     a.stats = stats;
     a.work_counter = c->d_work;
     a.status = c->d_status;
-    const int64_t warps_needed = ((int64_t)w * h + 31) / 32;
-    int64_t grid = (int64_t)c->num_sms * c->render_blocks_per_sm;
-    const int64_t max_useful = (warps_needed + (rt::RENDER_THREADS / 32) - 1) / (rt::RENDER_THREADS / 32);
-    if (grid > max_useful) grid = max_useful;
-    CU(rt::launch_render(a, (int)grid, cs));
+    CU(launch_render_cfg(c, a, c->render_cfg, cs));
+    return RT_OK;
+}
+
+static uint64_t tune_key(int w, int h, uint32_t n, int bounces) {
+    auto lg = [](uint64_t x) {
+        int k = 0;
+        while (x > 1) {
+            x >>= 1;
+            ++k;
+        }
+        return (uint64_t)k;
+    };
+    return (lg((uint64_t)w * h) << 16) | (lg(n) << 8) | (uint64_t)(bounces & 0xff);
+}
+
+int32_t rt_autotune_render(rt_ctx* c, rt_scene* s, const rt_camera* cam, int32_t w, int32_t h,
+                           int32_t max_bounces, int32_t trials, rt_render_config* best,
+                           float* best_ms) {
+    if (!c || !cam) return fail(RT_ERR_INVALID, "rt_autotune_render: null argument");
+    int32_t r = need_built(s, "rt_autotune_render");
+    if (r) return r;
+    if (w <= 0 || h <= 0) return fail(RT_ERR_INVALID, "rt_autotune_render: bad size");
+    if (trials < 1) trials = 1;
+    const uint64_t key = tune_key(w, h, s->N, max_bounces);
+    auto it = c->tuned.find(key);
+    if (it != c->tuned.end()) {
+        c->render_cfg = it->second;
+        if (best) *best = it->second;
+        if (best_ms) *best_ms = -1.0f;
+        return RT_OK;
+    }
+    cudaStream_t cs = c->stream;
+    uint8_t* rgba = nullptr;
+    CU(cudaMalloc(&rgba, 4 * (size_t)w * h));
+    cudaEvent_t e0, e1;
+    CU(cudaEventCreate(&e0));
+    CU(cudaEventCreate(&e1));
+    rt::RenderArgs a;
+    a.scene = view_of(s);
+    a.lights = s->lights;
+    a.cam = *cam;
+    a.width = w;
+    a.height = h;
+    a.max_bounces = max_bounces;
+    a.inv1e6 = c->inv1e6;
+    a.rgba = rgba;
+    a.image_rgb = nullptr;
+    a.stats = nullptr;
+    a.work_counter = c->d_work;
+    a.status = c->d_status;
+    rt_render_config bestc = c->render_cfg;
+    float bestt = 1e30f;
+    const int chunks[] = {32, 64, 128};
+    for (int v = 0; v < rt::render_variant_count(); ++v) {
+        const int occ = c->variant_occupancy[v];
+        const int bps_list[] = {occ, occ > 1 ? (occ + 1) / 2 : occ};
+        for (int bi = 0; bi < 2; ++bi) {
+            if (bi == 1 && bps_list[1] == bps_list[0]) continue;
+            for (int ch : chunks) {
+                rt_render_config cfg = {v, bps_list[bi], ch, 32};
+                std::vector<float> ts;
+                for (int t = 0; t < trials + 1; ++t) {   // the first launch warms caches
+                    cudaMemsetAsync(c->d_work, 0, sizeof(uint32_t), cs);
+                    cudaEventRecord(e0, cs);
+                    cudaError_t e = launch_render_cfg(c, a, cfg, cs);
+                    cudaEventRecord(e1, cs);
+                    if (e != cudaSuccess) {
+                        cudaFree(rgba);
+                        return fail(RT_ERR_CUDA, "rt_autotune_render: %s", cudaGetErrorString(e));
+                    }
+                    cudaEventSynchronize(e1);
+                    float ms = 0.f;
+                    cudaEventElapsedTime(&ms, e0, e1);
+                    if (t > 0) ts.push_back(ms);
+                }
+                std::sort(ts.begin(), ts.end());
+                const float tmin = ts[ts.size() / 2];   // median of the timed launches
+                if (tmin < bestt) {
+                    bestt = tmin;
+                    bestc = cfg;
+                }
+            }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(rgba);
+    CU(cudaGetLastError());
+    c->render_cfg = bestc;
+    c->tuned[key] = bestc;
+    if (best) *best = bestc;
+    if (best_ms) *best_ms = bestt;
     return RT_OK;
 }
 

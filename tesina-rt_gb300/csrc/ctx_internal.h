@@ -4,6 +4,8 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#include <map>
+
 #include "../../include/rt_cuda.h"
 
 struct rt_ctx {
@@ -19,6 +21,9 @@ struct rt_ctx {
     size_t d_out_cap = 0;
     rt_render_stats* d_stats = nullptr;  // rt_render_host counters
     float inv1e6 = 1.0f / 1e6f;
+    rt_render_config render_cfg = {4, 0, 32, 32};   // variant (128 threads, 8 blocks/SM)
+    int variant_occupancy[16] = {0};                // resident blocks per SM per variant
+    std::map<uint64_t, rt_render_config> tuned;     // autotuner cache by workload class
 };
 
 namespace rt {

@@ -332,7 +332,8 @@ __device__ __forceinline__ uint8_t to_unorm8(uint32_t v, float inv1e6) {
 // fused per-pixel Whitted path (Renderer::render_to_framebuffer, one pixel
 // per lane, persistent warps fetching 32 pixels at a time)
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(RENDER_THREADS) k_render(RenderArgs a) {
+template <int THREADS, int MINB>
+__global__ void __launch_bounds__(THREADS, MINB) k_render(RenderArgs a) {
     const SceneView S = a.scene;
     __shared__ BvhHeader sH;
     __shared__ rt_lights sL;
@@ -344,11 +345,13 @@ __global__ void __launch_bounds__(RENDER_THREADS) k_render(RenderArgs a) {
     const int lane = threadIdx.x & 31;
     const int pixels = a.width * a.height;
     uint64_t n_sec = 0, n_shadow = 0, n_hits = 0, n_prim = 0;
+    const int chunk = a.chunk;   // pixels a warp takes per fetch (multiple of 32)
     for (;;) {
-        int base = 0;
-        if (lane == 0) base = (int)atomicAdd(a.work_counter, 32u);
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (base >= pixels) break;
+        int base0 = 0;
+        if (lane == 0) base0 = (int)atomicAdd(a.work_counter, (unsigned)chunk);
+        base0 = __shfl_sync(0xffffffffu, base0, 0);
+        if (base0 >= pixels) break;
+        for (int base = base0; base < base0 + chunk && base < pixels; base += 32) {
         const int gid = base + lane;
         if (gid < pixels) {
             int x, y;
@@ -397,6 +400,7 @@ __global__ void __launch_bounds__(RENDER_THREADS) k_render(RenderArgs a) {
             px.z = to_unorm8(acc_b, a.inv1e6);
             px.w = 255;
             reinterpret_cast<uchar4*>(a.rgba)[pix] = px;
+        }
         }
     }
     if (a.stats) {
@@ -622,10 +626,32 @@ __global__ void k_fb_copy(const uint32_t* __restrict__ img, uchar4* __restrict__
 // ---------------------------------------------------------------------------
 static unsigned blocks(size_t n, int t) { return (unsigned)((n + t - 1) / t); }
 
-const void* launch_render_kernel_ptr() { return (const void*)k_render; }
+// Kernel variants the autotuner chooses from: block size x minimum resident
+// blocks per SM (which bounds the registers per thread).
+struct RenderVariant {
+    int threads, min_blocks;
+    void (*fn)(RenderArgs);
+};
+static const RenderVariant kVariants[] = {
+    {64, 8, k_render<64, 8>},    {64, 12, k_render<64, 12>},  {128, 4, k_render<128, 4>},
+    {128, 6, k_render<128, 6>},  {128, 8, k_render<128, 8>},  {256, 2, k_render<256, 2>},
+    {256, 3, k_render<256, 3>},  {256, 4, k_render<256, 4>},
+};
+constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
-cudaError_t launch_render(const RenderArgs& a, int grid, cudaStream_t s) {
-    k_render<<<grid, RENDER_THREADS, 0, s>>>(a);
+int render_variant_count() { return kNumVariants; }
+
+int render_variant_info(int v, int* threads, int* min_blocks, const void** fn) {
+    if (v < 0 || v >= kNumVariants) return -1;
+    if (threads) *threads = kVariants[v].threads;
+    if (min_blocks) *min_blocks = kVariants[v].min_blocks;
+    if (fn) *fn = (const void*)kVariants[v].fn;
+    return 0;
+}
+
+cudaError_t launch_render(const RenderArgs& a, int variant, int grid, cudaStream_t s) {
+    if (variant < 0 || variant >= kNumVariants) return cudaErrorInvalidValue;
+    kVariants[variant].fn<<<grid, kVariants[variant].threads, 0, s>>>(a);
     return cudaGetLastError();
 }
 

@@ -7,7 +7,6 @@
 
 namespace rt {
 
-constexpr int RENDER_THREADS = 128;
 
 struct RenderArgs {
     SceneView scene;
@@ -20,10 +19,13 @@ struct RenderArgs {
     rt_render_stats* stats;       // optional, accumulated
     uint32_t* work_counter;       // zeroed before launch
     uint32_t* status;
+    int chunk;                    // pixels per warp work fetch, multiple of 32
 };
 
-cudaError_t launch_render(const RenderArgs& a, int grid, cudaStream_t s);
-const void* launch_render_kernel_ptr();
+// Render kernel variants (block size, minimum blocks per SM) for the autotuner.
+int render_variant_count();
+int render_variant_info(int v, int* threads, int* min_blocks, const void** fn);
+cudaError_t launch_render(const RenderArgs& a, int variant, int grid, cudaStream_t s);
 cudaError_t launch_gen_primary(const rt_camera& cam, int w, int h, int q, const rt_pixel_sample* ps,
                                size_t count, size_t offset, rt_sample* out, cudaStream_t s);
 cudaError_t launch_trace(const SceneView& S, const rt_sample* smp, int n, rt_hit* hits,

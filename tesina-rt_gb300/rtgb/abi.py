@@ -36,6 +36,15 @@ class BvhCfg(C.Structure):
     _fields_ = [("depth", C.c_int32), ("min_leaf_size", C.c_int32)]
 
 
+class RenderConfig(C.Structure):
+    _fields_ = [("variant", C.c_int32), ("blocks_per_sm", C.c_int32), ("chunk", C.c_int32),
+                ("stack_depth", C.c_int32)]
+
+    def __repr__(self):
+        return "RenderConfig(variant=%d, blocks_per_sm=%d, chunk=%d)" % (
+            self.variant, self.blocks_per_sm, self.chunk)
+
+
 class RenderStats(C.Structure):
     _fields_ = [("primary_rays", C.c_uint64), ("secondary_rays", C.c_uint64),
                 ("shadow_rays", C.c_uint64), ("hits", C.c_uint64)]

@@ -56,6 +56,11 @@ SIGNATURES = {
     "rt_render": (I32, [P, P, P, I32, I32, I32, P, P, P, P]),
     "rt_render_host": (I32, [P, P, P, P, U32, P, P, I32, I32, I32, P, P, P]),
     "rt_sort_pairs_noalloc": (I32, [P, P, P, P, P, U32, I32, P]),
+    "rt_render_variants": (I32, [C.POINTER(I32)]),
+    "rt_render_variant_info": (I32, [P, I32, C.POINTER(I32), C.POINTER(I32), C.POINTER(I32)]),
+    "rt_set_render_config": (I32, [P, P]),
+    "rt_get_render_config": (I32, [P, P]),
+    "rt_autotune_render": (I32, [P, P, P, I32, I32, I32, I32, P, C.POINTER(F)]),
 }
 
 
@@ -141,6 +146,26 @@ class Context:
         count = w * h if count is None else count
         check(self.lib, self.lib.rt_gen_primary(self.h, C.byref(cam), w, h, quad, 1, None, count,
                                                 offset, out_buf.ptr, stream))
+
+    def render_config(self):
+        cfg = abi.RenderConfig()
+        check(self.lib, self.lib.rt_get_render_config(self.h, C.byref(cfg)))
+        return cfg
+
+    def set_render_config(self, variant, blocks_per_sm=0, chunk=32):
+        cfg = abi.RenderConfig(variant, blocks_per_sm, chunk, 32)
+        check(self.lib, self.lib.rt_set_render_config(self.h, C.byref(cfg)))
+
+    def variants(self):
+        n = I32(0)
+        check(self.lib, self.lib.rt_render_variants(C.byref(n)))
+        out = []
+        for v in range(n.value):
+            t, m, o = I32(0), I32(0), I32(0)
+            check(self.lib, self.lib.rt_render_variant_info(self.h, v, C.byref(t), C.byref(m),
+                                                            C.byref(o)))
+            out.append((t.value, m.value, o.value))
+        return out
 
     def fb_copy(self, img_buf, rgba_buf, pixels, stream=None):
         check(self.lib, self.lib.rt_fb_copy(self.h, img_buf.ptr, rgba_buf.ptr, pixels, stream))
@@ -296,6 +321,14 @@ class Scene:
                                                 C.byref(cfg), C.byref(cam), w, h, max_bounces,
                                                 _p(rgba), C.byref(st), stream))
         return rgba, st
+
+    def autotune(self, cam, w, h, max_bounces, trials=2):
+        cfg = abi.RenderConfig()
+        ms = F(0)
+        check(self.lib, self.lib.rt_autotune_render(self.ctx.h, self.h, C.byref(cam), w, h,
+                                                    max_bounces, trials, C.byref(cfg),
+                                                    C.byref(ms)))
+        return cfg, ms.value
 
     def close(self):
         if self.h:

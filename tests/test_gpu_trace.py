@@ -183,3 +183,37 @@ def test_render_host_e2e(ctx, orc):
     rimg, rst = o.render(cam, 128, 128, 2)
     assert np.array_equal(rgba, pyoracle.fb_copy(orc, rimg))
     assert st.primary_rays == 128 * 128
+
+
+def test_render_variants_identical(ctx, orc):
+    """Every kernel variant / chunk / residency the autotuner can pick gives
+    the same image; the autotuner installs and caches its choice."""
+    ter = tiny_terrain(96, 48, 12)
+    sc = ter.scene(1)
+    cam = scenes.camera((0.0, 4.0, -10.0), (0.0, 0.0, 0.0), aspect=200 / 120)
+    g = capi.Scene(ctx, sc)
+    g.build(30, 1)
+    w, h = 200, 120
+    rgba_d, img_d = ctx.alloc(4 * w * h), ctx.alloc(12 * w * h)
+    saved = ctx.render_config()
+    images = []
+    for v, (threads, minb, occ) in enumerate(ctx.variants()):
+        assert occ >= 1 and threads in (64, 128, 256)
+        for chunk in (32, 128, 256):
+            ctx.set_render_config(v, max(1, occ // 2), chunk)
+            g.render(cam, w, h, 4, rgba_d, img_d)
+            ctx.sync()
+            images.append(img_d.read(np.uint32))
+    for im in images[1:]:
+        assert np.array_equal(im, images[0])
+    cfg, ms = g.autotune(cam, w, h, 4, trials=1)
+    assert ms > 0 and 0 <= cfg.variant < len(ctx.variants())
+    cur = ctx.render_config()
+    assert (cur.variant, cur.blocks_per_sm, cur.chunk) == (cfg.variant, cfg.blocks_per_sm, cfg.chunk)
+    cfg2, ms2 = g.autotune(cam, w, h, 4, trials=1)          # cached: no timing
+    assert ms2 < 0 and cfg2.variant == cfg.variant
+    o = orc.new_scene(sc)
+    o.build(30, 1, 0)
+    rimg, _ = o.render(cam, w, h, 4)
+    assert np.array_equal(images[0].reshape(-1, 3), rimg)
+    ctx.set_render_config(saved.variant, saved.blocks_per_sm, saved.chunk)
