@@ -331,6 +331,43 @@ RT_API int32_t rt_autotune_render(rt_ctx* ctx, rt_scene* scene, const rt_camera*
                                   int32_t width, int32_t height, int32_t max_bounces,
                                   int32_t trials, rt_render_config* best, float* best_ms);
 
+/* ------------------------------------------------------------------------ */
+/* Batched form: many scenes per build launch, many images per render launch */
+/* ------------------------------------------------------------------------ */
+typedef struct rt_batch rt_batch;
+
+/* One image of a batch.  Images are packed in view order in one RGBA8
+ * buffer: view v starts at pixel rgba_offset = sum of the earlier views'
+ * width * height. */
+typedef struct rt_batch_view {
+    rt_scene* scene;             /* uploaded scene (several views may share one) */
+    rt_camera cam;
+    int32_t   width, height, max_bounces;
+    uint32_t  rgba_offset;
+} rt_batch_view;
+
+RT_API int32_t rt_batch_create(rt_ctx* ctx, rt_batch** batch);
+RT_API int32_t rt_batch_destroy(rt_ctx* ctx, rt_batch* batch);
+/* Declares the views (<= 4096) and their distinct scenes (<= 1024), one LBVH
+ * configuration for all of them, and prepares device tables and buffers. */
+RT_API int32_t rt_batch_set(rt_ctx* ctx, rt_batch* batch, const rt_batch_view* views,
+                            int32_t count, const rt_bvh_cfg* cfg);
+/* Builds the LBVH of every distinct scene in ONE persistent cooperative
+ * launch; results are the same as rt_bvh_build_lbvh on each scene. */
+RT_API int32_t rt_batch_build(rt_ctx* ctx, rt_batch* batch, rt_stream s);
+/* Renders every view in ONE persistent launch into d_rgba (total pixels x 4
+ * bytes); same pixels as rt_render per view.  d_stats optional, accumulated. */
+RT_API int32_t rt_batch_render(rt_ctx* ctx, rt_batch* batch, uint8_t* d_rgba,
+                               rt_render_stats* d_stats, rt_stream s);
+/* Captures build + render into a CUDA graph (on the context stream).  Each
+ * replay rebuilds every scene from the triangle order the capture saw and
+ * renders; d_stats (optional) is zeroed by every replay. */
+RT_API int32_t rt_batch_capture(rt_ctx* ctx, rt_batch* batch, uint8_t* d_rgba,
+                                rt_render_stats* d_stats);
+RT_API int32_t rt_batch_replay(rt_ctx* ctx, rt_batch* batch, rt_stream s);
+RT_API int32_t rt_batch_info(rt_ctx* ctx, rt_batch* batch, uint32_t* scenes,
+                             uint32_t* triangles, uint32_t* pixels);
+
 /* End-to-end convenience: host vertices in, host image out, synchronous:
  * optional vertex update -> LBVH build -> render -> RGBA8 to host. */
 RT_API int32_t rt_render_host(rt_ctx* ctx, rt_scene* scene, const float* h_pos4, const float* h_nrm4,

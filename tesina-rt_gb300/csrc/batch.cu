@@ -1,0 +1,327 @@
+// batch.cu — many scenes and many images per launch.
+//
+// rt_batch_build builds the LBVHs of every distinct scene of a batch in ONE
+// persistent cooperative launch: the stages of BVHBuilder::build_lbvh
+// (src/rt/bvh-builder.cpp:201-741) run over the concatenated triangle index
+// space of all scenes, separated by grid-wide barriers; the radix passes use
+// per-scene histograms and look-back regions, so each scene is sorted on its
+// own while all scenes' tiles share the machine.  Results land in each
+// scene's own buffers, exactly as a one-scene build would write them.
+//
+// rt_batch_render renders every view of the batch in ONE persistent launch:
+// warps fetch chunks of the concatenated pixel space of all images and run
+// the same per-pixel Whitted path as rt_render (trace_dev.cuh).
+//
+// rt_batch_capture records build + render in a CUDA graph that
+// rt_batch_replay relaunches.
+#include <cooperative_groups.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "../../include/rt_cuda.h"
+#include "batch.cuh"
+#include "lbvh_dev.cuh"
+#include "rt_internal.cuh"
+#include "trace_dev.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace rt {
+
+constexpr int kMaxBatchScenes = 1024;
+
+// Scene index of global element g (offsets ascending, off[count] = total).
+__device__ __forceinline__ int find_segment(const uint32_t* off, int count, uint32_t g) {
+    int lo = 0, hi = count - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (off[mid] <= g)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
+
+__global__ void __launch_bounds__(SORT_THREADS) k_batch_build(BatchBuildArgs A) {
+    cg::grid_group grid = cg::this_grid();
+    __shared__ SortSmem S;
+    __shared__ uint32_t s_toff[kMaxBatchScenes + 1];
+    __shared__ uint32_t s_tileoff[kMaxBatchScenes + 1];
+    __shared__ uint32_t s_hist[4][256];
+    __shared__ float s_red[SORT_WARPS][6];
+    __shared__ int s_cur;
+    const int nsc = A.count;
+    for (int i = threadIdx.x; i <= nsc; i += blockDim.x) {
+        s_toff[i] = A.tri_off[i];
+        s_tileoff[i] = A.tile_off[i];
+    }
+    __syncthreads();
+    const uint32_t total = s_toff[nsc];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const uint32_t nblk = gridDim.x;
+    const uint32_t gtid = blockIdx.x * blockDim.x + tid, gthreads = nblk * blockDim.x;
+
+    // ---- stage 0: initialise bounds, histograms, look-back, arrival flags ---
+    for (uint32_t i = gtid; i < (uint32_t)nsc * 8; i += gthreads)
+        A.scenes[i >> 3].bounds[i & 7] = (i & 7) < 3 ? 0xffffffffu : 0u;
+    for (uint32_t i = gtid; i < (uint32_t)nsc * 1024; i += gthreads)
+        A.scenes[i >> 10].hist[i & 1023] = 0;
+    for (int sc = 0; sc < nsc; ++sc) {
+        const BatchScene& B = A.scenes[sc];
+        const size_t words = (size_t)B.passes * (s_tileoff[sc + 1] - s_tileoff[sc]) * 256;
+        for (size_t i = gtid; i < words; i += gthreads) B.lookback[i] = 0;
+        for (uint32_t i = gtid; i + 1 < B.n; i += gthreads) B.flags[i] = 0;
+    }
+    if (gtid < 4) A.tile_ctr[gtid] = 0;
+    grid.sync();
+
+    // ---- stage 1: scene AABBs (steps of 256 consecutive triangles) ----------
+    for (uint32_t step = blockIdx.x; (size_t)step * SORT_THREADS < total; step += nblk) {
+        const uint32_t g = step * SORT_THREADS + tid;
+        const bool ok = g < total;
+        int s = ok ? find_segment(s_toff, nsc, g) : -1;
+        float lo[3] = {1e37f, 1e37f, 1e37f}, hi[3] = {-1e37f, -1e37f, -1e37f};
+        if (ok) {
+            const BatchScene& B = A.scenes[s];
+            tri_aabb(B.pos, B.idx_in, g - s_toff[s], lo, hi);
+        }
+        const uint32_t last = min(total - 1, step * SORT_THREADS + SORT_THREADS - 1);
+        const int s0 = find_segment(s_toff, nsc, step * SORT_THREADS);
+        const int s1 = find_segment(s_toff, nsc, last);
+        if (s0 == s1) {   // the whole step is one scene: block reduction, 6 atomics
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1)
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    lo[c] = fminf(lo[c], __shfl_xor_sync(0xffffffffu, lo[c], off));
+                    hi[c] = fmaxf(hi[c], __shfl_xor_sync(0xffffffffu, hi[c], off));
+                }
+            if (lane == 0)
+                for (int c = 0; c < 3; ++c) {
+                    s_red[warp][c] = lo[c];
+                    s_red[warp][3 + c] = hi[c];
+                }
+            __syncthreads();
+            if (tid < 3) {
+                float a = s_red[0][tid], b = s_red[0][3 + tid];
+                for (int k = 1; k < SORT_WARPS; ++k) {
+                    a = fminf(a, s_red[k][tid]);
+                    b = fmaxf(b, s_red[k][3 + tid]);
+                }
+                atomicMin(&A.scenes[s0].bounds[tid], f2o(a));
+                atomicMax(&A.scenes[s0].bounds[3 + tid], f2o(b));
+            }
+            __syncthreads();
+        } else if (ok) {   // a scene boundary inside the step: per-triangle atomics
+            for (int c = 0; c < 3; ++c) {
+                atomicMin(&A.scenes[s].bounds[c], f2o(lo[c]));
+                atomicMax(&A.scenes[s].bounds[3 + c], f2o(hi[c]));
+            }
+        }
+    }
+    grid.sync();
+
+    // ---- stage 2: Morton codes + per-scene digit histograms ------------------
+    // Each block walks a contiguous range of steps, keeping the histogram of
+    // the scene it is in and flushing it when the scene changes.
+    {
+        const uint32_t nsteps = (total + SORT_THREADS - 1) / SORT_THREADS;
+        const uint32_t per = (nsteps + nblk - 1) / nblk;
+        const uint32_t st0 = blockIdx.x * per, st1 = min(nsteps, st0 + per);
+        for (int i = tid; i < 4 * 256; i += blockDim.x) (&s_hist[0][0])[i] = 0;
+        if (tid == 0) s_cur = -1;
+        __syncthreads();
+        for (uint32_t step = st0; step < st1; ++step) {
+            const uint32_t g = step * SORT_THREADS + tid;
+            const bool ok = g < total;
+            const uint32_t last = min(total - 1, step * SORT_THREADS + SORT_THREADS - 1);
+            const int s0 = find_segment(s_toff, nsc, step * SORT_THREADS);
+            const int s1 = find_segment(s_toff, nsc, last);
+            const bool single = s0 == s1;
+            if (single && s0 != s_cur) {   // flush the previous scene's histogram
+                if (s_cur >= 0) {
+                    const BatchScene& P = A.scenes[s_cur];
+                    for (int i = tid; i < P.passes * 256; i += blockDim.x) {
+                        const uint32_t v = (&s_hist[0][0])[i];
+                        if (v) atomicAdd(&P.hist[i], v);
+                    }
+                }
+                __syncthreads();
+                for (int i = tid; i < 4 * 256; i += blockDim.x) (&s_hist[0][0])[i] = 0;
+                if (tid == 0) s_cur = s0;
+                __syncthreads();
+            }
+            if (ok) {
+                const int s = single ? s0 : find_segment(s_toff, nsc, g);
+                const BatchScene& B = A.scenes[s];
+                const uint32_t li = g - s_toff[s];
+                float lo[3], hi[3];
+                tri_aabb(B.pos, B.idx_in, li, lo, hi);
+                const MortonParams P = morton_params(B.bounds, B.depth);
+                const uint32_t code = morton_code(P, lo, hi);
+                B.keys_unsorted[li] = code;
+                B.vals0[li] = li;
+                for (int p = 0; p < B.passes; ++p) {
+                    const uint32_t d = (code >> (8 * p)) & 255u;
+                    if (single)
+                        atomicAdd(&s_hist[p][d], 1u);
+                    else
+                        atomicAdd(&B.hist[p * 256 + d], 1u);
+                }
+            }
+            __syncthreads();
+        }
+        if (s_cur >= 0) {
+            const BatchScene& P = A.scenes[s_cur];
+            for (int i = tid; i < P.passes * 256; i += blockDim.x) {
+                const uint32_t v = (&s_hist[0][0])[i];
+                if (v) atomicAdd(&P.hist[i], v);
+            }
+        }
+    }
+    grid.sync();
+
+    // ---- stage 3: radix passes; tiles of all scenes share the grid ----------
+    const uint32_t total_tiles = s_tileoff[nsc];
+    for (int p = 0; p < A.passes; ++p) {
+        for (;;) {
+            if (tid == 0) S.tile = atomicAdd(&A.tile_ctr[p], 1u);   // global tile order
+            __syncthreads();
+            const uint32_t t = S.tile;
+            __syncthreads();
+            if (t >= total_tiles) break;
+            const int s = find_segment(s_tileoff, nsc, t);
+            const BatchScene& B = A.scenes[s];
+            const uint32_t lt = t - s_tileoff[s];
+            const int dst = ((B.passes - 1 - p) & 1) ? 0 : 1;   // last pass -> sorted
+            const uint32_t* kin = p == 0 ? B.keys_unsorted : (dst ? B.keys1 : B.keys_sorted);
+            const uint32_t* vin = p == 0 ? B.vals0 : (dst ? B.vals1 : B.vals_sorted);
+            uint32_t* kout = dst ? B.keys_sorted : B.keys1;
+            uint32_t* vout = dst ? B.vals_sorted : B.vals1;
+            const uint32_t ntiles_s = s_tileoff[s + 1] - s_tileoff[s];
+            onesweep_tile(S, lt, kin, vin, kout, vout, B.n, 8 * p, B.hist + 256 * p,
+                          B.lookback + (size_t)p * ntiles_s * 256, A.status);
+        }
+        grid.sync();
+    }
+
+    // ---- stage 4: permutation into sorted order ------------------------------
+    for (uint32_t g = blockIdx.x * blockDim.x + tid; g < total; g += nblk * blockDim.x) {
+        const int s = find_segment(s_toff, nsc, g);
+        const BatchScene& B = A.scenes[s];
+        permute_one(g - s_toff[s], B.vals_sorted, B.idx_in, B.map_in, B.orig_in, B.pos, B.idx_out,
+                    B.map_out, B.orig_out, B.tris, B.leafbox);
+    }
+    grid.sync();
+
+    // ---- stage 5: bottom-up emit + refit -----------------------------------
+    for (uint32_t g = blockIdx.x * blockDim.x + tid; g < total; g += nblk * blockDim.x) {
+        const int s = find_segment(s_toff, nsc, g);
+        const BatchScene& B = A.scenes[s];
+        emit_climb(g - s_toff[s], B.n, B.keys_sorted, B.leafbox, B.nodes, B.flags, B.rangeL,
+                   B.rangeR, B.min_leaf, B.hdr);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// many-image render
+// ---------------------------------------------------------------------------
+template <int THREADS, int MINB>
+__global__ void __launch_bounds__(THREADS, MINB) k_render_batch(BatchRenderArgs A) {
+    __shared__ uint32_t s_poff[kMaxBatchViews + 1];
+    for (int i = threadIdx.x; i <= A.count; i += blockDim.x) s_poff[i] = A.pix_off[i];
+    __syncthreads();
+    const uint32_t total = s_poff[A.count];
+    const int lane = threadIdx.x & 31;
+    uint32_t n_prim = 0, n_sec = 0, n_shadow = 0, n_hits = 0;
+    for (;;) {
+        uint32_t base0 = 0;
+        if (lane == 0) base0 = atomicAdd(A.work_counter, (unsigned)A.chunk);
+        base0 = __shfl_sync(0xffffffffu, base0, 0);
+        if (base0 >= total) break;
+        for (uint32_t base = base0; base < base0 + A.chunk && base < total; base += 32) {
+            const uint32_t g = base + lane;
+            if (g < total) {
+                const int v = find_segment(s_poff, A.count, g);
+                const BatchView& V = A.views[v];
+                const int local = (int)(g - s_poff[v]);
+                int x, y;
+                pixel_of(warp_tile_order(local, V.width, V.height), V.width, V.height, 32, x, y);
+                const BvhHeader H = *V.scene.hdr;
+                const PixelResult pr = render_pixel(V.scene, H, *V.lights, V.cam, x, y, V.width,
+                                                    V.height, V.max_bounces, A.status);
+                ++n_prim;
+                n_sec += pr.secondary;
+                n_shadow += pr.shadow;
+                n_hits += pr.hits;
+                uchar4 px;
+                px.x = to_unorm8(pr.r, A.inv1e6);
+                px.y = to_unorm8(pr.g, A.inv1e6);
+                px.z = to_unorm8(pr.b, A.inv1e6);
+                px.w = 255;
+                reinterpret_cast<uchar4*>(A.rgba)[(size_t)V.rgba_offset + V.width * y + x] = px;
+            }
+        }
+    }
+    if (A.stats) {
+        n_prim = __reduce_add_sync(0xffffffffu, n_prim);
+        n_sec = __reduce_add_sync(0xffffffffu, n_sec);
+        n_shadow = __reduce_add_sync(0xffffffffu, n_shadow);
+        n_hits = __reduce_add_sync(0xffffffffu, n_hits);
+        if (lane == 0) {
+            atomicAdd((unsigned long long*)&A.stats->primary_rays, (unsigned long long)n_prim);
+            atomicAdd((unsigned long long*)&A.stats->secondary_rays, (unsigned long long)n_sec);
+            atomicAdd((unsigned long long*)&A.stats->shadow_rays, (unsigned long long)n_shadow);
+            atomicAdd((unsigned long long*)&A.stats->hits, (unsigned long long)n_hits);
+        }
+    }
+}
+
+struct BatchRenderVariant {
+    int threads, min_blocks;
+    void (*fn)(BatchRenderArgs);
+};
+static const BatchRenderVariant kBatchVariants[] = {
+    {128, 8, k_render_batch<128, 8>},
+    {256, 4, k_render_batch<256, 4>},
+    {128, 6, k_render_batch<128, 6>},
+};
+
+int batch_render_variant_count() { return (int)(sizeof(kBatchVariants) / sizeof(kBatchVariants[0])); }
+
+int batch_render_variant_info(int v, int* threads, const void** fn) {
+    if (v < 0 || v >= batch_render_variant_count()) return -1;
+    if (threads) *threads = kBatchVariants[v].threads;
+    if (fn) *fn = (const void*)kBatchVariants[v].fn;
+    return 0;
+}
+
+cudaError_t launch_batch_render(const BatchRenderArgs& a, int variant, int grid, cudaStream_t s) {
+    kBatchVariants[variant].fn<<<grid, kBatchVariants[variant].threads, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+const void* batch_build_kernel() { return (const void*)k_batch_build; }
+int batch_build_threads() { return SORT_THREADS; }
+int batch_max_scenes() { return kMaxBatchScenes; }
+int sort_tile_size() { return SORT_TILE; }
+
+cudaError_t launch_batch_build(const BatchBuildArgs& a, int grid, cudaStream_t s) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(SORT_THREADS);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_batch_build, a);
+}
+
+}  // namespace rt

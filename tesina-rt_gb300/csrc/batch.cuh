@@ -1,0 +1,81 @@
+// batch.cuh — host interface of the many-scene build and many-image render.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "rt_internal.cuh"
+
+namespace rt {
+
+constexpr int kMaxBatchViews = 4096;
+
+// One scene of a batched build: its arrays, as a one-scene build would use
+// them, plus its slices of the batch scratch.
+struct BatchScene {
+    uint32_t n;
+    int depth, min_leaf, passes;
+    const float4* pos;
+    const uint32_t* idx_in;
+    const uint32_t* map_in;
+    const uint32_t* orig_in;
+    uint32_t* idx_out;
+    uint32_t* map_out;
+    uint32_t* orig_out;
+    uint32_t* keys_unsorted;
+    uint32_t* vals0;
+    uint32_t* keys1;
+    uint32_t* vals1;
+    uint32_t* keys_sorted;
+    uint32_t* vals_sorted;
+    float4* tris;
+    float4* leafbox;
+    float4* nodes;
+    uint32_t* flags;
+    uint32_t* rangeL;
+    uint32_t* rangeR;
+    BvhHeader* hdr;
+    uint32_t* bounds;     // 8 words
+    uint32_t* hist;       // 4 * 256 words
+    uint32_t* lookback;   // passes * tiles * 256 words
+};
+
+struct BatchBuildArgs {
+    const BatchScene* scenes;
+    int count;
+    int passes;
+    const uint32_t* tri_off;    // count + 1 prefix offsets of triangles
+    const uint32_t* tile_off;   // count + 1 prefix offsets of sort tiles
+    uint32_t* tile_ctr;         // one counter per pass
+    uint32_t* status;
+};
+
+struct BatchView {
+    SceneView scene;
+    const rt_lights* lights;
+    rt_camera cam;
+    int width, height, max_bounces;
+    uint32_t rgba_offset;       // first pixel of this image in the output
+};
+
+struct BatchRenderArgs {
+    const BatchView* views;
+    int count;
+    const uint32_t* pix_off;    // count + 1 prefix offsets of pixels
+    uint8_t* rgba;
+    rt_render_stats* stats;
+    uint32_t* work_counter;
+    uint32_t* status;
+    int chunk;
+    float inv1e6;
+};
+
+const void* batch_build_kernel();
+int batch_build_threads();
+int batch_max_scenes();
+int sort_tile_size();
+cudaError_t launch_batch_build(const BatchBuildArgs& a, int grid, cudaStream_t s);
+int batch_render_variant_count();
+int batch_render_variant_info(int v, int* threads, const void** fn);
+cudaError_t launch_batch_render(const BatchRenderArgs& a, int variant, int grid, cudaStream_t s);
+
+}  // namespace rt

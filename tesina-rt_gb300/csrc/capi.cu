@@ -65,38 +65,6 @@ void dfree(T*& p) {
 
 }  // namespace
 
-struct rt_scene {
-    uint32_t V = 0, N = 0, M = 0;
-    uint32_t capV = 0, capN = 0, capM = 0;
-    float4* d_pos = nullptr;
-    float4* d_nrm = nullptr;
-    uint32_t* d_idx[2] = {nullptr, nullptr};
-    uint32_t* d_map[2] = {nullptr, nullptr};
-    uint32_t* d_orig[2] = {nullptr, nullptr};
-    int cur = 0;                     // which of the [2] buffers holds the current order
-    rt_material* d_mats = nullptr;
-    rt_lights lights;
-    // build products
-    uint32_t* d_keys_unsorted = nullptr;
-    uint32_t* d_vals0 = nullptr;
-    uint32_t* d_keys1 = nullptr;
-    uint32_t* d_vals1 = nullptr;
-    uint32_t* d_keys_sorted = nullptr;
-    uint32_t* d_vals_sorted = nullptr;
-    float4* d_tris = nullptr;
-    float4* d_leafbox = nullptr;
-    float4* d_nodes = nullptr;
-    uint32_t* d_flags = nullptr;
-    uint32_t* d_rangeL = nullptr;
-    uint32_t* d_rangeR = nullptr;
-    rt::BvhHeader* d_hdr = nullptr;
-    uint32_t* d_scratch = nullptr;
-    size_t scratch_bytes = 0;
-    uint32_t buildN = 0;             // capacity of the build buffers
-    bool built = false;
-    int depth = 30, min_leaf = 1;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-};
 
 namespace {
 
@@ -131,10 +99,25 @@ void free_geometry(rt_scene* s) {
     s->capV = s->capN = s->capM = 0;
 }
 
-int32_t ensure_build(rt_scene* s, int passes) {
+int32_t check_lights(const rt_lights* L) {
+    if (L->count < 1 || L->count > RT_MAX_LIGHTS)
+        return fail(RT_ERR_INVALID, "light count %d outside [1, %d]", L->count, RT_MAX_LIGHTS);
+    for (int i = 0; i < L->count; ++i) {
+        const int t = L->light[i].type;
+        if (t != RT_SPOT_L && t != RT_DIR_L && t != RT_POINT_L)
+            return fail(RT_ERR_INVALID, "light %d has unknown type %d", i, t);
+    }
+    return RT_OK;
+}
+
+cudaStream_t st(rt_ctx* c, rt_stream s) { return s ? (cudaStream_t)s : c->stream; }
+
+}  // namespace
+
+namespace rt {
+int32_t scene_ensure_build(rt_scene* s) {
     const uint32_t n = s->N;
     const size_t need_scratch = rt::lbvh_scratch_bytes(n, 4);
-    (void)passes;
     if (s->buildN >= n && s->scratch_bytes >= need_scratch && s->d_hdr) return RT_OK;
     free_build(s);
     const size_t nn = n > 1 ? n - 1 : 1;
@@ -153,7 +136,7 @@ int32_t ensure_build(rt_scene* s, int passes) {
     return RT_OK;
 }
 
-rt::SceneView view_of(const rt_scene* s) {
+SceneView scene_view(const rt_scene* s) {
     rt::SceneView v;
     v.nodes = s->d_nodes;
     v.tris = s->d_tris;
@@ -165,20 +148,9 @@ rt::SceneView view_of(const rt_scene* s) {
     return v;
 }
 
-int32_t check_lights(const rt_lights* L) {
-    if (L->count < 1 || L->count > RT_MAX_LIGHTS)
-        return fail(RT_ERR_INVALID, "light count %d outside [1, %d]", L->count, RT_MAX_LIGHTS);
-    for (int i = 0; i < L->count; ++i) {
-        const int t = L->light[i].type;
-        if (t != RT_SPOT_L && t != RT_DIR_L && t != RT_POINT_L)
-            return fail(RT_ERR_INVALID, "light %d has unknown type %d", i, t);
-    }
-    return RT_OK;
-}
+}  // namespace rt
 
-cudaStream_t st(rt_ctx* c, rt_stream s) { return s ? (cudaStream_t)s : c->stream; }
-
-}  // namespace
+static inline rt::SceneView view_of(const rt_scene* s) { return rt::scene_view(s); }
 
 extern "C" {
 
@@ -545,7 +517,7 @@ int32_t rt_bvh_build_lbvh(rt_ctx* c, rt_scene* s, const rt_bvh_cfg* cfg, rt_stre
     if (min_leaf > 256) min_leaf = 256;
     s->depth = depth;
     s->min_leaf = min_leaf;
-    int32_t r = ensure_build(s, (depth + 7) / 8);
+    int32_t r = rt::scene_ensure_build(s);
     if (r) return r;
     cudaStream_t cs = st(c, stream);
     CU(cudaEventRecord(s->ev0, cs));

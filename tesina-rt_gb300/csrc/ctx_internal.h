@@ -7,6 +7,7 @@
 #include <map>
 
 #include "../../include/rt_cuda.h"
+#include "rt_internal.cuh"
 
 struct rt_ctx {
     int device = 0;
@@ -26,7 +27,46 @@ struct rt_ctx {
     std::map<uint64_t, rt_render_config> tuned;     // autotuner cache by workload class
 };
 
+// Scene state: geometry, the double-buffered triangle order and the build
+// products (see the design doc section 3 for the layout).
+struct rt_scene {
+    uint32_t V = 0, N = 0, M = 0;
+    uint32_t capV = 0, capN = 0, capM = 0;
+    float4* d_pos = nullptr;
+    float4* d_nrm = nullptr;
+    uint32_t* d_idx[2] = {nullptr, nullptr};
+    uint32_t* d_map[2] = {nullptr, nullptr};
+    uint32_t* d_orig[2] = {nullptr, nullptr};
+    int cur = 0;                     // which of the [2] buffers holds the current order
+    rt_material* d_mats = nullptr;
+    rt_lights lights;
+    // build products
+    uint32_t* d_keys_unsorted = nullptr;
+    uint32_t* d_vals0 = nullptr;
+    uint32_t* d_keys1 = nullptr;
+    uint32_t* d_vals1 = nullptr;
+    uint32_t* d_keys_sorted = nullptr;
+    uint32_t* d_vals_sorted = nullptr;
+    float4* d_tris = nullptr;
+    float4* d_leafbox = nullptr;
+    float4* d_nodes = nullptr;
+    uint32_t* d_flags = nullptr;
+    uint32_t* d_rangeL = nullptr;
+    uint32_t* d_rangeR = nullptr;
+    rt::BvhHeader* d_hdr = nullptr;
+    uint32_t* d_scratch = nullptr;
+    size_t scratch_bytes = 0;
+    uint32_t buildN = 0;             // capacity of the build buffers
+    bool built = false;
+    int depth = 30, min_leaf = 1;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
 namespace rt {
 // Records the message returned by rt_last_error() and returns code.
 int32_t set_error(int32_t code, const char* fmt, ...);
+// Allocates (or keeps) the build buffers for the scene's triangle count.
+int32_t scene_ensure_build(rt_scene* s);
+// Device view of the scene's current (sorted) order.
+SceneView scene_view(const rt_scene* s);
 }  // namespace rt

@@ -45,6 +45,11 @@ class RenderConfig(C.Structure):
             self.variant, self.blocks_per_sm, self.chunk)
 
 
+class BatchView(C.Structure):
+    _fields_ = [("scene", C.c_void_p), ("cam", Camera), ("width", C.c_int32),
+                ("height", C.c_int32), ("max_bounces", C.c_int32), ("rgba_offset", C.c_uint32)]
+
+
 class RenderStats(C.Structure):
     _fields_ = [("primary_rays", C.c_uint64), ("secondary_rays", C.c_uint64),
                 ("shadow_rays", C.c_uint64), ("hits", C.c_uint64)]

@@ -61,6 +61,14 @@ SIGNATURES = {
     "rt_set_render_config": (I32, [P, P]),
     "rt_get_render_config": (I32, [P, P]),
     "rt_autotune_render": (I32, [P, P, P, I32, I32, I32, I32, P, C.POINTER(F)]),
+    "rt_batch_create": (I32, [P, C.POINTER(P)]),
+    "rt_batch_destroy": (I32, [P, P]),
+    "rt_batch_set": (I32, [P, P, P, I32, P]),
+    "rt_batch_build": (I32, [P, P, P]),
+    "rt_batch_render": (I32, [P, P, P, P, P]),
+    "rt_batch_capture": (I32, [P, P, P, P]),
+    "rt_batch_replay": (I32, [P, P, P]),
+    "rt_batch_info": (I32, [P, P, C.POINTER(U32), C.POINTER(U32), C.POINTER(U32)]),
 }
 
 
@@ -333,6 +341,66 @@ class Scene:
     def close(self):
         if self.h:
             self.lib.rt_scene_destroy(self.ctx.h, self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            if self.ctx.h:
+                self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """An rt_batch: views of uploaded scenes, built and rendered together."""
+
+    def __init__(self, ctx):
+        self.ctx, self.lib = ctx, ctx.lib
+        h = P()
+        check(self.lib, self.lib.rt_batch_create(ctx.h, C.byref(h)))
+        self.h = h
+
+    def set(self, items, depth=30, min_leaf=1):
+        """items: list of (Scene, Camera, width, height, max_bounces)."""
+        n = len(items)
+        arr = (abi.BatchView * n)()
+        off = 0
+        self.offsets = []
+        for k, (sc, cam, w, h, b) in enumerate(items):
+            arr[k].scene = sc.h
+            arr[k].cam = cam
+            arr[k].width, arr[k].height, arr[k].max_bounces = w, h, b
+            arr[k].rgba_offset = off
+            self.offsets.append((off, w, h))
+            off += w * h
+        self.pixels = off
+        self._items = items
+        cfg = abi.BvhCfg(depth, min_leaf)
+        check(self.lib, self.lib.rt_batch_set(self.ctx.h, self.h, arr, n, C.byref(cfg)))
+
+    def build(self, stream=None):
+        check(self.lib, self.lib.rt_batch_build(self.ctx.h, self.h, stream))
+
+    def render(self, rgba_buf, stats_buf=None, stream=None):
+        check(self.lib, self.lib.rt_batch_render(self.ctx.h, self.h, rgba_buf.ptr,
+                                                 stats_buf.ptr if stats_buf else None, stream))
+
+    def capture(self, rgba_buf, stats_buf=None):
+        check(self.lib, self.lib.rt_batch_capture(self.ctx.h, self.h, rgba_buf.ptr,
+                                                  stats_buf.ptr if stats_buf else None))
+
+    def replay(self, stream=None):
+        check(self.lib, self.lib.rt_batch_replay(self.ctx.h, self.h, stream))
+
+    def info(self):
+        a, b, c = U32(0), U32(0), U32(0)
+        check(self.lib, self.lib.rt_batch_info(self.ctx.h, self.h, C.byref(a), C.byref(b),
+                                               C.byref(c)))
+        return a.value, b.value, c.value
+
+    def close(self):
+        if self.h:
+            self.lib.rt_batch_destroy(self.ctx.h, self.h)
             self.h = None
 
     def __del__(self):
