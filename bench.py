@@ -140,6 +140,76 @@ def cpu_baseline(wl, frame_pos, frame_nrm, sample_rays=65536):
             "lbvh_mtri_s": sc.n_tris / t_build / 1e6}
 
 
+def measure_batched(ctx, lib, torch, reps=5):
+    """Batched workload: 64 scenes built in one launch and rendered in one
+    launch (CUDA-graph replay) against the same 64 requests through the plain
+    per-request path (build + render per scene, one stream).  Pixels of both
+    are compared; throughput is Mrays/s (primary + secondary)."""
+    from rtgb import capi, scenes
+    wl = scenes.workload_batched()
+    items = wl["items"]
+    stream = torch.cuda.Stream()
+    sh = C.c_void_p(stream.cuda_stream)
+    gs = [capi.Scene(ctx, it["scene"]) for it in items]
+    px = sum(it["width"] * it["height"] for it in items)
+    tris = sum(it["scene"].n_tris for it in items)
+    # plain per-request path
+    rgba_plain = [ctx.alloc(4 * it["width"] * it["height"]) for it in items]
+    stats = ctx.alloc(32)
+
+    def plain_all():
+        for g, it, out in zip(gs, items, rgba_plain):
+            g.build(30, 1, stream=sh)
+            g.render(it["camera"], it["width"], it["height"], it["max_bounces"], out, None,
+                     stats, stream=sh)
+
+    for _ in range(2):
+        plain_all()
+    torch.cuda.synchronize()
+    stats.zero(sh)
+    t_plain = []
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        plain_all()
+        e1.record(stream)
+        stream.synchronize()
+        t_plain.append(e0.elapsed_time(e1))
+    rays = stats.read(np.uint64)
+    rays_plain = int(rays[0] + rays[1]) // reps
+    # batched: one build launch + one render launch, graph-replayed
+    batch = capi.Batch(ctx)
+    batch.set([(g, it["camera"], it["width"], it["height"], it["max_bounces"])
+               for g, it in zip(gs, items)])
+    rgba_b = ctx.alloc(4 * px)
+    bstats = ctx.alloc(32)
+    batch.capture(rgba_b, bstats)
+    for _ in range(2):
+        batch.replay(sh)
+    torch.cuda.synchronize()
+    t_b = []
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        batch.replay(sh)
+        e1.record(stream)
+        stream.synchronize()
+        t_b.append(e0.elapsed_time(e1))
+    st = bstats.read(np.uint64)
+    rays_b = int(st[0] + st[1])
+    out = rgba_b.read(np.uint8)
+    same = all(np.array_equal(out[4 * off:4 * (off + w * h)], rp.read(np.uint8))
+               for (off, w, h), rp in zip(batch.offsets, rgba_plain))
+    mp = rays_plain / (statistics.median(t_plain) * 1e-3) / 1e6
+    mb = rays_b / (statistics.median(t_b) * 1e-3) / 1e6
+    batch.close()
+    return {"workload": wl["name"], "scenes": len(items), "triangles": tris, "pixels": px,
+            "rays_per_batch": rays_b, "plain_ms": statistics.median(t_plain),
+            "batched_ms": statistics.median(t_b), "plain_mrays_s": mp, "batched_mrays_s": mb,
+            "speedup": mb / mp, "identical_pixels": bool(same and rays_b == rays_plain),
+            "launches_per_batch": 3, "launches_plain": 10 * len(items)}
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -325,6 +395,12 @@ def run_gpu(args):
                       "peak": peak, "unit": "GB/s", "frac": build_gbs / peak,
                       "bytes_per_tri": B_BUILD_PER_TRI, "peak_kind": peak_kind,
                       "ms": med_build, "lbvh_mtri_s": n_tris / (med_build * 1e-3) / 1e6}
+    batched = None
+    if world == 1 and not args.no_batched:
+        try:
+            batched = measure_batched(ctx, lib, torch)
+        except Exception as e:
+            batched = {"error": str(e)}
     cpu = None
     if world == 1 and not args.no_cpu_baseline:
         try:
@@ -345,6 +421,7 @@ def run_gpu(args):
            "rays_per_frame": rays_step, "shadow_rays_per_frame": shadow_step,
            "roofline": roofline, "build_roofline": build_roofline,
            "cpu_baseline": cpu,
+           "batched": batched,
            "e2e": {"value": e2e_value, "unit": UNIT,
                    "h2d_bytes_per_step": 2 * 16 * V,
                    "d2h_bytes_per_step": 4 * w * h + 32,
@@ -369,6 +446,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         log("warmup raised to 3")

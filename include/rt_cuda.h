@@ -367,6 +367,12 @@ RT_API int32_t rt_batch_capture(rt_ctx* ctx, rt_batch* batch, uint8_t* d_rgba,
 RT_API int32_t rt_batch_replay(rt_ctx* ctx, rt_batch* batch, rt_stream s);
 RT_API int32_t rt_batch_info(rt_ctx* ctx, rt_batch* batch, uint32_t* scenes,
                              uint32_t* triangles, uint32_t* pixels);
+/* Profiling of the batched build: when enabled, the build kernel records a
+ * device timestamp after each of its stages; rt_batch_stage_times returns the
+ * durations in ms of: init, scene bounds, Morton + histograms, radix passes,
+ * permutation, emit + refit (synchronous). */
+RT_API int32_t rt_batch_profile(rt_ctx* ctx, rt_batch* batch, int32_t enable);
+RT_API int32_t rt_batch_stage_times(rt_ctx* ctx, rt_batch* batch, float ms[6]);
 
 /* End-to-end convenience: host vertices in, host image out, synchronous:
  * optional vertex update -> LBVH build -> render -> RGBA8 to host. */

@@ -32,6 +32,21 @@ namespace cg = cooperative_groups;
 namespace rt {
 
 constexpr int kMaxBatchScenes = 1024;
+// Keys per thread of the batched radix tiles: 8 (2048-key tiles) keeps the
+// persistent kernel at <= 64 registers, i.e. 4 resident blocks per SM, which
+// doubles the threads available to the latency-bound emit stage.
+constexpr int kBatchItems = 8;
+
+__device__ __forceinline__ unsigned long long globaltimer() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Stage timestamps for profiling (block 0, thread 0, after each barrier).
+__device__ __forceinline__ void stamp(const BatchBuildArgs& A, int k) {
+    if (A.stage_ns && blockIdx.x == 0 && threadIdx.x == 0) A.stage_ns[k] = globaltimer();
+}
 
 // Scene index of global element g (offsets ascending, off[count] = total).
 __device__ __forceinline__ int find_segment(const uint32_t* off, int count, uint32_t g) {
@@ -46,9 +61,9 @@ __device__ __forceinline__ int find_segment(const uint32_t* off, int count, uint
     return lo;
 }
 
-__global__ void __launch_bounds__(SORT_THREADS) k_batch_build(BatchBuildArgs A) {
+__global__ void __launch_bounds__(SORT_THREADS, 4) k_batch_build(BatchBuildArgs A) {
     cg::grid_group grid = cg::this_grid();
-    __shared__ SortSmem S;
+    __shared__ SortSmemT<kBatchItems> S;
     __shared__ uint32_t s_toff[kMaxBatchScenes + 1];
     __shared__ uint32_t s_tileoff[kMaxBatchScenes + 1];
     __shared__ uint32_t s_hist[4][256];
@@ -64,6 +79,7 @@ __global__ void __launch_bounds__(SORT_THREADS) k_batch_build(BatchBuildArgs A) 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const uint32_t nblk = gridDim.x;
     const uint32_t gtid = blockIdx.x * blockDim.x + tid, gthreads = nblk * blockDim.x;
+    stamp(A, 0);
 
     // ---- stage 0: initialise bounds, histograms, look-back, arrival flags ---
     for (uint32_t i = gtid; i < (uint32_t)nsc * 8; i += gthreads)
@@ -78,6 +94,7 @@ __global__ void __launch_bounds__(SORT_THREADS) k_batch_build(BatchBuildArgs A) 
     }
     if (gtid < 4) A.tile_ctr[gtid] = 0;
     grid.sync();
+    stamp(A, 1);
 
     // ---- stage 1: scene AABBs (steps of 256 consecutive triangles) ----------
     for (uint32_t step = blockIdx.x; (size_t)step * SORT_THREADS < total; step += nblk) {
@@ -124,6 +141,7 @@ __global__ void __launch_bounds__(SORT_THREADS) k_batch_build(BatchBuildArgs A) 
         }
     }
     grid.sync();
+    stamp(A, 2);
 
     // ---- stage 2: Morton codes + per-scene digit histograms ------------------
     // Each block walks a contiguous range of steps, keeping the histogram of
@@ -184,6 +202,7 @@ __global__ void __launch_bounds__(SORT_THREADS) k_batch_build(BatchBuildArgs A) 
         }
     }
     grid.sync();
+    stamp(A, 3);
 
     // ---- stage 3: radix passes; tiles of all scenes share the grid ----------
     const uint32_t total_tiles = s_tileoff[nsc];
@@ -203,10 +222,11 @@ __global__ void __launch_bounds__(SORT_THREADS) k_batch_build(BatchBuildArgs A) 
             uint32_t* kout = dst ? B.keys_sorted : B.keys1;
             uint32_t* vout = dst ? B.vals_sorted : B.vals1;
             const uint32_t ntiles_s = s_tileoff[s + 1] - s_tileoff[s];
-            onesweep_tile(S, lt, kin, vin, kout, vout, B.n, 8 * p, B.hist + 256 * p,
+            onesweep_tile<kBatchItems>(S, lt, kin, vin, kout, vout, B.n, 8 * p, B.hist + 256 * p,
                           B.lookback + (size_t)p * ntiles_s * 256, A.status);
         }
         grid.sync();
+        if (p == A.passes - 1) stamp(A, 4);
     }
 
     // ---- stage 4: permutation into sorted order ------------------------------
@@ -217,13 +237,33 @@ __global__ void __launch_bounds__(SORT_THREADS) k_batch_build(BatchBuildArgs A) 
                     B.map_out, B.orig_out, B.tris, B.leafbox);
     }
     grid.sync();
-
+    stamp(A, 5);
     // ---- stage 5: bottom-up emit + refit -----------------------------------
-    for (uint32_t g = blockIdx.x * blockDim.x + tid; g < total; g += nblk * blockDim.x) {
-        const int s = find_segment(s_toff, nsc, g);
-        const BatchScene& B = A.scenes[s];
-        emit_climb(g - s_toff[s], B.n, B.keys_sorted, B.leafbox, B.nodes, B.flags, B.rangeL,
-                   B.rangeR, B.min_leaf, B.hdr);
+    // groups of 4 consecutive triangles of one scene per thread, climbed in
+    // lockstep (emit_climb_multi); groups never straddle scenes
+    constexpr int KC = 4;
+    {
+        // group g covers scene s's triangles [4j, 4j+4): enumerate groups of
+        // every scene in order
+        uint32_t ngroups = 0;
+        for (int sc = 0; sc < nsc; ++sc) ngroups += (s_toff[sc + 1] - s_toff[sc] + KC - 1) / KC;
+        for (uint32_t g = gtid; g < ngroups; g += gthreads) {
+            // find the scene of group g (linear scan over the per-scene group counts)
+            uint32_t acc = 0;
+            int s = 0;
+            for (; s < nsc; ++s) {
+                const uint32_t gs = (s_toff[s + 1] - s_toff[s] + KC - 1) / KC;
+                if (g < acc + gs) break;
+                acc += gs;
+            }
+            const BatchScene& B = A.scenes[s];
+            emit_climb_multi<KC>((g - acc) * KC, B.n, B.keys_sorted, B.leafbox, B.nodes, B.flags,
+                                 B.rangeL, B.rangeR, B.min_leaf, B.hdr);
+        }
+    }
+    if (A.stage_ns) {
+        grid.sync();
+        stamp(A, 6);
     }
 }
 
@@ -245,8 +285,11 @@ __global__ void __launch_bounds__(THREADS, MINB) k_render_batch(BatchRenderArgs 
         if (base0 >= total) break;
         for (uint32_t base = base0; base < base0 + A.chunk && base < total; base += 32) {
             const uint32_t g = base + lane;
+            // the view of the warp's first pixel; lanes past its end look their own up
+            const int v0 = find_segment(s_poff, A.count, base);
+            const bool same = g < s_poff[v0 + 1];
             if (g < total) {
-                const int v = find_segment(s_poff, A.count, g);
+                const int v = same ? v0 : find_segment(s_poff, A.count, g);
                 const BatchView& V = A.views[v];
                 const int local = (int)(g - s_poff[v]);
                 int x, y;
@@ -308,7 +351,7 @@ cudaError_t launch_batch_render(const BatchRenderArgs& a, int variant, int grid,
 const void* batch_build_kernel() { return (const void*)k_batch_build; }
 int batch_build_threads() { return SORT_THREADS; }
 int batch_max_scenes() { return kMaxBatchScenes; }
-int sort_tile_size() { return SORT_TILE; }
+int sort_tile_size() { return SORT_THREADS * kBatchItems; }
 
 cudaError_t launch_batch_build(const BatchBuildArgs& a, int grid, cudaStream_t s) {
     cudaLaunchConfig_t cfg = {};

@@ -47,6 +47,7 @@ struct BatchBuildArgs {
     const uint32_t* tile_off;   // count + 1 prefix offsets of sort tiles
     uint32_t* tile_ctr;         // one counter per pass
     uint32_t* status;
+    unsigned long long* stage_ns;   // optional: globaltimer after each stage (8 entries)
 };
 
 struct BatchView {

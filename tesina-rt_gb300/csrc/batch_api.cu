@@ -44,6 +44,8 @@ struct rt_batch {
     int render_variant = 0, render_grid = 0, render_chunk = 32;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
+    unsigned long long* d_stage = nullptr;  // stage timestamps when profiling is on
+    bool profile = false;
 };
 
 namespace {
@@ -63,6 +65,7 @@ void free_tables(rt_batch* b) {
     dfree(b->d_views);
     dfree(b->d_pix_off);
     dfree(b->d_lights);
+    dfree(b->d_stage);
     if (b->exec) cudaGraphExecDestroy(b->exec);
     if (b->graph) cudaGraphDestroy(b->graph);
     b->exec = nullptr;
@@ -147,6 +150,7 @@ rt::BatchBuildArgs build_args(rt_ctx* c, rt_batch* b) {
     a.tile_off = b->d_tile_off;
     a.tile_ctr = b->d_ctr;
     a.status = c->d_status;
+    a.stage_ns = b->profile ? b->d_stage : nullptr;
     return a;
 }
 
@@ -254,7 +258,8 @@ int32_t rt_batch_set(rt_ctx* c, rt_batch* b, const rt_batch_view* views, int32_t
         cudaMalloc(&b->d_ctr, 4 * 8) || cudaMalloc(&b->d_scratch, 4 * words) ||
         cudaMalloc(&b->d_views, sizeof(rt::BatchView) * count) ||
         cudaMalloc(&b->d_pix_off, 4 * (count + 1)) ||
-        cudaMalloc(&b->d_lights, sizeof(rt_lights) * ns)) {
+        cudaMalloc(&b->d_lights, sizeof(rt_lights) * ns) ||
+        cudaMalloc(&b->d_stage, sizeof(unsigned long long) * 8)) {
         cudaGetLastError();
         free_tables(b);
         return fail(RT_ERR_OOM, "rt_batch_set: device allocation failed");
@@ -358,6 +363,22 @@ int32_t rt_batch_capture(rt_ctx* c, rt_batch* b, uint8_t* d_rgba, rt_render_stat
 int32_t rt_batch_replay(rt_ctx* c, rt_batch* b, rt_stream stream) {
     if (!c || !b || !b->exec) return fail(RT_ERR_INVALID, "rt_batch_replay: nothing captured");
     CU(cudaGraphLaunch(b->exec, stream ? (cudaStream_t)stream : c->stream));
+    return RT_OK;
+}
+
+int32_t rt_batch_profile(rt_ctx* c, rt_batch* b, int32_t enable) {
+    if (!c || !b) return fail(RT_ERR_INVALID, "rt_batch_profile: null argument");
+    b->profile = enable != 0;
+    return RT_OK;
+}
+
+int32_t rt_batch_stage_times(rt_ctx* c, rt_batch* b, float* ms) {
+    if (!c || !b || !ms || !b->d_stage)
+        return fail(RT_ERR_INVALID, "rt_batch_stage_times: null argument or batch not set");
+    unsigned long long t[8];
+    CU(cudaStreamSynchronize(c->stream));
+    CU(cudaMemcpy(t, b->d_stage, sizeof(t), cudaMemcpyDeviceToHost));
+    for (int k = 0; k < 6; ++k) ms[k] = (float)((double)(t[k + 1] - t[k]) * 1e-6);
     return RT_OK;
 }
 

@@ -136,21 +136,25 @@ __device__ __forceinline__ uint32_t block_excl_scan_256(uint32_t v, uint32_t* s_
     return warp_base + x - v;
 }
 
-struct SortSmem {
-    uint32_t keys[SORT_TILE];
-    uint32_t vals[SORT_TILE];
+template <int ITEMS>
+struct SortSmemT {
+    uint32_t keys[SORT_THREADS * ITEMS];
+    uint32_t vals[SORT_THREADS * ITEMS];
     uint32_t whist[SORT_WARPS][256];
     uint32_t goff[256];
     uint32_t lstart[256];
     uint32_t scan[SORT_WARPS];
     uint32_t tile;
 };
+using SortSmem = SortSmemT<SORT_ITEMS>;
 
 // One tile of a stable LSD radix pass (8-bit digit at `shift`): warp-striped
 // loads, __match_any_sync ranking in index order, decoupled look-back over
 // the earlier tiles of the same sequence, shared-memory staging and a
-// coalesced scatter.  Must be called by all SORT_THREADS threads of a block.
-__device__ __forceinline__ void onesweep_tile(SortSmem& S, uint32_t tile,
+// coalesced scatter.  Must be called by all SORT_THREADS threads of a block;
+// a tile holds SORT_THREADS * ITEMS keys.
+template <int ITEMS = SORT_ITEMS>
+__device__ __forceinline__ void onesweep_tile(SortSmemT<ITEMS>& S, uint32_t tile,
                                               const uint32_t* __restrict__ kin,
                                               const uint32_t* __restrict__ vin,
                                               uint32_t* __restrict__ kout,
@@ -161,20 +165,20 @@ __device__ __forceinline__ void onesweep_tile(SortSmem& S, uint32_t tile,
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     for (int i = tid; i < SORT_WARPS * 256; i += SORT_THREADS) (&S.whist[0][0])[i] = 0;
     __syncthreads();
-    const size_t base = (size_t)tile * SORT_TILE;
+    const size_t base = (size_t)tile * (SORT_THREADS * ITEMS);
     const uint32_t lanemask_lt = (1u << lane) - 1u;
 
-    uint32_t k[SORT_ITEMS], v[SORT_ITEMS], rank[SORT_ITEMS];
+    uint32_t k[ITEMS], v[ITEMS], rank[ITEMS];
 #pragma unroll
-    for (int j = 0; j < SORT_ITEMS; ++j) {
-        const size_t g = base + (size_t)warp * (SORT_ITEMS * 32) + j * 32 + lane;
+    for (int j = 0; j < ITEMS; ++j) {
+        const size_t g = base + (size_t)warp * (ITEMS * 32) + j * 32 + lane;
         const bool ok = g < n;
         k[j] = ok ? __ldcs(&kin[g]) : 0xffffffffu;
         v[j] = ok ? __ldcs(&vin[g]) : 0u;
     }
 #pragma unroll
-    for (int j = 0; j < SORT_ITEMS; ++j) {
-        const size_t g = base + (size_t)warp * (SORT_ITEMS * 32) + j * 32 + lane;
+    for (int j = 0; j < ITEMS; ++j) {
+        const size_t g = base + (size_t)warp * (ITEMS * 32) + j * 32 + lane;
         const bool ok = g < n;
         const uint32_t d = (k[j] >> shift) & 255u;
         const uint32_t valid = __ballot_sync(0xffffffffu, ok);
@@ -231,8 +235,8 @@ __device__ __forceinline__ void onesweep_tile(SortSmem& S, uint32_t tile,
     S.lstart[dgt] = lstart;
     __syncthreads();
 #pragma unroll
-    for (int j = 0; j < SORT_ITEMS; ++j) {
-        const size_t g = base + (size_t)warp * (SORT_ITEMS * 32) + j * 32 + lane;
+    for (int j = 0; j < ITEMS; ++j) {
+        const size_t g = base + (size_t)warp * (ITEMS * 32) + j * 32 + lane;
         if (g < n) {
             const uint32_t d = (k[j] >> shift) & 255u;
             const uint32_t p = S.lstart[d] + S.whist[warp][d] + rank[j];
@@ -241,7 +245,7 @@ __device__ __forceinline__ void onesweep_tile(SortSmem& S, uint32_t tile,
         }
     }
     __syncthreads();
-    const uint32_t valid_n = (uint32_t)min((size_t)SORT_TILE, (size_t)n - base);
+    const uint32_t valid_n = (uint32_t)min((size_t)(SORT_THREADS * ITEMS), (size_t)n - base);
     for (uint32_t i = tid; i < valid_n; i += SORT_THREADS) {
         const uint32_t key = S.keys[i];
         const uint32_t d = (key >> shift) & 255u;
@@ -374,6 +378,106 @@ __device__ __forceinline__ void emit_climb(uint32_t i, uint32_t n,
             hdr->root_lo = lo;
             hdr->root_hi = hi;
             return;
+        }
+    }
+}
+
+// K climbs of emit_climb advanced in lockstep by one thread: one release
+// fence before the K arrival counters are bumped and one acquire fence before
+// the winners read their siblings, instead of one ordering point per climber
+// and level.  Used where few threads must cover many triangles (the
+// persistent many-scene build).  Climbers are the triangles first..first+K-1
+// of one scene (those >= n are idle).
+template <int K>
+__device__ __forceinline__ void emit_climb_multi(uint32_t first, uint32_t n,
+                                                 const uint32_t* __restrict__ skeys,
+                                                 const float4* __restrict__ leafbox,
+                                                 float4* __restrict__ nodes,
+                                                 uint32_t* __restrict__ flags,
+                                                 uint32_t* __restrict__ rangeL,
+                                                 uint32_t* __restrict__ rangeR, int min_leaf,
+                                                 BvhHeader* __restrict__ hdr) {
+    if (n == 1) {
+        if (first == 0) emit_climb(0, 1, skeys, leafbox, nodes, flags, rangeL, rangeR, min_leaf, hdr);
+        return;
+    }
+    uint32_t l[K], r[K], p[K];
+    int32_t ref[K], cnt[K];
+    float4 lo[K], hi[K];
+    bool alive[K], left[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        const uint32_t i = first + k;
+        alive[k] = i < n;
+        l[k] = r[k] = i;
+        ref[k] = (int32_t)i;
+        cnt[k] = 1;
+        if (alive[k]) {
+            lo[k] = leafbox[2 * (size_t)i];
+            hi[k] = leafbox[2 * (size_t)i + 1];
+        }
+    }
+    for (;;) {
+        bool any = false;
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            if (!alive[k]) continue;
+            any = true;
+            if (l[k] == 0 || (r[k] != n - 1 && delta(skeys, r[k]) < delta(skeys, l[k] - 1))) {
+                p[k] = r[k];
+                left[k] = true;
+            } else {
+                p[k] = l[k] - 1;
+                left[k] = false;
+            }
+            float* rec = reinterpret_cast<float*>(nodes + 4 * (size_t)p[k]);
+            int* rec_i = reinterpret_cast<int*>(nodes + 4 * (size_t)p[k] + 3);
+            if (left[k]) {
+                nodes[4 * (size_t)p[k]] = make_float4(lo[k].x, lo[k].y, lo[k].z, hi[k].x);
+                *reinterpret_cast<float2*>(rec + 4) = make_float2(hi[k].y, hi[k].z);
+                rec_i[0] = ref[k];
+                rec_i[2] = cnt[k];
+                rangeL[p[k]] = l[k];
+            } else {
+                *reinterpret_cast<float2*>(rec + 6) = make_float2(lo[k].x, lo[k].y);
+                nodes[4 * (size_t)p[k] + 2] = make_float4(lo[k].z, hi[k].x, hi[k].y, hi[k].z);
+                rec_i[1] = ref[k];
+                rec_i[3] = cnt[k];
+                rangeR[p[k]] = r[k];
+            }
+        }
+        if (!any) return;
+        __threadfence();   // release every record written above
+#pragma unroll
+        for (int k = 0; k < K; ++k)
+            if (alive[k] && atomicAdd(&flags[p[k]], 1u) == 0) alive[k] = false;
+        __threadfence();   // acquire the siblings' records
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            if (!alive[k]) continue;
+            const size_t q = p[k];
+            const float4 n0 = __ldcg(&nodes[4 * q]);
+            const float4 n1 = __ldcg(&nodes[4 * q + 1]);
+            const float4 n2 = __ldcg(&nodes[4 * q + 2]);
+            const uint32_t L = left[k] ? l[k] : __ldcg(&rangeL[q]);
+            const uint32_t R = left[k] ? __ldcg(&rangeR[q]) : r[k];
+            lo[k] = make_float4(fminf(n0.x, n1.z), fminf(n0.y, n1.w), fminf(n0.z, n2.x), 0.f);
+            hi[k] = make_float4(fmaxf(n0.w, n2.y), fmaxf(n1.x, n2.z), fmaxf(n1.y, n2.w), 0.f);
+            const uint32_t count = R - L + 1;
+            const bool interior =
+                count >= (uint32_t)min_leaf + 3u && __ldg(&skeys[L]) != __ldg(&skeys[R]);
+            ref[k] = interior ? (int32_t)q : (int32_t)L;
+            cnt[k] = interior ? 0 : (int32_t)count;
+            l[k] = L;
+            r[k] = R;
+            if (L == 0 && R == n - 1) {
+                hdr->root_ref = ref[k];
+                hdr->root_cnt = cnt[k];
+                hdr->n_tris = n;
+                hdr->root_lo = lo[k];
+                hdr->root_hi = hi[k];
+                alive[k] = false;
+            }
         }
     }
 }

@@ -69,6 +69,8 @@ SIGNATURES = {
     "rt_batch_capture": (I32, [P, P, P, P]),
     "rt_batch_replay": (I32, [P, P, P]),
     "rt_batch_info": (I32, [P, P, C.POINTER(U32), C.POINTER(U32), C.POINTER(U32)]),
+    "rt_batch_profile": (I32, [P, P, I32]),
+    "rt_batch_stage_times": (I32, [P, P, P]),
 }
 
 
@@ -391,6 +393,14 @@ class Batch:
 
     def replay(self, stream=None):
         check(self.lib, self.lib.rt_batch_replay(self.ctx.h, self.h, stream))
+
+    def profile(self, enable=True):
+        check(self.lib, self.lib.rt_batch_profile(self.ctx.h, self.h, int(enable)))
+
+    def stage_times(self):
+        ms = (F * 6)()
+        check(self.lib, self.lib.rt_batch_stage_times(self.ctx.h, self.h, ms))
+        return dict(zip(["init", "bounds", "morton", "sort", "permute", "emit"], list(ms)))
 
     def info(self):
         a, b, c = U32(0), U32(0), U32(0)

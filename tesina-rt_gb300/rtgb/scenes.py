@@ -302,3 +302,20 @@ def workload_stress(seed=2):
         poses.append(camera(tuple(v), (0.0, 0.0, 0.0), fov_deg=60.0, aspect=3840 / 2160))
     return dict(name="terrain17M_3840x2160_d6", terrain=ter, cameras=poses, width=3840,
                 height=2160, max_bounces=6, depth=30, min_leaf=1)
+
+
+def workload_batched(seed=3, count=64):
+    """Batched: 64 triangle soups (as the small workload) with triangle counts
+    log-uniform in [1k, 500k], resolutions from {256x256, 512x512, 1024x768},
+    reflection depth uniform in 1..4."""
+    rng = np.random.default_rng(seed)
+    items = []
+    res = [(256, 256), (512, 512), (1024, 768)]
+    for k in range(count):
+        n = int(round(math.exp(rng.uniform(math.log(1000), math.log(500000)))))
+        w, h = res[int(rng.integers(0, 3))]
+        depth = int(rng.integers(1, 5))
+        sc = soup(n, seed=seed * 1000 + k)
+        cam = camera((0.0, 0.0, -4.0), (0.0, 0.0, 0.0), fov_deg=60.0, aspect=w / h)
+        items.append(dict(scene=sc, camera=cam, width=w, height=h, max_bounces=depth))
+    return dict(name="soups64_1k-500k_mixed-res", items=items)
