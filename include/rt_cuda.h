@@ -374,6 +374,60 @@ RT_API int32_t rt_batch_info(rt_ctx* ctx, rt_batch* batch, uint32_t* scenes,
 RT_API int32_t rt_batch_profile(rt_ctx* ctx, rt_batch* batch, int32_t enable);
 RT_API int32_t rt_batch_stage_times(rt_ctx* ctx, rt_batch* batch, float ms[6]);
 
+/* ------------------------------------------------------------------------ */
+/* Served form: resident scenes, admission, continuous batching             */
+/* ------------------------------------------------------------------------ */
+typedef struct rt_server rt_server;
+
+enum { RT_REQ_RENDER = 0, RT_REQ_UPLOAD = 1 };
+
+typedef struct rt_server_cfg {
+    uint64_t hbm_budget_bytes;   /* resident scenes + framebuffer arena            */
+    uint64_t fb_arena_bytes;     /* device framebuffers of admitted requests        */
+    int32_t  max_batch_views;    /* requests per render launch; 1 = plain path     */
+    int32_t  max_inflight;       /* render launches on the GPU at once (streams)   */
+} rt_server_cfg;
+
+typedef struct rt_request {
+    int32_t  type;               /* RT_REQ_RENDER / RT_REQ_UPLOAD                   */
+    int32_t  max_bounces;
+    int32_t  width, height;
+    uint64_t scene_id;           /* render: target scene                           */
+    rt_camera cam;
+    const rt_scene_desc* upload; /* upload: caller-owned until the request is done */
+} rt_request;
+
+typedef struct rt_request_info {
+    int32_t  status;             /* RT_OK or the failure (RT_ERR_REJECTED, ...)     */
+    int32_t  batch_views;        /* requests in the launch that served this one     */
+    uint64_t scene_id;           /* upload: id of the new scene                     */
+    double   submit_ms, start_ms, done_ms;   /* server clock                        */
+    uint64_t rays;               /* primary + secondary rays traced                 */
+} rt_request_info;
+
+typedef struct rt_server_stats {
+    uint64_t completed, rejected, evicted, batches, rays, resident_scenes;
+    uint64_t resident_bytes;
+    double   p50_ms, p99_ms, mean_batch_views, first_submit_ms, last_done_ms;
+} rt_server_stats;
+
+RT_API int32_t rt_server_create(rt_ctx* ctx, const rt_server_cfg* cfg, rt_server** server);
+RT_API int32_t rt_server_destroy(rt_server* server);
+/* Synchronous upload + LBVH build of a resident scene (counted in the budget). */
+RT_API int32_t rt_server_add_scene(rt_server* server, const rt_scene_desc* desc,
+                                   uint64_t* scene_id);
+/* Thread-safe, non-blocking.  Renders and uploads are admitted in arrival
+ * order as framebuffer space and memory allow; uploads that do not fit even
+ * after evicting least-recently-used idle scenes are rejected. */
+RT_API int32_t rt_server_submit(rt_server* server, const rt_request* req, uint64_t* ticket);
+/* Blocks until the request is done; copies a render's RGBA8 image to h_rgba
+ * (may be NULL) and releases it. */
+RT_API int32_t rt_server_result(rt_server* server, uint64_t ticket, uint8_t* h_rgba,
+                                rt_request_info* info);
+/* Latency percentiles over requests completed since the last reset. */
+RT_API int32_t rt_server_get_stats(rt_server* server, rt_server_stats* stats);
+RT_API int32_t rt_server_reset_stats(rt_server* server);
+
 /* End-to-end convenience: host vertices in, host image out, synchronous:
  * optional vertex update -> LBVH build -> render -> RGBA8 to host. */
 RT_API int32_t rt_render_host(rt_ctx* ctx, rt_scene* scene, const float* h_pos4, const float* h_nrm4,

@@ -50,6 +50,34 @@ class BatchView(C.Structure):
                 ("height", C.c_int32), ("max_bounces", C.c_int32), ("rgba_offset", C.c_uint32)]
 
 
+RT_REQ_RENDER, RT_REQ_UPLOAD = 0, 1
+
+
+class ServerCfg(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_uint64), ("fb_arena_bytes", C.c_uint64),
+                ("max_batch_views", C.c_int32), ("max_inflight", C.c_int32)]
+
+
+class Request(C.Structure):
+    _fields_ = [("type", C.c_int32), ("max_bounces", C.c_int32), ("width", C.c_int32),
+                ("height", C.c_int32), ("scene_id", C.c_uint64), ("cam", Camera),
+                ("upload", C.c_void_p)]
+
+
+class RequestInfo(C.Structure):
+    _fields_ = [("status", C.c_int32), ("batch_views", C.c_int32), ("scene_id", C.c_uint64),
+                ("submit_ms", C.c_double), ("start_ms", C.c_double), ("done_ms", C.c_double),
+                ("rays", C.c_uint64)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("completed", C.c_uint64), ("rejected", C.c_uint64), ("evicted", C.c_uint64),
+                ("batches", C.c_uint64), ("rays", C.c_uint64), ("resident_scenes", C.c_uint64),
+                ("resident_bytes", C.c_uint64), ("p50_ms", C.c_double), ("p99_ms", C.c_double),
+                ("mean_batch_views", C.c_double), ("first_submit_ms", C.c_double),
+                ("last_done_ms", C.c_double)]
+
+
 class RenderStats(C.Structure):
     _fields_ = [("primary_rays", C.c_uint64), ("secondary_rays", C.c_uint64),
                 ("shadow_rays", C.c_uint64), ("hits", C.c_uint64)]

@@ -71,6 +71,13 @@ SIGNATURES = {
     "rt_batch_info": (I32, [P, P, C.POINTER(U32), C.POINTER(U32), C.POINTER(U32)]),
     "rt_batch_profile": (I32, [P, P, I32]),
     "rt_batch_stage_times": (I32, [P, P, P]),
+    "rt_server_create": (I32, [P, P, C.POINTER(P)]),
+    "rt_server_destroy": (I32, [P]),
+    "rt_server_add_scene": (I32, [P, P, C.POINTER(C.c_uint64)]),
+    "rt_server_submit": (I32, [P, P, C.POINTER(C.c_uint64)]),
+    "rt_server_result": (I32, [P, C.c_uint64, P, P]),
+    "rt_server_get_stats": (I32, [P, P]),
+    "rt_server_reset_stats": (I32, [P]),
 }
 
 
@@ -417,5 +424,65 @@ class Batch:
         try:
             if self.ctx.h:
                 self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """An rt_server: resident scenes, admission, continuous batching."""
+
+    def __init__(self, ctx, budget=120 << 30, arena=2 << 30, max_views=256, max_inflight=2):
+        self.ctx, self.lib = ctx, ctx.lib
+        cfg = abi.ServerCfg(budget, arena, max_views, max_inflight)
+        h = P()
+        check(self.lib, self.lib.rt_server_create(ctx.h, C.byref(cfg), C.byref(h)))
+        self.h = h
+        self._uploads = {}
+
+    def add_scene(self, sc):
+        d = scene_desc(sc)
+        sid = C.c_uint64(0)
+        check(self.lib, self.lib.rt_server_add_scene(self.h, C.byref(d), C.byref(sid)))
+        return sid.value
+
+    def submit_render(self, scene_id, cam, w, h, bounces):
+        r = abi.Request(abi.RT_REQ_RENDER, bounces, w, h, scene_id, cam, None)
+        t = C.c_uint64(0)
+        check(self.lib, self.lib.rt_server_submit(self.h, C.byref(r), C.byref(t)))
+        return t.value
+
+    def submit_upload(self, sc):
+        d = scene_desc(sc)
+        r = abi.Request(abi.RT_REQ_UPLOAD, 0, 0, 0, 0, abi.Camera(), C.addressof(d))
+        t = C.c_uint64(0)
+        check(self.lib, self.lib.rt_server_submit(self.h, C.byref(r), C.byref(t)))
+        self._uploads[t.value] = (d, sc)        # host data stays alive until done
+        return t.value
+
+    def result(self, ticket, w=0, h=0, raise_on_error=True):
+        rgba = np.zeros((h * w, 4), np.uint8) if w * h else None
+        info = abi.RequestInfo()
+        r = self.lib.rt_server_result(self.h, ticket, _p(rgba), C.byref(info))
+        self._uploads.pop(ticket, None)
+        if r and raise_on_error:
+            raise RtError(r, self.lib.rt_last_error().decode(errors="replace"))
+        return rgba, info
+
+    def stats(self):
+        st = abi.ServerStats()
+        check(self.lib, self.lib.rt_server_get_stats(self.h, C.byref(st)))
+        return st
+
+    def reset_stats(self):
+        check(self.lib, self.lib.rt_server_reset_stats(self.h))
+
+    def close(self):
+        if self.h:
+            self.lib.rt_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
         except Exception:
             pass

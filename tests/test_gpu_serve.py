@@ -1,0 +1,111 @@
+"""Served form: resident scenes, admission against a memory budget, LRU
+eviction, continuous batching.  A request's image is the same alone, in a
+mixed burst with uploads, and through the plain rt_render path."""
+import numpy as np
+import pytest
+
+from helpers import tiny_terrain
+from rtgb import capi, scenes
+
+pytestmark = pytest.mark.gpu
+
+
+def _plain(ctx, sc, cam, w, h, b):
+    g = capi.Scene(ctx, sc)
+    g.build(30, 1)
+    rgba = ctx.alloc(4 * w * h)
+    g.render(cam, w, h, b, rgba)
+    ctx.sync()
+    return rgba.read(np.uint8).reshape(-1, 4)
+
+
+def _pool():
+    return [scenes.soup(5000, seed=31), scenes.soup(40000, seed=32),
+            tiny_terrain(64, 32, 6).scene(1)]
+
+
+def test_result_alone_equals_mix_and_plain(ctx):
+    pool = _pool()
+    srv = capi.Server(ctx, budget=4 << 30, arena=256 << 20, max_views=64, max_inflight=2)
+    ids = [srv.add_scene(sc) for sc in pool]
+    cam = scenes.camera((0.5, 0.5, -4.0), (0, 0, 0), aspect=160 / 120)
+    probe = (ids[1], cam, 160, 120, 3)
+    alone, info = srv.result(srv.submit_render(*probe), 160, 120)
+    assert info.status == 0 and info.batch_views == 1
+    assert np.array_equal(alone, _plain(ctx, pool[1], cam, 160, 120, 3))
+    # a mixed burst: renders of every scene and size, two uploads, the probe
+    rng = np.random.default_rng(3)
+    extra = [scenes.soup(20000, seed=40), tiny_terrain(32, 16, 2).scene(0)]
+    tickets = []
+    for k in range(40):
+        if k in (7, 23):
+            tickets.append(("up", srv.submit_upload(extra[k == 23]), None))
+            continue
+        if k == 20:
+            tickets.append(("probe", srv.submit_render(*probe), (160, 120)))
+            continue
+        w, h = int(rng.integers(16, 200)), int(rng.integers(16, 200))
+        sid = ids[int(rng.integers(0, 3))]
+        c = scenes.camera(tuple(rng.normal(size=3) * 2 + [0, 0, -4]), (0, 0, 0), aspect=w / h)
+        tickets.append(("r", srv.submit_render(sid, c, w, h, int(rng.integers(0, 5))), (w, h)))
+    new_ids = []
+    views = []
+    for kind, t, wh in tickets:
+        if kind == "up":
+            _, inf = srv.result(t)
+            assert inf.status == 0 and inf.scene_id > 0
+            new_ids.append(inf.scene_id)
+        else:
+            img, inf = srv.result(t, *wh)
+            assert inf.status == 0
+            views.append(inf.batch_views)
+            if kind == "probe":
+                assert np.array_equal(img, alone)
+    assert max(views) > 1                       # requests shared launches
+    # the uploaded scenes render like the plain path
+    for sid, sc in zip(new_ids, extra):
+        img, _ = srv.result(srv.submit_render(sid, cam, 160, 120, 2), 160, 120)
+        assert np.array_equal(img, _plain(ctx, sc, cam, 160, 120, 2))
+    st = srv.stats()
+    assert st.completed == 43 and st.rejected == 0   # probe alone + 40 in the burst + 2
+    srv.close()
+
+
+def test_admission_and_lru_eviction(ctx):
+    small = [scenes.soup(20000, seed=50 + k) for k in range(3)]
+    one = 20000 * 300                           # ~ bytes of one such scene
+    srv = capi.Server(ctx, budget=(64 << 20) + int(2.5 * one), arena=64 << 20, max_views=16,
+                      max_inflight=1)
+    a = srv.add_scene(small[0])
+    b = srv.add_scene(small[1])
+    cam = scenes.camera((0, 0, -4), (0, 0, 0))
+    srv.result(srv.submit_render(b, cam, 32, 32, 1), 32, 32)      # b used last -> a is LRU
+    _, inf = srv.result(srv.submit_upload(small[2]))
+    assert inf.status == 0
+    st = srv.stats()
+    assert st.evicted == 1 and st.resident_scenes == 2
+    _, inf = srv.result(srv.submit_render(a, cam, 32, 32, 1), 32, 32, raise_on_error=False)
+    assert inf.status == -2                     # evicted scene
+    huge = scenes.soup(400000, seed=60)
+    _, inf = srv.result(srv.submit_upload(huge), raise_on_error=False)
+    assert inf.status == -8                     # does not fit even after eviction
+    img, inf = srv.result(srv.submit_render(b, cam, 32, 32, 1), 32, 32)
+    assert inf.status == 0
+    srv.close()
+
+
+def test_plain_mode_and_oversized_frame(ctx):
+    pool = _pool()
+    srv = capi.Server(ctx, budget=2 << 30, arena=1 << 20, max_views=1, max_inflight=4)
+    ids = [srv.add_scene(sc) for sc in pool]
+    cam = scenes.camera((0, 0, -4), (0, 0, 0))
+    ts = [srv.submit_render(ids[k % 3], cam, 64, 64, 2) for k in range(9)]
+    for k, t in enumerate(ts):
+        img, inf = srv.result(t, 64, 64)
+        assert inf.batch_views == 1
+        assert np.array_equal(img, _plain(ctx, pool[k % 3], cam, 64, 64, 2))
+    # a frame larger than the whole framebuffer arena is rejected, not queued
+    _, inf = srv.result(srv.submit_render(ids[0], cam, 1024, 1024, 1), 1024, 1024,
+                        raise_on_error=False)
+    assert inf.status == -8
+    srv.close()
