@@ -386,6 +386,9 @@ typedef struct rt_server_cfg {
     uint64_t fb_arena_bytes;     /* device framebuffers of admitted requests        */
     int32_t  max_batch_views;    /* requests per render launch; 1 = plain path     */
     int32_t  max_inflight;       /* render launches on the GPU at once (streams)   */
+    int32_t  max_scenes;         /* resident-scene cap, 0 = none: an upload beyond
+                                    it evicts the least recently used scene        */
+    int32_t  reserved;           /* 0                                              */
 } rt_server_cfg;
 
 typedef struct rt_request {
@@ -418,13 +421,17 @@ RT_API int32_t rt_server_add_scene(rt_server* server, const rt_scene_desc* desc,
                                    uint64_t* scene_id);
 /* Thread-safe, non-blocking.  Renders and uploads are admitted in arrival
  * order as framebuffer space and memory allow; uploads that do not fit even
- * after evicting least-recently-used idle scenes are rejected. */
+ * after evicting least-recently-used idle scenes are rejected.  Recency is
+ * the order of submission (add_scene, upload and render submits).  With
+ * max_scenes set, an upload that would exceed it marks the least recently
+ * used scene evicted at submit: renders already submitted for it are still
+ * served, later ones fail with RT_ERR_INVALID. */
 RT_API int32_t rt_server_submit(rt_server* server, const rt_request* req, uint64_t* ticket);
 /* Blocks until the request is done; copies a render's RGBA8 image to h_rgba
  * (may be NULL) and releases it. */
 RT_API int32_t rt_server_result(rt_server* server, uint64_t ticket, uint8_t* h_rgba,
                                 rt_request_info* info);
-/* Latency percentiles over requests completed since the last reset. */
+/* Latency percentiles over render requests completed since the last reset. */
 RT_API int32_t rt_server_get_stats(rt_server* server, rt_server_stats* stats);
 RT_API int32_t rt_server_reset_stats(rt_server* server);
 

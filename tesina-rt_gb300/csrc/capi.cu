@@ -148,6 +148,20 @@ SceneView scene_view(const rt_scene* s) {
     return v;
 }
 
+uint32_t* work_counter(rt_ctx* c, cudaStream_t s) {
+    if (!s || s == c->stream) return c->d_work;
+    std::lock_guard<std::mutex> lk(c->work_mu);
+    auto it = c->work_by_stream.find(s);
+    if (it != c->work_by_stream.end()) return it->second;
+    uint32_t* p = nullptr;
+    if (cudaMalloc(&p, 64 * sizeof(uint32_t)) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    c->work_by_stream[s] = p;
+    return p;
+}
+
 }  // namespace rt
 
 static inline rt::SceneView view_of(const rt_scene* s) { return rt::scene_view(s); }
@@ -229,6 +243,7 @@ int32_t rt_shutdown(rt_ctx* c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     dfree(c->d_status);
     dfree(c->d_work);
+    for (auto& kv : c->work_by_stream) dfree(kv.second);
     dfree(c->d_sec_scratch);
     dfree(c->d_out);
     dfree(c->d_stats);
@@ -776,7 +791,9 @@ int32_t rt_render(rt_ctx* c, rt_scene* s, const rt_camera* cam, int32_t w, int32
     if (max_bounces < 0 || max_bounces > 64)
         return fail(RT_ERR_INVALID, "rt_render: bad max_bounces %d", max_bounces);
     cudaStream_t cs = st(c, stream);
-    CU(cudaMemsetAsync(c->d_work, 0, sizeof(uint32_t), cs));
+    uint32_t* work = rt::work_counter(c, cs);
+    if (!work) return fail(RT_ERR_OOM, "rt_render: work counter");
+    CU(cudaMemsetAsync(work, 0, sizeof(uint32_t), cs));
     rt::RenderArgs a;
     a.scene = view_of(s);
     a.lights = s->lights;
@@ -788,7 +805,7 @@ int32_t rt_render(rt_ctx* c, rt_scene* s, const rt_camera* cam, int32_t w, int32
     a.rgba = rgba;
     a.image_rgb = img;
     a.stats = stats;
-    a.work_counter = c->d_work;
+    a.work_counter = work;
     a.status = c->d_status;
     CU(launch_render_cfg(c, a, c->render_cfg, cs));
     return RT_OK;

@@ -5,6 +5,7 @@
 #include <stdint.h>
 
 #include <map>
+#include <mutex>
 
 #include "../../include/rt_cuda.h"
 #include "rt_internal.cuh"
@@ -15,7 +16,12 @@ struct rt_ctx {
     int render_blocks_per_sm = 1;
     cudaStream_t stream = nullptr;
     uint32_t* d_status = nullptr;        // RT_DEV_* bits
-    uint32_t* d_work = nullptr;          // persistent-kernel work counters
+    uint32_t* d_work = nullptr;          // work counter of launches on `stream`
+    // work counters of launches on other streams, one per stream: launches
+    // on one stream are ordered, so a counter is never shared by two
+    // running kernels
+    std::map<cudaStream_t, uint32_t*> work_by_stream;
+    std::mutex work_mu;
     uint32_t* d_sec_scratch = nullptr;   // rt_gen_secondary block offsets
     size_t sec_scratch_bytes = 0;
     uint8_t* d_out = nullptr;            // rt_render_host image staging
@@ -27,8 +33,8 @@ struct rt_ctx {
     std::map<uint64_t, rt_render_config> tuned;     // autotuner cache by workload class
 };
 
-// Scene state: geometry, the double-buffered triangle order and the build
-// products (see the design doc section 3 for the layout).
+// Scene state: geometry, the double-buffered triangle order (the build's
+// permute writes the other half, `cur` flips) and the build products.
 struct rt_scene {
     uint32_t V = 0, N = 0, M = 0;
     uint32_t capV = 0, capN = 0, capM = 0;
@@ -69,4 +75,7 @@ int32_t set_error(int32_t code, const char* fmt, ...);
 int32_t scene_ensure_build(rt_scene* s);
 // Device view of the scene's current (sorted) order.
 SceneView scene_view(const rt_scene* s);
+// The persistent-kernel work counter for launches on stream s (nullptr if it
+// cannot be allocated).
+uint32_t* work_counter(rt_ctx* c, cudaStream_t s);
 }  // namespace rt

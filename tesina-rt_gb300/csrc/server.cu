@@ -5,8 +5,10 @@
 //      images were copied to pinned host staging by the same stream),
 //   2. admits uploads in arrival order: a new scene is charged to the HBM
 //      budget, least-recently-used idle scenes are evicted to make room, or
-//      the upload is rejected; admitted uploads are copied and their LBVH is
-//      built on a separate build stream,
+//      the upload is rejected; admitted uploads are handed to the upload
+//      thread, which copies them and builds their LBVH on a separate build
+//      stream (and frees evicted scenes), so that pageable copies and the
+//      device-wide synchronisation of cudaFree never hold up render launches,
 //   3. forms a render launch from the queued render requests whose scene is
 //      ready and whose framebuffer fits in the device arena, in arrival order,
 //      up to max_batch_views, and launches it (one many-image persistent
@@ -97,16 +99,28 @@ struct ServedScene {
     uint64_t bytes = 0;
     int refs = 0;               // in-flight renders
     int pending = 0;            // queued renders not yet launched
-    double last_use = 0;
+    uint64_t last_use = 0;      // submission clock of the latest use
     bool ready = false;         // BVH built
+    bool doomed = false;        // evicted under the scene cap; freed when idle
     cudaEvent_t built = nullptr;
     uint64_t upload_ticket = 0; // upload request waiting for the build
+};
+
+// Work for the upload thread: build a new scene, or free an evicted one.
+struct UpJob {
+    bool reap = false;
+    uint64_t ticket = 0, scene_id = 0;
+    const rt_scene_desc* desc = nullptr;
+    rt_scene* scene = nullptr;
+    rt_lights* lights = nullptr;
+    cudaEvent_t built = nullptr;
 };
 
 struct Req {
     uint64_t ticket;
     rt_request r;
     double submit_ms = 0, start_ms = 0, done_ms = 0;
+    uint64_t stamp = 0;          // submission clock
     int32_t status = 1;          // 1 = pending
     int32_t batch_views = 0;
     uint64_t scene_id = 0;
@@ -131,6 +145,13 @@ struct rt_server {
     std::thread th;
     bool stop = false;
     uint64_t next_ticket = 1, next_scene = 1;
+    uint64_t use_clock = 1;            // submission order, for LRU
+    int uploads_queued = 0;            // submitted uploads not yet admitted
+    // upload thread
+    std::thread up_th;
+    std::condition_variable up_cv;
+    std::deque<UpJob> up_jobs;
+    bool up_stop = false;
     std::deque<uint64_t> incoming;     // tickets in arrival order
     std::unordered_map<uint64_t, Req> reqs;
     std::map<uint64_t, ServedScene> scenes;
@@ -150,7 +171,7 @@ struct rt_server {
     std::vector<uint32_t*> h_pix_off;
     std::vector<rt_render_stats*> h_stats;
     std::deque<Launch> inflight;
-    int render_grid = 0;
+    int render_grid = 0, render_threads = 128;
     // statistics
     std::vector<double> latencies;
     uint64_t completed = 0, rejected = 0, evicted = 0, batches = 0, rays = 0, views_sum = 0;
@@ -172,11 +193,27 @@ void finish(rt_server* S, Req& q, int32_t status, double t) {
     q.done_ms = t;
     if (status == RT_OK) {
         S->completed++;
-        S->latencies.push_back(q.done_ms - q.submit_ms);
+        if (q.r.type == RT_REQ_RENDER) S->latencies.push_back(q.done_ms - q.submit_ms);
         S->last_done = std::max(S->last_done, t);
     } else {
         S->rejected++;
     }
+}
+
+// Takes an idle scene out of the table and hands its memory to the upload
+// thread.  Called with the lock held.
+void evict(rt_server* S, uint64_t id) {
+    auto it = S->scenes.find(id);
+    UpJob j;
+    j.reap = true;
+    j.scene = it->second.scene;
+    j.lights = it->second.d_lights;
+    j.built = it->second.built;
+    S->resident_bytes -= it->second.bytes;
+    S->evicted++;
+    S->scenes.erase(it);
+    S->up_jobs.push_back(j);
+    S->up_cv.notify_all();
 }
 
 // Evicts least-recently-used idle scenes until `need` more bytes fit; evicts
@@ -197,13 +234,7 @@ bool make_room(rt_server* S, uint64_t need) {
             if (!victim || sc.last_use < victim->last_use) victim = &sc;
         }
         if (!victim) return false;
-        rt_scene_destroy(S->ctx, victim->scene);
-        cudaFree(victim->d_lights);
-        if (victim->built) cudaEventDestroy(victim->built);
-        S->resident_bytes -= victim->bytes;
-        S->evicted++;
-        const uint64_t vid = victim->id;
-        S->scenes.erase(vid);
+        evict(S, victim->id);
     }
     return true;
 }
@@ -269,7 +300,6 @@ void retire(rt_server* S) {
         if (sc.ready || !sc.built) continue;
         if (cudaEventQuery(sc.built) != cudaSuccess) continue;
         sc.ready = true;
-        sc.last_use = now_ms();
         if (sc.upload_ticket) {
             Req& q = S->reqs[sc.upload_ticket];
             q.scene_id = sc.id;
@@ -278,6 +308,13 @@ void retire(rt_server* S) {
             S->done_cv.notify_all();
         }
     }
+    // scenes evicted under the scene cap, once their renders are done
+    std::vector<uint64_t> idle;
+    for (auto& kv : S->scenes) {
+        const ServedScene& sc = kv.second;
+        if (sc.doomed && sc.ready && sc.refs == 0 && sc.pending == 0) idle.push_back(kv.first);
+    }
+    for (uint64_t id : idle) evict(S, id);
 }
 
 // One render launch from the queued renders.  Called with the lock held.
@@ -322,7 +359,6 @@ bool launch_renders(rt_server* S) {
         }
         it->second.refs++;
         it->second.pending--;
-        it->second.last_use = t;
         q.start_ms = t;
         take.push_back(tk);
     }
@@ -331,6 +367,7 @@ bool launch_renders(rt_server* S) {
     if (take.empty()) return false;
     cudaStream_t cs = S->streams[slot];
     rt_render_stats* dstats = S->d_stats[slot];
+    uint64_t launch_px = 0;
     cudaMemsetAsync(dstats, 0, sizeof(rt_render_stats), cs);
     if (S->cfg.max_batch_views == 1) {
         // plain per-request path: the one-scene render kernel
@@ -357,6 +394,7 @@ bool launch_renders(rt_server* S) {
             hp[v + 1] = hp[v] + (uint32_t)(q.r.width * q.r.height);
             q.batch_views = (int32_t)take.size();
         }
+        launch_px = hp[take.size()];
         cudaMemcpyAsync(S->d_views[slot], hv, sizeof(rt::BatchView) * take.size(),
                         cudaMemcpyHostToDevice, cs);
         cudaMemcpyAsync(S->d_pix_off[slot], hp, 4 * (take.size() + 1), cudaMemcpyHostToDevice, cs);
@@ -371,7 +409,11 @@ bool launch_renders(rt_server* S) {
         a.status = S->ctx->d_status;
         a.chunk = 32;
         a.inv1e6 = S->ctx->inv1e6;
-        rt::launch_batch_render(a, 0, S->render_grid, cs);
+        // a small launch takes only the blocks its pixels need, so that
+        // launches on other streams run beside it
+        const uint64_t need = (launch_px + S->render_threads - 1) / S->render_threads;
+        const int grid = (int)std::min<uint64_t>(S->render_grid, std::max<uint64_t>(1, need));
+        rt::launch_batch_render(a, 0, grid, cs);
     }
     for (uint64_t tk : take) {
         Req& q = S->reqs[tk];
@@ -405,6 +447,7 @@ void admit_uploads(rt_server* S) {
         const uint64_t need = scene_bytes(q.r.upload);
         if (!make_room(S, need)) {
             if (S->inflight.empty()) {   // nothing will free memory: reject
+                S->uploads_queued--;
                 finish(S, q, RT_ERR_REJECTED, now_ms());
                 S->done_cv.notify_all();
             } else {
@@ -414,18 +457,64 @@ void admit_uploads(rt_server* S) {
         }
         ServedScene sc;
         sc.id = S->next_scene++;
-        q.start_ms = now_ms();
-        if (create_scene(S, q.r.upload, S->build_stream, &sc)) {
-            finish(S, q, RT_ERR_INVALID, now_ms());
-            S->done_cv.notify_all();
-            continue;
-        }
         sc.bytes = need;
         sc.upload_ticket = tk;
+        sc.last_use = q.stamp;
+        q.start_ms = now_ms();
         S->resident_bytes += need;
         S->scenes[sc.id] = sc;
+        S->uploads_queued--;
+        UpJob j;
+        j.ticket = tk;
+        j.scene_id = sc.id;
+        j.desc = q.r.upload;
+        S->up_jobs.push_back(j);
+        S->up_cv.notify_all();
     }
     S->incoming.insert(S->incoming.begin(), keep.begin(), keep.end());
+}
+
+// The upload thread: copies and builds admitted uploads on the build stream,
+// frees evicted scenes.  The lock is released while it works.
+void upload_loop(rt_server* S) {
+    cudaSetDevice(S->ctx->device);
+    std::unique_lock<std::mutex> lk(S->mu);
+    for (;;) {
+        S->up_cv.wait(lk, [&] { return S->up_stop || !S->up_jobs.empty(); });
+        if (S->up_jobs.empty()) break;   // stopping, nothing left
+        const UpJob j = S->up_jobs.front();
+        S->up_jobs.pop_front();
+        lk.unlock();
+        if (j.reap) {
+            rt_scene_destroy(S->ctx, j.scene);
+            cudaFree(j.lights);
+            if (j.built) cudaEventDestroy(j.built);
+            lk.lock();
+            continue;
+        }
+        ServedScene made;
+        const int32_t r = create_scene(S, j.desc, S->build_stream, &made);
+        lk.lock();
+        auto it = S->scenes.find(j.scene_id);
+        if (r == RT_OK && it != S->scenes.end()) {
+            it->second.scene = made.scene;
+            it->second.d_lights = made.d_lights;
+            it->second.built = made.built;   // retire() marks it ready
+        } else {
+            if (r == RT_OK) {   // not reachable: unbuilt scenes are never evicted
+                rt_scene_destroy(S->ctx, made.scene);
+                cudaFree(made.d_lights);
+                cudaEventDestroy(made.built);
+            }
+            if (it != S->scenes.end()) {
+                S->resident_bytes -= it->second.bytes;
+                S->scenes.erase(it);
+            }
+            finish(S, S->reqs[j.ticket], r ? r : RT_ERR, now_ms());
+            S->done_cv.notify_all();
+        }
+        S->cv.notify_all();
+    }
 }
 
 void server_loop(rt_server* S) {
@@ -459,7 +548,8 @@ int32_t rt_server_create(rt_ctx* c, const rt_server_cfg* cfg, rt_server** out) {
     if (!c || !cfg || !out) return fail(RT_ERR_INVALID, "rt_server_create: null argument");
     if (cfg->max_batch_views < 1 || cfg->max_batch_views > rt::kMaxBatchViews ||
         cfg->max_inflight < 1 || cfg->max_inflight > 8 || cfg->fb_arena_bytes < 4096 ||
-        cfg->fb_arena_bytes >= (1ull << 34) || cfg->fb_arena_bytes > cfg->hbm_budget_bytes)
+        cfg->fb_arena_bytes >= (1ull << 34) || cfg->fb_arena_bytes > cfg->hbm_budget_bytes ||
+        cfg->max_scenes < 0 || cfg->reserved != 0)
         return fail(RT_ERR_INVALID, "rt_server_create: bad configuration");
     rt_server* S = new (std::nothrow) rt_server();
     if (!S) return fail(RT_ERR_OOM, "rt_server_create: host allocation failed");
@@ -510,8 +600,11 @@ int32_t rt_server_create(rt_ctx* c, const rt_server_cfg* cfg, rt_server** out) {
         rt_server_destroy(S);
         return fail(RT_ERR_OOM, "rt_server_create: device resources");
     }
-    // overlapping launches share the machine
-    S->render_grid = std::max(1, bps * c->num_sms / nslot);
+    // a launch may fill the machine; launches on other streams fill in as
+    // its blocks run out of work
+    S->render_grid = std::max(1, bps * c->num_sms);
+    S->render_threads = threads;
+    S->up_th = std::thread(upload_loop, S);
     S->th = std::thread(server_loop, S);
     *out = S;
     return RT_OK;
@@ -525,11 +618,17 @@ int32_t rt_server_destroy(rt_server* S) {
     }
     S->cv.notify_all();
     if (S->th.joinable()) S->th.join();
+    {
+        std::lock_guard<std::mutex> lk(S->mu);
+        S->up_stop = true;
+    }
+    S->up_cv.notify_all();
+    if (S->up_th.joinable()) S->up_th.join();   // drains its queue first
     cudaSetDevice(S->ctx->device);
     cudaDeviceSynchronize();
     for (auto& kv : S->scenes) {
-        rt_scene_destroy(S->ctx, kv.second.scene);
-        cudaFree(kv.second.d_lights);
+        if (kv.second.scene) rt_scene_destroy(S->ctx, kv.second.scene);
+        if (kv.second.d_lights) cudaFree(kv.second.d_lights);
         if (kv.second.built) cudaEventDestroy(kv.second.built);
     }
     for (auto& L : S->inflight) cudaEventDestroy(L.done);
@@ -552,21 +651,34 @@ int32_t rt_server_destroy(rt_server* S) {
 
 int32_t rt_server_add_scene(rt_server* S, const rt_scene_desc* d, uint64_t* id) {
     if (!S || !d || !id) return fail(RT_ERR_INVALID, "rt_server_add_scene: null argument");
-    std::unique_lock<std::mutex> lk(S->mu);
     const uint64_t need = scene_bytes(d);
+    std::unique_lock<std::mutex> lk(S->mu);
     if (!make_room(S, need))
         return fail(RT_ERR_REJECTED, "rt_server_add_scene: %llu bytes exceed the budget",
                     (unsigned long long)need);
+    S->resident_bytes += need;   // reserved while the scene is built unlocked
+    lk.unlock();
     ServedScene sc;
+    cudaStream_t bs = nullptr;
+    int32_t r = cudaStreamCreateWithFlags(&bs, cudaStreamNonBlocking) == cudaSuccess
+                    ? create_scene(S, d, bs, &sc)
+                    : fail(RT_ERR_CUDA, "rt_server_add_scene: stream");
+    if (r == RT_OK && cudaStreamSynchronize(bs) != cudaSuccess) {
+        rt_scene_destroy(S->ctx, sc.scene);
+        cudaFree(sc.d_lights);
+        cudaEventDestroy(sc.built);
+        r = fail(RT_ERR_CUDA, "rt_server_add_scene: build failed");
+    }
+    if (bs) cudaStreamDestroy(bs);
+    lk.lock();
+    if (r) {
+        S->resident_bytes -= need;
+        return r;
+    }
     sc.id = S->next_scene++;
-    int32_t r = create_scene(S, d, S->build_stream, &sc);
-    if (r) return r;
-    if (cudaStreamSynchronize(S->build_stream) != cudaSuccess)
-        return fail(RT_ERR_CUDA, "rt_server_add_scene: build failed");
     sc.ready = true;
     sc.bytes = need;
-    sc.last_use = now_ms();
-    S->resident_bytes += need;
+    sc.last_use = S->use_clock++;
     S->scenes[sc.id] = sc;
     *id = sc.id;
     return RT_OK;
@@ -587,15 +699,40 @@ int32_t rt_server_submit(rt_server* S, const rt_request* r, uint64_t* ticket) {
         Req q;
         q.ticket = S->next_ticket++;
         q.r = *r;
-        if (r->type == RT_REQ_RENDER) {
-            auto it = S->scenes.find(r->scene_id);
-            if (it != S->scenes.end()) it->second.pending++;
-        }
+        q.stamp = S->use_clock++;
         q.submit_ms = now_ms();
         if (S->first_submit < 0) S->first_submit = q.submit_ms;
+        *ticket = q.ticket;
+        if (r->type == RT_REQ_RENDER) {
+            auto it = S->scenes.find(r->scene_id);
+            if (it != S->scenes.end() && it->second.doomed) {
+                S->reqs[q.ticket] = q;   // evicted: fails without queueing
+                finish(S, S->reqs[q.ticket], RT_ERR_INVALID, q.submit_ms);
+                return RT_OK;
+            }
+            if (it != S->scenes.end()) {
+                it->second.pending++;
+                it->second.last_use = q.stamp;
+            }
+        } else if (S->cfg.max_scenes > 0) {
+            // the scene cap: this upload displaces the least recently used
+            // scene now, so that eviction follows submission order
+            int live = S->uploads_queued;
+            for (auto& kv : S->scenes) live += !kv.second.doomed;
+            while (live >= S->cfg.max_scenes) {
+                ServedScene* victim = nullptr;
+                for (auto& kv : S->scenes) {
+                    ServedScene& sc = kv.second;
+                    if (!sc.doomed && (!victim || sc.last_use < victim->last_use)) victim = &sc;
+                }
+                if (!victim) break;
+                victim->doomed = true;
+                live--;
+            }
+        }
+        if (r->type == RT_REQ_UPLOAD) S->uploads_queued++;
         S->reqs[q.ticket] = q;
         S->incoming.push_back(q.ticket);
-        *ticket = q.ticket;
     }
     S->cv.notify_all();
     return RT_OK;

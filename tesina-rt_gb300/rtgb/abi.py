@@ -55,7 +55,8 @@ RT_REQ_RENDER, RT_REQ_UPLOAD = 0, 1
 
 class ServerCfg(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_uint64), ("fb_arena_bytes", C.c_uint64),
-                ("max_batch_views", C.c_int32), ("max_inflight", C.c_int32)]
+                ("max_batch_views", C.c_int32), ("max_inflight", C.c_int32),
+                ("max_scenes", C.c_int32), ("reserved", C.c_int32)]
 
 
 class Request(C.Structure):

@@ -431,9 +431,10 @@ class Batch:
 class Server:
     """An rt_server: resident scenes, admission, continuous batching."""
 
-    def __init__(self, ctx, budget=120 << 30, arena=2 << 30, max_views=256, max_inflight=2):
+    def __init__(self, ctx, budget=120 << 30, arena=2 << 30, max_views=256, max_inflight=2,
+                 max_scenes=0):
         self.ctx, self.lib = ctx, ctx.lib
-        cfg = abi.ServerCfg(budget, arena, max_views, max_inflight)
+        cfg = abi.ServerCfg(budget, arena, max_views, max_inflight, max_scenes, 0)
         h = P()
         check(self.lib, self.lib.rt_server_create(ctx.h, C.byref(cfg), C.byref(h)))
         self.h = h

@@ -319,3 +319,64 @@ def workload_batched(seed=3, count=64):
         cam = camera((0.0, 0.0, -4.0), (0.0, 0.0, 0.0), fov_deg=60.0, aspect=w / h)
         items.append(dict(scene=sc, camera=cam, width=w, height=h, max_bounces=depth))
     return dict(name="soups64_1k-500k_mixed-res", items=items)
+
+
+def _served_scene(kind, n, seed):
+    """One scene of the served pool: a soup of n triangles, or an fBm field of
+    about n triangles (2 per cell, cells 2:1) over [-2,2]x[-1,1] with 16 mirror
+    spheres (16x8 segments)."""
+    if kind == "soup":
+        return soup(n, seed=seed)
+    nz = max(2, int(round(math.sqrt(max(n - 16 * 256, 8) / 4.0))))
+    ter = Terrain(2 * nz, nz, extent=(-2.0, 2.0, -1.0, 1.0), n_spheres=16, seed=seed,
+                  sphere_seg=(16, 8))
+    return ter.scene(0)
+
+
+def workload_served(seed=5, pool=32, uploads=8, n_min=10_000, n_max=2_000_000):
+    """Served: a pool of resident scenes (soups and fBm fields alternating,
+    triangle counts log-uniform in [n_min, n_max]) and a set of scenes that
+    upload requests bring in.  Scenes are described here and made on demand
+    (``make``), so that a caller holds only what it uploads."""
+    rng = np.random.default_rng(seed)
+
+    def spec(k, base):
+        n = int(round(math.exp(rng.uniform(math.log(n_min), math.log(n_max)))))
+        return ("soup" if k % 2 == 0 else "field", n, base + k)
+
+    return dict(name="served%d_soups+fields_%dk-%dM" % (pool, n_min // 1000, n_max // 1_000_000),
+                pool=[spec(k, seed * 1000) for k in range(pool)],
+                uploads=[spec(k, seed * 1000 + 500) for k in range(uploads)],
+                make=lambda s: _served_scene(*s))
+
+
+def served_requests(count, rate, seed=7, upload_frac=0.05, min_px=128 * 128,
+                    max_px=1920 * 1080, depth=(1, 5), radius=(3.0, 6.0)):
+    """A Poisson request stream: ``count`` requests at ``rate`` per second
+    (rate None: all at time 0).  Renders have a camera on a sphere of radius
+    uniform in ``radius`` aimed at the origin, a pixel count log-uniform in
+    [min_px, max_px] at a 16:9 or 4:3 or 1:1 aspect, and a reflection depth
+    uniform in ``depth``; ``upload_frac`` of the requests upload a scene.  A
+    render names its scene by a uniform draw ``u`` in [0,1) over the scenes
+    the client can target at that point."""
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    out = []
+    aspects = (16 / 9, 4 / 3, 1.0)
+    for k in range(count):
+        if rate:
+            t += float(rng.exponential(1.0 / rate))
+        if rng.random() < upload_frac:
+            out.append(dict(kind="upload", t=t, index=int(rng.integers(0, 1 << 30))))
+            continue
+        px = math.exp(rng.uniform(math.log(min_px), math.log(max_px)))
+        a = aspects[int(rng.integers(0, 3))]
+        w = max(16, min(1920, int(round(math.sqrt(px * a)))))
+        h = max(16, min(1080, int(round(px / w))))
+        v = rng.normal(size=3)
+        v = v / np.linalg.norm(v) * rng.uniform(*radius)
+        cam = camera(tuple(float(x) for x in v), (0.0, 0.0, 0.0), fov_deg=60.0, aspect=w / h)
+        out.append(dict(kind="render", t=t, width=w, height=h,
+                        max_bounces=int(rng.integers(depth[0], depth[1] + 1)),
+                        camera=cam, u=float(rng.random())))
+    return out

@@ -109,3 +109,51 @@ def test_plain_mode_and_oversized_frame(ctx):
                         raise_on_error=False)
     assert inf.status == -8
     srv.close()
+
+
+def test_scene_cap_displaces_lru_at_submit(ctx):
+    pool = [scenes.soup(3000, seed=70 + k) for k in range(3)]
+    srv = capi.Server(ctx, budget=1 << 30, arena=16 << 20, max_views=8, max_inflight=2,
+                      max_scenes=3)
+    s0, s1, s2 = [srv.add_scene(sc) for sc in pool]
+    cam = scenes.camera((0, 0, -4), (0, 0, 0))
+    t0 = srv.submit_render(s0, cam, 48, 48, 1)          # s1 is now least recent
+    t2 = srv.submit_render(s2, cam, 48, 48, 1)          # pending while s1 goes
+    up = srv.submit_upload(scenes.soup(4000, seed=79))   # displaces s1 at submit
+    t1 = srv.submit_render(s1, cam, 48, 48, 1)
+    _, inf = srv.result(t1, 48, 48, raise_on_error=False)
+    assert inf.status == -2                              # displaced scene
+    for t in (t0, t2):
+        assert srv.result(t, 48, 48)[1].status == 0
+    _, inf = srv.result(up)
+    new = inf.scene_id
+    img, _ = srv.result(srv.submit_render(new, cam, 48, 48, 1), 48, 48)
+    assert np.array_equal(img, _plain(ctx, scenes.soup(4000, seed=79), cam, 48, 48, 1))
+    # s0 was used before s2: the next upload displaces s0 even though a render
+    # of it is queued; the queued render is still served
+    t0b = srv.submit_render(s0, cam, 48, 48, 2)
+    srv.submit_render(s2, cam, 48, 48, 1)
+    srv.submit_render(new, cam, 48, 48, 1)
+    up2 = srv.submit_upload(scenes.soup(2000, seed=80))
+    img, inf = srv.result(t0b, 48, 48)
+    assert inf.status == 0 and np.array_equal(img, _plain(ctx, pool[0], cam, 48, 48, 2))
+    assert srv.result(up2)[1].status == 0
+    _, inf = srv.result(srv.submit_render(s0, cam, 48, 48, 1), 48, 48, raise_on_error=False)
+    assert inf.status == -2
+    st = srv.stats()
+    assert st.evicted == 2 and st.resident_scenes == 3
+    srv.close()
+
+
+def test_stream_images_equal_plain_and_served(ctx):
+    from rtgb import served
+    wl = scenes.workload_served(seed=11, pool=6, uploads=3, n_min=2000, n_max=40000)
+    cache = served.SceneCache(wl)
+    reqs = scenes.served_requests(80, None, seed=12, upload_frac=0.08, min_px=24 * 24,
+                                  max_px=200 * 150)
+    a = served.run_stream(ctx, cache, reqs, max_views=1)
+    b = served.run_stream(ctx, cache, reqs, max_views=32, max_inflight=3)
+    assert a["failed"] == b["failed"] == 0 and a["upload_failed"] == b["upload_failed"] == 0
+    assert a["uploads"] >= 3 and a["evicted"] == b["evicted"] == a["uploads"]
+    assert a["crc"] == b["crc"] and len(a["crc"]) == a["renders"]
+    assert b["mean_batch_views"] > 1 and a["mean_batch_views"] == 1
