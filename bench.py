@@ -210,6 +210,72 @@ def measure_batched(ctx, lib, torch, reps=5):
             "launches_per_batch": 3, "launches_plain": 10 * len(items)}
 
 
+SERVED_KEYS = ("p50_ms", "p99_ms", "mean_ms", "max_ms", "mrays_s", "req_s", "rays", "span_ms",
+               "launches", "mean_batch_views", "failed", "upload_failed", "upload_p50_ms",
+               "evicted", "resident_scenes")
+
+
+def measure_served(ctx, rates=(2000, 1000, 300, 50), n_req=400, seed=5):
+    """Served workload: 32 resident scenes (soups and fBm fields alternating,
+    10k-2M triangles log-uniform), a 120 GB admission budget and a scene cap
+    of 32, so that each upload (5% of requests; copy + LBVH build) displaces
+    the least recently used scene.  Requests: camera on a sphere of radius
+    U[3,6] aimed at the origin, pixels log-uniform 128^2..1920x1080, depth
+    U{1..5}.  One burst (all requests at t=0: capacity) and Poisson streams
+    at several rates, each through the served configuration (continuous
+    batching: up to 256 requests per launch, 3 launches in flight) and the
+    plain per-request configuration (one rt_render launch per request, one at
+    a time).  Latency = submit to image in pinned host memory, server clock;
+    Mrays/s = primary+secondary rays / (last done - first submit).  Images
+    of the two configurations are compared request by request (CRC32)."""
+    from rtgb import scenes, served
+    wl = scenes.workload_served(seed)
+    cache = served.SceneCache(wl)
+    t = time.time()
+    for s in wl["pool"] + wl["uploads"]:
+        cache.get(s)
+    log("served: %d pool + %d upload scenes made in %.1f s" % (len(wl["pool"]), len(wl["uploads"]),
+                                                             time.time() - t))
+    cfgs = (("served", dict(max_views=256, max_inflight=3)), ("plain", dict(max_views=1)))
+    # warm-up: module loads, pinned staging, first launches
+    warm = scenes.served_requests(24, None, seed=seed + 99)
+    for _, kw in cfgs:
+        served.run_stream(ctx, cache, warm, hash_images=False, **kw)
+    runs = []
+    identical = True
+    for rate in (None,) + tuple(rates):
+        n = n_req if rate is None or rate >= 200 else max(100, int(rate * 4))
+        reqs = scenes.served_requests(n, rate, seed=seed + 100 + (rate or 0))
+        row = {"rate_req_s": rate if rate else "burst", "requests": n,
+               "uploads": sum(r["kind"] == "upload" for r in reqs)}
+        crcs = {}
+        for name, kw in cfgs:
+            r = served.run_stream(ctx, cache, reqs, **kw)
+            crcs[name] = r["crc"]
+            row[name] = {k: r[k] for k in SERVED_KEYS}
+        row["identical_images"] = bool(crcs["served"] == crcs["plain"] and
+                                       len(crcs["plain"]) == n - row["uploads"])
+        row["served_p99_le_plain_p50"] = row["served"]["p99_ms"] <= row["plain"]["p50_ms"]
+        row["mrays_ratio"] = row["served"]["mrays_s"] / max(row["plain"]["mrays_s"], 1e-9)
+        identical &= row["identical_images"]
+        log("served rate %s: served p50 %.2f p99 %.2f ms %.0f Mrays/s | plain p50 %.2f p99 %.2f ms "
+            "%.0f Mrays/s | same %s" % (row["rate_req_s"], row["served"]["p50_ms"],
+                                        row["served"]["p99_ms"], row["served"]["mrays_s"],
+                                        row["plain"]["p50_ms"], row["plain"]["p99_ms"],
+                                        row["plain"]["mrays_s"], row["identical_images"]))
+        runs.append(row)
+    burst = runs[0]
+    return {"workload": wl["name"],
+            "pool_scenes": len(wl["pool"]),
+            "pool_triangles": int(sum(s[1] for s in wl["pool"])),
+            "hbm_budget_gb": 120, "max_scenes": len(wl["pool"]), "upload_frac": 0.05,
+            "served_cfg": dict(cfgs[0][1]), "plain_cfg": dict(cfgs[1][1]),
+            "capacity_mrays_s": {"served": burst["served"]["mrays_s"],
+                                 "plain": burst["plain"]["mrays_s"],
+                                 "ratio": burst["mrays_ratio"]},
+            "identical_images": identical, "runs": runs}
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -401,6 +467,12 @@ def run_gpu(args):
             batched = measure_batched(ctx, lib, torch)
         except Exception as e:
             batched = {"error": str(e)}
+    served_leg = None
+    if world == 1 and not args.no_served:
+        try:
+            served_leg = measure_served(ctx)
+        except Exception as e:
+            served_leg = {"error": str(e)}
     cpu = None
     if world == 1 and not args.no_cpu_baseline:
         try:
@@ -422,6 +494,7 @@ def run_gpu(args):
            "roofline": roofline, "build_roofline": build_roofline,
            "cpu_baseline": cpu,
            "batched": batched,
+           "served": served_leg,
            "e2e": {"value": e2e_value, "unit": UNIT,
                    "h2d_bytes_per_step": 2 * 16 * V,
                    "d2h_bytes_per_step": 4 * w * h + 32,
@@ -447,6 +520,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-served", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         log("warmup raised to 3")

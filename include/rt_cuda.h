@@ -427,6 +427,12 @@ RT_API int32_t rt_server_add_scene(rt_server* server, const rt_scene_desc* desc,
  * used scene evicted at submit: renders already submitted for it are still
  * served, later ones fail with RT_ERR_INVALID. */
 RT_API int32_t rt_server_submit(rt_server* server, const rt_request* req, uint64_t* ticket);
+/* An upload request that returns the new scene's id at once: renders may
+ * name it immediately and are served once its LBVH is built (they fail if
+ * the upload is rejected).  The descriptor stays caller-owned until the
+ * upload's result is taken. */
+RT_API int32_t rt_server_upload(rt_server* server, const rt_scene_desc* desc, uint64_t* ticket,
+                                uint64_t* scene_id);
 /* Blocks until the request is done; copies a render's RGBA8 image to h_rgba
  * (may be NULL) and releases it. */
 RT_API int32_t rt_server_result(rt_server* server, uint64_t ticket, uint8_t* h_rgba,

@@ -52,14 +52,35 @@ namespace {
     } while (0)
 
 template <class T>
-cudaError_t dalloc(T** p, size_t count) {
-    if (count == 0) count = 1;
-    return cudaMalloc(reinterpret_cast<void**>(p), sizeof(T) * count);
+void dfree(T*& p) {
+    if (p) cudaFree(p);
+    p = nullptr;
+}
+
+// Scene buffers: cudaMalloc/cudaFree, or, for a scene given a memory pool,
+// stream-ordered allocation from the pool on the scene's pool stream (a
+// free returns memory to the pool without synchronising the device).
+template <class T>
+cudaError_t salloc(rt_scene* s, T** p, size_t bytes) {
+    if (bytes == 0) bytes = 1;
+    if (s->pool)
+        return cudaMallocFromPoolAsync(reinterpret_cast<void**>(p), bytes, s->pool, s->pool_stream);
+    return cudaMalloc(reinterpret_cast<void**>(p), bytes);
 }
 
 template <class T>
-void dfree(T*& p) {
-    if (p) cudaFree(p);
+cudaError_t salloc_n(rt_scene* s, T** p, size_t count) {
+    return salloc(s, p, sizeof(T) * (count ? count : 1));
+}
+
+template <class T>
+void sfree(rt_scene* s, T*& p) {
+    if (p) {
+        if (s->pool)
+            cudaFreeAsync(p, s->pool_stream);
+        else
+            cudaFree(p);
+    }
     p = nullptr;
 }
 
@@ -69,33 +90,33 @@ void dfree(T*& p) {
 namespace {
 
 void free_build(rt_scene* s) {
-    dfree(s->d_keys_unsorted);
-    dfree(s->d_vals0);
-    dfree(s->d_keys1);
-    dfree(s->d_vals1);
-    dfree(s->d_keys_sorted);
-    dfree(s->d_vals_sorted);
-    dfree(s->d_tris);
-    dfree(s->d_leafbox);
-    dfree(s->d_nodes);
-    dfree(s->d_flags);
-    dfree(s->d_rangeL);
-    dfree(s->d_rangeR);
-    dfree(s->d_hdr);
-    dfree(s->d_scratch);
+    sfree(s, s->d_keys_unsorted);
+    sfree(s, s->d_vals0);
+    sfree(s, s->d_keys1);
+    sfree(s, s->d_vals1);
+    sfree(s, s->d_keys_sorted);
+    sfree(s, s->d_vals_sorted);
+    sfree(s, s->d_tris);
+    sfree(s, s->d_leafbox);
+    sfree(s, s->d_nodes);
+    sfree(s, s->d_flags);
+    sfree(s, s->d_rangeL);
+    sfree(s, s->d_rangeR);
+    sfree(s, s->d_hdr);
+    sfree(s, s->d_scratch);
     s->buildN = 0;
     s->scratch_bytes = 0;
 }
 
 void free_geometry(rt_scene* s) {
-    dfree(s->d_pos);
-    dfree(s->d_nrm);
+    sfree(s, s->d_pos);
+    sfree(s, s->d_nrm);
     for (int i = 0; i < 2; ++i) {
-        dfree(s->d_idx[i]);
-        dfree(s->d_map[i]);
-        dfree(s->d_orig[i]);
+        sfree(s, s->d_idx[i]);
+        sfree(s, s->d_map[i]);
+        sfree(s, s->d_orig[i]);
     }
-    dfree(s->d_mats);
+    sfree(s, s->d_mats);
     s->capV = s->capN = s->capM = 0;
 }
 
@@ -121,12 +142,13 @@ int32_t scene_ensure_build(rt_scene* s) {
     if (s->buildN >= n && s->scratch_bytes >= need_scratch && s->d_hdr) return RT_OK;
     free_build(s);
     const size_t nn = n > 1 ? n - 1 : 1;
-    if (dalloc(&s->d_keys_unsorted, n) || dalloc(&s->d_vals0, n) || dalloc(&s->d_keys1, n) ||
-        dalloc(&s->d_vals1, n) || dalloc(&s->d_keys_sorted, n) || dalloc(&s->d_vals_sorted, n) ||
-        dalloc(&s->d_tris, 3 * (size_t)n) || dalloc(&s->d_leafbox, 2 * (size_t)n) ||
-        dalloc(&s->d_nodes, 4 * nn) || dalloc(&s->d_flags, nn) || dalloc(&s->d_rangeL, nn) ||
-        dalloc(&s->d_rangeR, nn) || dalloc(&s->d_hdr, 1) ||
-        cudaMalloc(reinterpret_cast<void**>(&s->d_scratch), need_scratch)) {
+    if (salloc_n(s, &s->d_keys_unsorted, n) || salloc_n(s, &s->d_vals0, n) ||
+        salloc_n(s, &s->d_keys1, n) || salloc_n(s, &s->d_vals1, n) ||
+        salloc_n(s, &s->d_keys_sorted, n) || salloc_n(s, &s->d_vals_sorted, n) ||
+        salloc_n(s, &s->d_tris, 3 * (size_t)n) || salloc_n(s, &s->d_leafbox, 2 * (size_t)n) ||
+        salloc_n(s, &s->d_nodes, 4 * nn) || salloc_n(s, &s->d_flags, nn) ||
+        salloc_n(s, &s->d_rangeL, nn) || salloc_n(s, &s->d_rangeR, nn) ||
+        salloc_n(s, &s->d_hdr, 1) || salloc(s, &s->d_scratch, need_scratch)) {
         cudaGetLastError();
         free_build(s);
         return fail(RT_ERR_OOM, "device allocation of LBVH buffers for %u triangles failed", n);
@@ -148,6 +170,11 @@ SceneView scene_view(const rt_scene* s) {
     return v;
 }
 
+void scene_use_pool(rt_scene* s, cudaMemPool_t pool, cudaStream_t stream) {
+    s->pool = pool;
+    s->pool_stream = stream;
+}
+
 uint32_t* work_counter(rt_ctx* c, cudaStream_t s) {
     if (!s || s == c->stream) return c->d_work;
     std::lock_guard<std::mutex> lk(c->work_mu);
@@ -160,6 +187,14 @@ uint32_t* work_counter(rt_ctx* c, cudaStream_t s) {
     }
     c->work_by_stream[s] = p;
     return p;
+}
+
+void release_work_counter(rt_ctx* c, cudaStream_t s) {
+    std::lock_guard<std::mutex> lk(c->work_mu);
+    auto it = c->work_by_stream.find(s);
+    if (it == c->work_by_stream.end()) return;
+    cudaFree(it->second);
+    c->work_by_stream.erase(it);
 }
 
 }  // namespace rt
@@ -338,7 +373,8 @@ int32_t rt_scene_create(rt_ctx* c, rt_scene** out) {
 
 int32_t rt_scene_destroy(rt_ctx* c, rt_scene* s) {
     if (!s) return RT_OK;
-    if (c) cudaStreamSynchronize(c->stream);
+    // pool-allocated buffers are freed in order on the pool stream instead
+    if (c && !s->pool) cudaStreamSynchronize(c->stream);
     free_build(s);
     free_geometry(s);
     if (s->ev0) cudaEventDestroy(s->ev0);
@@ -380,10 +416,11 @@ int32_t rt_scene_upload(rt_ctx* c, rt_scene* s, const rt_scene_desc* d, rt_strea
     CU(cudaStreamSynchronize(cs));
     if (s->capV < V || s->capN < N || s->capM < M) {
         free_geometry(s);
-        if (dalloc(&s->d_pos, V) || dalloc(&s->d_nrm, V) || dalloc(&s->d_idx[0], 3 * (size_t)N) ||
-            dalloc(&s->d_idx[1], 3 * (size_t)N) || dalloc(&s->d_map[0], N) ||
-            dalloc(&s->d_map[1], N) || dalloc(&s->d_orig[0], N) || dalloc(&s->d_orig[1], N) ||
-            dalloc(&s->d_mats, M)) {
+        if (salloc_n(s, &s->d_pos, V) || salloc_n(s, &s->d_nrm, V) ||
+            salloc_n(s, &s->d_idx[0], 3 * (size_t)N) || salloc_n(s, &s->d_idx[1], 3 * (size_t)N) ||
+            salloc_n(s, &s->d_map[0], N) || salloc_n(s, &s->d_map[1], N) ||
+            salloc_n(s, &s->d_orig[0], N) || salloc_n(s, &s->d_orig[1], N) ||
+            salloc_n(s, &s->d_mats, M)) {
             cudaGetLastError();
             free_geometry(s);
             return fail(RT_ERR_OOM, "rt_scene_upload: device allocation failed");

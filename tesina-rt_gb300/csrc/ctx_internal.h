@@ -66,6 +66,10 @@ struct rt_scene {
     bool built = false;
     int depth = 30, min_leaf = 1;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // stream-ordered allocation (served scenes): buffers come from `pool` in
+    // the order of `pool_stream`; nullptr = cudaMalloc
+    cudaMemPool_t pool = nullptr;
+    cudaStream_t pool_stream = nullptr;
 };
 
 namespace rt {
@@ -78,4 +82,9 @@ SceneView scene_view(const rt_scene* s);
 // The persistent-kernel work counter for launches on stream s (nullptr if it
 // cannot be allocated).
 uint32_t* work_counter(rt_ctx* c, cudaStream_t s);
+// Gives a new, empty scene a memory pool: its buffers are allocated and freed
+// in the order of `stream`, which must carry its uploads and builds.
+void scene_use_pool(rt_scene* s, cudaMemPool_t pool, cudaStream_t stream);
+// Frees the work counter of stream s (before the stream is destroyed).
+void release_work_counter(rt_ctx* c, cudaStream_t s);
 }  // namespace rt

@@ -6,9 +6,11 @@
 //   2. admits uploads in arrival order: a new scene is charged to the HBM
 //      budget, least-recently-used idle scenes are evicted to make room, or
 //      the upload is rejected; admitted uploads are handed to the upload
-//      thread, which copies them and builds their LBVH on a separate build
-//      stream (and frees evicted scenes), so that pageable copies and the
-//      device-wide synchronisation of cudaFree never hold up render launches,
+//      thread, which copies them and builds their LBVH on a separate,
+//      high-priority build stream, and frees evicted scenes, so that
+//      pageable copies never hold up render launches.  Scene memory comes
+//      from a stream-ordered device pool: an eviction returns it to the pool
+//      without the device-wide synchronisation of cudaFree,
 //   3. forms a render launch from the queued render requests whose scene is
 //      ready and whose framebuffer fits in the device arena, in arrival order,
 //      up to max_batch_views, and launches it (one many-image persistent
@@ -101,6 +103,7 @@ struct ServedScene {
     int pending = 0;            // queued renders not yet launched
     uint64_t last_use = 0;      // submission clock of the latest use
     bool ready = false;         // BVH built
+    bool admitted = false;      // charged to the budget (an upload waits until then)
     bool doomed = false;        // evicted under the scene cap; freed when idle
     cudaEvent_t built = nullptr;
     uint64_t upload_ticket = 0; // upload request waiting for the build
@@ -146,7 +149,6 @@ struct rt_server {
     bool stop = false;
     uint64_t next_ticket = 1, next_scene = 1;
     uint64_t use_clock = 1;            // submission order, for LRU
-    int uploads_queued = 0;            // submitted uploads not yet admitted
     // upload thread
     std::thread up_th;
     std::condition_variable up_cv;
@@ -161,6 +163,7 @@ struct rt_server {
     uint8_t* d_fb = nullptr;
     uint8_t* h_fb = nullptr;           // pinned mirror of the arena
     cudaStream_t build_stream = nullptr;
+    cudaMemPool_t pool = nullptr;      // scene memory, stream-ordered on build_stream
     std::vector<cudaStream_t> streams;
     std::vector<bool> slot_busy;
     std::vector<rt::BatchView*> d_views;
@@ -171,7 +174,7 @@ struct rt_server {
     std::vector<uint32_t*> h_pix_off;
     std::vector<rt_render_stats*> h_stats;
     std::deque<Launch> inflight;
-    int render_grid = 0, render_threads = 128;
+    int render_grid = 0, render_threads = 128, render_bps = 1;
     // statistics
     std::vector<double> latencies;
     uint64_t completed = 0, rejected = 0, evicted = 0, batches = 0, rays = 0, views_sum = 0;
@@ -186,6 +189,28 @@ uint64_t scene_bytes(const rt_scene_desc* d) {
     return 32 * V + 40 * N + 32 * M                     // geometry, both orders
            + N * (24 + 48 + 32 + 64 + 12)                // sort, triangles, leaves, nodes, flags
            + 4 * (8 + 1024 + 4 + 4 * tiles * 256) + 4096;
+}
+
+// Scene memory: a device pool that keeps what is freed for later uploads.
+cudaError_t pool_create(int device, cudaMemPool_t* pool) {
+    cudaMemPoolProps props;
+    memset(&props, 0, sizeof(props));
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = device;
+    cudaError_t e = cudaMemPoolCreate(pool, &props);
+    if (e != cudaSuccess) return e;
+    uint64_t keep = UINT64_MAX;
+    return cudaMemPoolSetAttribute(*pool, cudaMemPoolAttrReleaseThreshold, &keep);
+}
+
+// Builds run on the highest-priority stream: their blocks are scheduled
+// first as render blocks retire, so an upload is not held behind a burst.
+cudaError_t build_stream_create(cudaStream_t* s) {
+    int lo = 0, hi = 0;
+    cudaError_t e = cudaDeviceGetStreamPriorityRange(&lo, &hi);
+    if (e != cudaSuccess) return e;
+    return cudaStreamCreateWithPriority(s, cudaStreamNonBlocking, hi);
 }
 
 void finish(rt_server* S, Req& q, int32_t status, double t) {
@@ -243,6 +268,7 @@ int32_t create_scene(rt_server* S, const rt_scene_desc* d, cudaStream_t stream, 
     rt_scene* sc = nullptr;
     int32_t r = rt_scene_create(S->ctx, &sc);
     if (r) return r;
+    rt::scene_use_pool(sc, S->pool, stream);
     r = rt_scene_upload(S->ctx, sc, d, stream);
     if (r) {
         rt_scene_destroy(S->ctx, sc);
@@ -254,12 +280,15 @@ int32_t create_scene(rt_server* S, const rt_scene_desc* d, cudaStream_t stream, 
         rt_scene_destroy(S->ctx, sc);
         return r;
     }
-    if (cudaMalloc(&out->d_lights, sizeof(rt_lights)) ||
+    if (cudaMallocFromPoolAsync(reinterpret_cast<void**>(&out->d_lights), sizeof(rt_lights),
+                                S->pool, stream) ||
         cudaMemcpyAsync(out->d_lights, &d->lights, sizeof(rt_lights), cudaMemcpyHostToDevice,
                         stream) ||
         cudaEventCreateWithFlags(&out->built, cudaEventDisableTiming) ||
         cudaEventRecord(out->built, stream)) {
         cudaGetLastError();
+        if (out->d_lights) cudaFreeAsync(out->d_lights, stream);
+        out->d_lights = nullptr;
         rt_scene_destroy(S->ctx, sc);
         return fail(RT_ERR_CUDA, "rt_server: scene resources");
     }
@@ -412,7 +441,14 @@ bool launch_renders(rt_server* S) {
         // a small launch takes only the blocks its pixels need, so that
         // launches on other streams run beside it
         const uint64_t need = (launch_px + S->render_threads - 1) / S->render_threads;
-        const int grid = (int)std::min<uint64_t>(S->render_grid, std::max<uint64_t>(1, need));
+        // while an upload builds, two block slots per SM stay free for its
+        // kernels: a persistent launch would otherwise hold every SM until
+        // it ends and the build's nine kernels would each wait for a gap
+        bool building = false;
+        for (auto& kv : S->scenes) building |= kv.second.admitted && !kv.second.ready;
+        const int cap = building && S->render_bps > 2
+                            ? (S->render_bps - 2) * S->ctx->num_sms : S->render_grid;
+        const int grid = (int)std::min<uint64_t>(cap, std::max<uint64_t>(1, need));
         rt::launch_batch_render(a, 0, grid, cs);
     }
     for (uint64_t tk : take) {
@@ -447,7 +483,7 @@ void admit_uploads(rt_server* S) {
         const uint64_t need = scene_bytes(q.r.upload);
         if (!make_room(S, need)) {
             if (S->inflight.empty()) {   // nothing will free memory: reject
-                S->uploads_queued--;
+                S->scenes.erase(q.scene_id);   // its queued renders fail
                 finish(S, q, RT_ERR_REJECTED, now_ms());
                 S->done_cv.notify_all();
             } else {
@@ -455,18 +491,14 @@ void admit_uploads(rt_server* S) {
             }
             continue;
         }
-        ServedScene sc;
-        sc.id = S->next_scene++;
+        ServedScene& sc = S->scenes[q.scene_id];
         sc.bytes = need;
-        sc.upload_ticket = tk;
-        sc.last_use = q.stamp;
+        sc.admitted = true;
         q.start_ms = now_ms();
         S->resident_bytes += need;
-        S->scenes[sc.id] = sc;
-        S->uploads_queued--;
         UpJob j;
         j.ticket = tk;
-        j.scene_id = sc.id;
+        j.scene_id = q.scene_id;
         j.desc = q.r.upload;
         S->up_jobs.push_back(j);
         S->up_cv.notify_all();
@@ -485,9 +517,9 @@ void upload_loop(rt_server* S) {
         const UpJob j = S->up_jobs.front();
         S->up_jobs.pop_front();
         lk.unlock();
-        if (j.reap) {
+        if (j.reap) {   // pool frees: no device synchronisation
             rt_scene_destroy(S->ctx, j.scene);
-            cudaFree(j.lights);
+            cudaFreeAsync(j.lights, S->build_stream);
             if (j.built) cudaEventDestroy(j.built);
             lk.lock();
             continue;
@@ -503,7 +535,7 @@ void upload_loop(rt_server* S) {
         } else {
             if (r == RT_OK) {   // not reachable: unbuilt scenes are never evicted
                 rt_scene_destroy(S->ctx, made.scene);
-                cudaFree(made.d_lights);
+                cudaFreeAsync(made.d_lights, S->build_stream);
                 cudaEventDestroy(made.built);
             }
             if (it != S->scenes.end()) {
@@ -563,7 +595,8 @@ int32_t rt_server_create(rt_ctx* c, const rt_server_cfg* cfg, rt_server** out) {
     const int nslot = S->cfg.max_inflight, nv = S->cfg.max_batch_views;
     bool ok = cudaMalloc(&S->d_fb, cfg->fb_arena_bytes) == cudaSuccess &&
               cudaMallocHost(&S->h_fb, cfg->fb_arena_bytes) == cudaSuccess &&
-              cudaStreamCreateWithFlags(&S->build_stream, cudaStreamNonBlocking) == cudaSuccess;
+              build_stream_create(&S->build_stream) == cudaSuccess &&
+              pool_create(c->device, &S->pool) == cudaSuccess;
     for (int k = 0; ok && k < nslot; ++k) {
         cudaStream_t st;
         rt::BatchView *dv, *hv;
@@ -577,6 +610,9 @@ int32_t rt_server_create(rt_ctx* c, const rt_server_cfg* cfg, rt_server** out) {
              cudaMalloc(&dw, 64) == cudaSuccess &&
              cudaMalloc(&ds, sizeof(rt_render_stats)) == cudaSuccess &&
              cudaMallocHost(&hs, sizeof(rt_render_stats)) == cudaSuccess;
+        // the plain path renders with rt_render, whose work counter for
+        // this stream is made here rather than in the first request
+        if (ok && nv == 1) ok = rt::work_counter(c, st) != nullptr;
         if (!ok) break;
         S->streams.push_back(st);
         S->slot_busy.push_back(false);
@@ -604,6 +640,7 @@ int32_t rt_server_create(rt_ctx* c, const rt_server_cfg* cfg, rt_server** out) {
     // its blocks run out of work
     S->render_grid = std::max(1, bps * c->num_sms);
     S->render_threads = threads;
+    S->render_bps = bps;
     S->up_th = std::thread(upload_loop, S);
     S->th = std::thread(server_loop, S);
     *out = S;
@@ -628,11 +665,14 @@ int32_t rt_server_destroy(rt_server* S) {
     cudaDeviceSynchronize();
     for (auto& kv : S->scenes) {
         if (kv.second.scene) rt_scene_destroy(S->ctx, kv.second.scene);
-        if (kv.second.d_lights) cudaFree(kv.second.d_lights);
+        if (kv.second.d_lights) cudaFreeAsync(kv.second.d_lights, S->build_stream);
         if (kv.second.built) cudaEventDestroy(kv.second.built);
     }
+    if (S->build_stream) cudaStreamSynchronize(S->build_stream);
+    if (S->pool) cudaMemPoolDestroy(S->pool);
     for (auto& L : S->inflight) cudaEventDestroy(L.done);
     for (size_t k = 0; k < S->streams.size(); ++k) {
+        rt::release_work_counter(S->ctx, S->streams[k]);
         cudaStreamDestroy(S->streams[k]);
         cudaFree(S->d_views[k]);
         cudaFreeHost(S->h_views[k]);
@@ -659,17 +699,13 @@ int32_t rt_server_add_scene(rt_server* S, const rt_scene_desc* d, uint64_t* id) 
     S->resident_bytes += need;   // reserved while the scene is built unlocked
     lk.unlock();
     ServedScene sc;
-    cudaStream_t bs = nullptr;
-    int32_t r = cudaStreamCreateWithFlags(&bs, cudaStreamNonBlocking) == cudaSuccess
-                    ? create_scene(S, d, bs, &sc)
-                    : fail(RT_ERR_CUDA, "rt_server_add_scene: stream");
-    if (r == RT_OK && cudaStreamSynchronize(bs) != cudaSuccess) {
+    int32_t r = create_scene(S, d, S->build_stream, &sc);
+    if (r == RT_OK && cudaEventSynchronize(sc.built) != cudaSuccess) {
         rt_scene_destroy(S->ctx, sc.scene);
-        cudaFree(sc.d_lights);
+        cudaFreeAsync(sc.d_lights, S->build_stream);
         cudaEventDestroy(sc.built);
         r = fail(RT_ERR_CUDA, "rt_server_add_scene: build failed");
     }
-    if (bs) cudaStreamDestroy(bs);
     lk.lock();
     if (r) {
         S->resident_bytes -= need;
@@ -677,6 +713,7 @@ int32_t rt_server_add_scene(rt_server* S, const rt_scene_desc* d, uint64_t* id) 
     }
     sc.id = S->next_scene++;
     sc.ready = true;
+    sc.admitted = true;
     sc.bytes = need;
     sc.last_use = S->use_clock++;
     S->scenes[sc.id] = sc;
@@ -684,7 +721,7 @@ int32_t rt_server_add_scene(rt_server* S, const rt_scene_desc* d, uint64_t* id) 
     return RT_OK;
 }
 
-int32_t rt_server_submit(rt_server* S, const rt_request* r, uint64_t* ticket) {
+static int32_t submit(rt_server* S, const rt_request* r, uint64_t* ticket, uint64_t* scene_id) {
     if (!S || !r || !ticket) return fail(RT_ERR_INVALID, "rt_server_submit: null argument");
     if (r->type == RT_REQ_RENDER) {
         if (r->width <= 0 || r->height <= 0 || r->max_bounces < 0 || r->max_bounces > 64)
@@ -717,7 +754,7 @@ int32_t rt_server_submit(rt_server* S, const rt_request* r, uint64_t* ticket) {
         } else if (S->cfg.max_scenes > 0) {
             // the scene cap: this upload displaces the least recently used
             // scene now, so that eviction follows submission order
-            int live = S->uploads_queued;
+            int live = 0;
             for (auto& kv : S->scenes) live += !kv.second.doomed;
             while (live >= S->cfg.max_scenes) {
                 ServedScene* victim = nullptr;
@@ -730,12 +767,36 @@ int32_t rt_server_submit(rt_server* S, const rt_request* r, uint64_t* ticket) {
                 live--;
             }
         }
-        if (r->type == RT_REQ_UPLOAD) S->uploads_queued++;
+        if (r->type == RT_REQ_UPLOAD) {
+            // the scene exists from now on: renders may name it at once and
+            // wait for its build
+            ServedScene sc;
+            sc.id = S->next_scene++;
+            sc.upload_ticket = q.ticket;
+            sc.last_use = q.stamp;
+            S->scenes[sc.id] = sc;
+            q.scene_id = sc.id;
+            if (scene_id) *scene_id = sc.id;
+        }
         S->reqs[q.ticket] = q;
         S->incoming.push_back(q.ticket);
     }
     S->cv.notify_all();
     return RT_OK;
+}
+
+int32_t rt_server_submit(rt_server* S, const rt_request* r, uint64_t* ticket) {
+    return submit(S, r, ticket, nullptr);
+}
+
+int32_t rt_server_upload(rt_server* S, const rt_scene_desc* desc, uint64_t* ticket,
+                         uint64_t* scene_id) {
+    if (!desc || !scene_id) return fail(RT_ERR_INVALID, "rt_server_upload: null argument");
+    rt_request r;
+    memset(&r, 0, sizeof(r));
+    r.type = RT_REQ_UPLOAD;
+    r.upload = desc;
+    return submit(S, &r, ticket, scene_id);
 }
 
 int32_t rt_server_result(rt_server* S, uint64_t ticket, uint8_t* h_rgba, rt_request_info* info) {

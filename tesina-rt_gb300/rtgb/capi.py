@@ -75,6 +75,7 @@ SIGNATURES = {
     "rt_server_destroy": (I32, [P]),
     "rt_server_add_scene": (I32, [P, P, C.POINTER(C.c_uint64)]),
     "rt_server_submit": (I32, [P, P, C.POINTER(C.c_uint64)]),
+    "rt_server_upload": (I32, [P, P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
     "rt_server_result": (I32, [P, C.c_uint64, P, P]),
     "rt_server_get_stats": (I32, [P, P]),
     "rt_server_reset_stats": (I32, [P]),
@@ -459,6 +460,14 @@ class Server:
         check(self.lib, self.lib.rt_server_submit(self.h, C.byref(r), C.byref(t)))
         self._uploads[t.value] = (d, sc)        # host data stays alive until done
         return t.value
+
+    def upload(self, sc):
+        """Upload request returning (ticket, scene id); the id is usable at once."""
+        d = scene_desc(sc)
+        t, sid = C.c_uint64(0), C.c_uint64(0)
+        check(self.lib, self.lib.rt_server_upload(self.h, C.byref(d), C.byref(t), C.byref(sid)))
+        self._uploads[t.value] = (d, sc)
+        return t.value, sid.value
 
     def result(self, ticket, w=0, h=0, raise_on_error=True):
         rgba = np.zeros((h * w, 4), np.uint8) if w * h else None

@@ -3,12 +3,11 @@ stream (``scenes.served_requests``) and collects results on a second thread.
 
 The client keeps a mirror of the server's recency order (every add_scene and
 submit advances it by one, as the server's submission clock does) so that it
-never targets a scene that an upload has displaced under the scene cap, and
-an uploaded scene becomes a render target a fixed number of requests after
-its upload, waiting for the upload if needed.  The sequence of scenes,
-cameras, sizes and depths is therefore the same for every server
-configuration, and images can be compared request by request."""
-import collections
+never targets a scene that an upload has displaced under the scene cap.  An
+upload's scene id is known at submit (rt_server_upload) and is a render
+target from then on; the server holds such renders until the build is done.
+The sequence of scenes, cameras, sizes and depths is therefore the same for
+every server configuration, and images can be compared request by request."""
 import queue
 import threading
 import time
@@ -17,8 +16,6 @@ import zlib
 import numpy as np
 
 from . import capi
-
-UPLOAD_LAG = 10   # requests between an upload and its first render
 
 
 class SceneCache:
@@ -64,7 +61,7 @@ def run_stream(ctx, cache, requests, max_views, max_inflight=2, budget=120 << 30
             last[sid] = clock
         srv.reset_stats()
         todo = queue.Queue()
-        done = {}
+        done, ups = {}, {}
 
         def collect():
             while True:
@@ -73,36 +70,21 @@ def run_stream(ctx, cache, requests, max_views, max_inflight=2, budget=120 << 30
                     return
                 k, tk, w, h = item
                 img, info = srv.result(tk, w, h, raise_on_error=False)
+                if w == 0:
+                    ups[k] = (info.status, info.done_ms - info.submit_ms)
+                    continue
                 crc = zlib.crc32(img) if (hash_images and info.status == 0) else None
                 done[k] = (info.status, info.submit_ms, info.start_ms, info.done_ms,
                            info.batch_views, info.rays, crc)
 
         th = threading.Thread(target=collect, daemon=True)
         th.start()
-        uploads = collections.deque()       # (first target index, ticket, key)
-        up_lat, up_fail = [], 0
         t0 = time.perf_counter()
         for k, rq in enumerate(requests):
-            while uploads and uploads[0][0] <= k:
-                _, tk, key = uploads.popleft()
-                _, info = srv.result(tk, raise_on_error=False)
-                i = order.index(key)
-                if info.status == 0:
-                    up_lat.append(info.done_ms - info.submit_ms)
-                    order[i] = info.scene_id
-                    last[info.scene_id] = last.pop(key)
-                    if key in doomed:
-                        doomed.discard(key)
-                        doomed.add(info.scene_id)
-                else:
-                    up_fail += 1
-                    order.pop(i)
-                    last.pop(key)
-                    doomed.discard(key)
             _pace(t0, rq["t"])
             clock += 1
             if rq["kind"] == "render":
-                cand = [s for s in order if isinstance(s, int) and s not in doomed]
+                cand = [s for s in order if s not in doomed]
                 sid = cand[min(len(cand) - 1, int(rq["u"] * len(cand)))]
                 last[sid] = clock
                 tk = srv.submit_render(sid, rq["camera"], rq["width"], rq["height"],
@@ -114,24 +96,20 @@ def run_stream(ctx, cache, requests, max_views, max_inflight=2, budget=120 << 30
                     victim = min(live, key=last.get)
                     doomed.add(victim)
                     live.remove(victim)
-                ups = wl["uploads"]
-                tk = srv.submit_upload(cache.get(ups[rq["index"] % len(ups)]))
-                key = ("upload", tk)
-                order.append(key)
-                last[key] = clock
-                uploads.append((k + UPLOAD_LAG, tk, key))
-        for _, tk, _ in uploads:
-            _, info = srv.result(tk, raise_on_error=False)
-            if info.status == 0:
-                up_lat.append(info.done_ms - info.submit_ms)
-            else:
-                up_fail += 1
+                specs = wl["uploads"]
+                tk, sid = srv.upload(cache.get(specs[rq["index"] % len(specs)]))
+                order.append(sid)
+                last[sid] = clock
+                todo.put((k, tk, 0, 0))
+        submit_s = time.perf_counter() - t0
         todo.put(None)
         th.join()
         st = srv.stats()
     finally:
         srv.close()
     rend = [v for v in done.values()]
+    up_lat = [v[1] for v in ups.values() if v[0] == 0]
+    up_fail = sum(v[0] != 0 for v in ups.values())
     ok = [v for v in rend if v[0] == 0]
     lat = np.array([v[3] - v[1] for v in ok]) if ok else np.zeros(1)
     span_ms = st.last_done_ms - st.first_submit_ms
@@ -143,7 +121,7 @@ def run_stream(ctx, cache, requests, max_views, max_inflight=2, budget=120 << 30
         mean_ms=float(lat.mean()), max_ms=float(lat.max()),
         server_p50_ms=st.p50_ms, server_p99_ms=st.p99_ms,
         upload_p50_ms=float(np.median(up_lat)) if up_lat else None,
-        rays=int(st.rays), span_ms=span_ms, offered_s=offered,
+        rays=int(st.rays), span_ms=span_ms, offered_s=offered, submit_s=submit_s,
         mrays_s=st.rays / (span_ms * 1e-3) / 1e6 if span_ms > 0 else 0.0,
         req_s=len(ok) / (span_ms * 1e-3) if span_ms > 0 else 0.0,
         launches=int(st.batches), mean_batch_views=st.mean_batch_views,
