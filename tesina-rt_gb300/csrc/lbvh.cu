@@ -12,11 +12,13 @@
 //                   bvh-builder-sort.cl and bvh-builder.cpp:361-454);
 //   k_permute       rearrange_indices / rearrange_map (:49-72) fused with the
 //                   triangle records used by traversal and the leaf AABBs;
-//   k_emit_refit    one bottom-up pass that builds the radix tree (Apetrei's
+//   k_emit_chunked  one bottom-up pass that builds the radix tree (Apetrei's
 //                   agglomerative formulation of Karras' tree), collapses it
 //                   to the reference's leaf rule (find_middle, :484-552) and
 //                   computes every AABB (build_leaf_bbox / build_node_bbox,
-//                   :262-311) on the way up.
+//                   :262-311) on the way up; nodes inside a 512-triangle
+//                   chunk are joined in shared memory, the rest through
+//                   global arrival counters.
 // The per-element work lives in lbvh_dev.cuh, shared with the many-scene
 // persistent build of batch.cu.
 #include <cuda_runtime.h>
@@ -151,16 +153,35 @@ __global__ void __launch_bounds__(256) k_refit_leaves(uint32_t n, const uint32_t
     }
 }
 
-__global__ void __launch_bounds__(256) k_emit_refit(uint32_t n, const uint32_t* __restrict__ skeys,
-                                                    const float4* __restrict__ leafbox,
-                                                    float4* __restrict__ nodes,
-                                                    uint32_t* __restrict__ flags,
-                                                    uint32_t* __restrict__ rangeL,
-                                                    uint32_t* __restrict__ rangeR, int min_leaf,
-                                                    BvhHeader* __restrict__ hdr) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    emit_climb(i, n, skeys, leafbox, nodes, flags, rangeL, rangeR, min_leaf, hdr);
+constexpr int EMIT_CHUNK = 512;
+
+// emit_chunk over chunks of EMIT_CHUNK sorted triangles, one per block.
+__global__ void __launch_bounds__(EMIT_CHUNK) k_emit_chunked(
+    uint32_t n, const uint32_t* __restrict__ skeys, const float4* __restrict__ leafbox,
+    float4* __restrict__ nodes, uint32_t* __restrict__ flags, uint32_t* __restrict__ rangeL,
+    uint32_t* __restrict__ rangeR, int min_leaf, BvhHeader* __restrict__ hdr,
+    uint32_t* __restrict__ status) {
+    extern __shared__ __align__(16) unsigned char emit_smem[];
+    __shared__ uint64_t s_warp[32];
+    auto& S = *reinterpret_cast<EmitSmem<EMIT_CHUNK>*>(emit_smem);
+    emit_chunk<EMIT_CHUNK>(S, s_warp, blockIdx.x * (uint32_t)EMIT_CHUNK, n, skeys, leafbox, nodes,
+                           flags, rangeL, rangeR, min_leaf, hdr, status);
+}
+
+static cudaError_t launch_emit(const LbvhArgs& a, cudaStream_t s) {
+    const uint32_t n = a.n;
+    static const cudaError_t attr = cudaFuncSetAttribute(
+        k_emit_chunked, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        (int)sizeof(EmitSmem<EMIT_CHUNK>));
+    if (attr != cudaSuccess) return attr;
+    if (n > 1) {
+        cudaError_t e = cudaMemsetAsync(a.flags, 0, sizeof(uint32_t) * (n - 1), s);
+        if (e) return e;
+    }
+    k_emit_chunked<<<(n + EMIT_CHUNK - 1) / EMIT_CHUNK, EMIT_CHUNK, sizeof(EmitSmem<EMIT_CHUNK>),
+                     s>>>(n, a.keys_sorted, a.leafbox, a.nodes, a.flags, a.rangeL, a.rangeR,
+                          a.min_leaf, a.hdr, a.status);
+    return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------------------
@@ -214,13 +235,7 @@ cudaError_t lbvh_build(const LbvhArgs& a, cudaStream_t s) {
     k_permute<<<grid_for(n, 256, sms * 16), 256, 0, s>>>(n, a.vals_sorted, a.idx_in, a.map_in,
                                                          a.orig_in, a.pos, a.idx_out, a.map_out,
                                                          a.orig_out, a.tris, a.leafbox);
-    if (n > 1) {
-        e = cudaMemsetAsync(a.flags, 0, sizeof(uint32_t) * (n - 1), s);
-        if (e) return e;
-    }
-    k_emit_refit<<<(n + 255) / 256, 256, 0, s>>>(n, a.keys_sorted, a.leafbox, a.nodes, a.flags,
-                                                 a.rangeL, a.rangeR, a.min_leaf, a.hdr);
-    return cudaGetLastError();
+    return launch_emit(a, s);
 }
 
 size_t radix_scratch_words(uint32_t n, int passes) {
@@ -262,15 +277,9 @@ cudaError_t lbvh_refit(const LbvhArgs& a, cudaStream_t s) {
     const uint32_t n = a.n;
     k_refit_leaves<<<grid_for(n, 256, a.num_sms * 16), 256, 0, s>>>(n, a.idx_out, a.pos, a.tris,
                                                                     a.leafbox);
-    if (n > 1) {
-        cudaError_t e = cudaMemsetAsync(a.flags, 0, sizeof(uint32_t) * (n - 1), s);
-        if (e) return e;
-    }
     // the climb is deterministic in the sorted keys, so rerunning it on the
     // same keys reproduces the same topology with the new boxes
-    k_emit_refit<<<(n + 255) / 256, 256, 0, s>>>(n, a.keys_sorted, a.leafbox, a.nodes, a.flags,
-                                                 a.rangeL, a.rangeR, a.min_leaf, a.hdr);
-    return cudaGetLastError();
+    return launch_emit(a, s);
 }
 
 }  // namespace rt

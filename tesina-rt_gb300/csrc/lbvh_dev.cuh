@@ -382,6 +382,214 @@ __device__ __forceinline__ void emit_climb(uint32_t i, uint32_t n,
     }
 }
 
+// ---------------------------------------------------------------------------
+// Chunked emit + refit.  A block takes the C sorted triangles [b0, b1] and
+// starts one climber per triangle, as emit_climb does.  While a climber's
+// parent lies wholly inside the chunk, the node is assembled in shared memory
+// (each child writes its half, as in emit_climb), the arrival counter is a
+// shared atomic and the keys come from a shared copy, so that climb touches
+// no global memory; the chunk's nodes are written out at the end with
+// coalesced stores.  Only nodes whose range crosses a chunk boundary (about
+// depth x n / C of them) use the global records and counters of emit_climb.
+// The tree is the same: which climber finishes a node never changes it.
+//
+// Whether the parent stays inside is known before arriving.  With D(k) the
+// augmented delta of boundary k (D(-1) = D(n-1) = max), a left child [l, r]
+// has parent p = r whose range ends at the first k > r with D(k) > D(r), so
+// the parent is inside iff max D(r+1..b1) > D(r); a right child's parent
+// p = l-1 is inside iff max D(b0-1..l-2) > D(l-1).  Both children of a node
+// get the same answer from the chunk's prefix and suffix maxima of D.
+// ---------------------------------------------------------------------------
+template <int C>
+struct EmitSmem {
+    uint64_t d[C + 1];     // D(b0 - 1 + j)
+    uint64_t pre[C + 1];   // max D(b0 - 1 .. b0 - 1 + j)
+    uint64_t suf[C + 1];   // max D(b0 - 1 + j .. b1)
+    float4 node[C][4];     // nodes p = b0 + q, in the global layout
+    uint32_t key[C];       // sorted keys b0..b1
+    uint32_t bound[2][C];  // left child's l, right child's r
+    uint32_t flag[C];      // arrivals at node b0 + q
+};
+
+__device__ __forceinline__ uint64_t delta_or_max(const uint32_t* __restrict__ k, int64_t i,
+                                                 uint32_t n) {
+    return (i < 0 || i >= (int64_t)n - 1) ? ~0ull : delta(k, (uint32_t)i);
+}
+
+// Inclusive max-scan over the block (C threads, one value each).
+template <int C>
+__device__ __forceinline__ uint64_t block_max_scan(uint64_t v, uint64_t* s_warp) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint64_t u = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v = v > u ? v : u;
+    }
+    if (lane == 31) s_warp[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        uint64_t x = lane < C / 32 ? s_warp[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint64_t u = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x = x > u ? x : u;
+        }
+        if (lane < C / 32) s_warp[lane] = x;
+    }
+    __syncthreads();
+    if (w > 0) {
+        const uint64_t u = s_warp[w - 1];
+        v = v > u ? v : u;
+    }
+    __syncthreads();   // s_warp is reused by the next scan
+    return v;
+}
+
+// One child's half of node record `rec` (the layout emit_climb writes).
+__device__ __forceinline__ void write_half(float4* rec, bool is_left, float4 lo, float4 hi,
+                                           int32_t ref, int32_t cnt) {
+    float* f = reinterpret_cast<float*>(rec);
+    int* ri = reinterpret_cast<int*>(rec + 3);
+    if (is_left) {
+        rec[0] = make_float4(lo.x, lo.y, lo.z, hi.x);
+        *reinterpret_cast<float2*>(f + 4) = make_float2(hi.y, hi.z);
+        ri[0] = ref;
+        ri[2] = cnt;
+    } else {
+        *reinterpret_cast<float2*>(f + 6) = make_float2(lo.x, lo.y);
+        rec[2] = make_float4(lo.z, hi.x, hi.y, hi.z);
+        ri[1] = ref;
+        ri[3] = cnt;
+    }
+}
+
+template <int C>
+__device__ __forceinline__ void emit_chunk(EmitSmem<C>& S, uint64_t* s_warp, uint32_t b0,
+                                           uint32_t n, const uint32_t* __restrict__ skeys,
+                                           const float4* __restrict__ leafbox,
+                                           float4* __restrict__ nodes,
+                                           uint32_t* __restrict__ flags,
+                                           uint32_t* __restrict__ rangeL,
+                                           uint32_t* __restrict__ rangeR, int min_leaf,
+                                           BvhHeader* __restrict__ hdr,
+                                           uint32_t* __restrict__ status) {
+    const uint32_t t = threadIdx.x;
+    const uint32_t b1 = min(b0 + (uint32_t)C - 1u, n - 1u);
+    const uint32_t m = b1 - b0 + 1;   // D entries 0..m cover boundaries b0-1..b1
+    // boundaries, their prefix maxima and (by a reversed scan) suffix maxima
+    const uint64_t dt = t <= m ? delta_or_max(skeys, (int64_t)b0 - 1 + t, n) : 0ull;
+    const uint64_t dC = m == (uint32_t)C ? delta_or_max(skeys, (int64_t)b0 - 1 + C, n) : 0ull;
+    S.d[t] = dt;
+    if (t == 0) S.d[C] = dC;
+    S.flag[t] = 0;
+    if (t < m) S.key[t] = __ldg(&skeys[b0 + t]);
+    const uint64_t pf = block_max_scan<C>(dt, s_warp);
+    S.pre[t] = pf;
+    const uint32_t tr = (uint32_t)C - 1u - t;   // reversed position
+    const uint64_t dr = tr <= m ? delta_or_max(skeys, (int64_t)b0 - 1 + tr, n) : 0ull;
+    uint64_t sf = block_max_scan<C>(dr, s_warp);
+    sf = sf > dC ? sf : dC;
+    S.suf[tr] = sf;
+    if (t == (uint32_t)C - 1u) {
+        S.pre[C] = pf > dC ? pf : dC;
+        S.suf[C] = dC;
+    }
+    __syncthreads();
+    const uint32_t i = b0 + t;
+    float4 lo = make_float4(0.f, 0.f, 0.f, 0.f), hi = lo;
+    bool climbing = i < n;
+    if (climbing) {
+        lo = leafbox[2 * (size_t)i];
+        hi = leafbox[2 * (size_t)i + 1];
+    }
+    if (climbing && n == 1) {
+        hdr->root_ref = 0;
+        hdr->root_cnt = 1;
+        hdr->n_tris = 1;
+        hdr->root_lo = lo;
+        hdr->root_hi = hi;
+        climbing = false;
+    }
+    uint32_t l = i, r = i;
+    int32_t ref = (int32_t)i, cnt = 1;
+    bool local = true;
+    while (climbing) {
+        uint64_t dl, dr2;   // D(l-1), D(r)
+        if (local) {
+            dl = S.d[l - b0];
+            dr2 = S.d[r - b0 + 1];
+        } else {
+            dl = delta_or_max(skeys, (int64_t)l - 1, n);
+            dr2 = delta_or_max(skeys, (int64_t)r, n);
+        }
+        const bool is_left = dr2 < dl;
+        const uint32_t p = is_left ? r : l - 1;
+        if (local)
+            local = is_left ? (r < b1 && S.suf[r - b0 + 2] > dr2)
+                            : (l > b0 && S.pre[l - b0 - 1] > dl);
+        float4 n0, n1, n2;
+        uint32_t L, R, kL, kR;
+        if (local) {
+            const uint32_t q = p - b0;
+            write_half(S.node[q], is_left, lo, hi, ref, cnt);
+            S.bound[is_left ? 0 : 1][q] = is_left ? l : r;
+            __threadfence_block();
+            if (atomicAdd(&S.flag[q], 1u) == 0) break;   // the sibling finishes p
+            __threadfence_block();
+            n0 = S.node[q][0];
+            n1 = S.node[q][1];
+            n2 = S.node[q][2];
+            L = is_left ? l : S.bound[0][q];
+            R = is_left ? S.bound[1][q] : r;
+            kL = L >= b0 && L <= b1 ? S.key[L - b0] : 0u;
+            kR = R >= b0 && R <= b1 ? S.key[R - b0] : 0u;
+        } else {
+            write_half(nodes + 4 * (size_t)p, is_left, lo, hi, ref, cnt);
+            if (is_left)
+                rangeL[p] = l;
+            else
+                rangeR[p] = r;
+            if (atomic_add_acq_rel(&flags[p], 1u) == 0) break;
+            n0 = __ldcg(&nodes[4 * (size_t)p]);
+            n1 = __ldcg(&nodes[4 * (size_t)p + 1]);
+            n2 = __ldcg(&nodes[4 * (size_t)p + 2]);
+            L = is_left ? l : __ldcg(&rangeL[p]);
+            R = is_left ? __ldcg(&rangeR[p]) : r;
+            kL = L < n ? __ldg(&skeys[L]) : 0u;
+            kR = R < n ? __ldg(&skeys[R]) : 0u;
+        }
+        // every step must strictly widen the range; anything else is a
+        // broken invariant, reported instead of climbing on
+        if (L > l || R < r || R - L <= r - l || R >= n) {
+            atomicOr(status, RT_DEV_BADINDEX);
+            break;
+        }
+        // merge_bbox(left, right) = fmin / fmax of the two boxes of the record
+        lo = make_float4(fminf(n0.x, n1.z), fminf(n0.y, n1.w), fminf(n0.z, n2.x), 0.f);
+        hi = make_float4(fmaxf(n0.w, n2.y), fmaxf(n1.x, n2.z), fmaxf(n1.y, n2.w), 0.f);
+        const uint32_t count = R - L + 1;
+        const bool interior = count >= (uint32_t)min_leaf + 3u && kL != kR;
+        ref = interior ? (int32_t)p : (int32_t)L;
+        cnt = interior ? 0 : (int32_t)count;
+        l = L;
+        r = R;
+        if (L == 0 && R == n - 1) {
+            hdr->root_ref = ref;
+            hdr->root_cnt = cnt;
+            hdr->n_tris = n;
+            hdr->root_lo = lo;
+            hdr->root_hi = hi;
+            break;
+        }
+    }
+    // the chunk's nodes that were joined here (both children arrived)
+    __syncthreads();
+    for (uint32_t e = t; e < 4u * (uint32_t)C; e += (uint32_t)C) {
+        const uint32_t q = e >> 2;
+        if (q + 1 < m && S.flag[q] == 2u) nodes[4 * ((size_t)b0 + q) + (e & 3u)] = S.node[q][e & 3u];
+    }
+}
+
 // K climbs of emit_climb advanced in lockstep by one thread: one release
 // fence before the K arrival counters are bumped and one acquire fence before
 // the winners read their siblings, instead of one ordering point per climber
