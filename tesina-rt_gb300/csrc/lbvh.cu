@@ -12,13 +12,13 @@
 //                   bvh-builder-sort.cl and bvh-builder.cpp:361-454);
 //   k_permute       rearrange_indices / rearrange_map (:49-72) fused with the
 //                   triangle records used by traversal and the leaf AABBs;
-//   k_emit_chunked  one bottom-up pass that builds the radix tree (Apetrei's
-//                   agglomerative formulation of Karras' tree), collapses it
-//                   to the reference's leaf rule (find_middle, :484-552) and
-//                   computes every AABB (build_leaf_bbox / build_node_bbox,
-//                   :262-311) on the way up; nodes inside a 512-triangle
-//                   chunk are joined in shared memory, the rest through
-//                   global arrival counters.
+//   k_emit_level    bottom-up build of the radix tree (Apetrei's
+//                   agglomerative formulation of Karras' tree), collapsed to
+//                   the reference's leaf rule (find_middle, :484-552), with
+//                   every AABB (build_leaf_bbox / build_node_bbox, :262-311)
+//                   computed on the way up; a few launches whose warps join
+//                   runs of 32 items with shuffles (level 0 over 512
+//                   triangles per block, then over what 8 blocks left).
 // The per-element work lives in lbvh_dev.cuh, shared with the many-scene
 // persistent build of batch.cu.
 #include <cuda_runtime.h>
@@ -153,34 +153,69 @@ __global__ void __launch_bounds__(256) k_refit_leaves(uint32_t n, const uint32_t
     }
 }
 
-constexpr int EMIT_CHUNK = 512;
+constexpr int EMIT_C0 = 512;                       // triangles per level-0 block
+constexpr int EMIT_C1 = EMIT_GROUP * EMIT_FMAX;    // items per block above level 0
 
-// emit_chunk over chunks of EMIT_CHUNK sorted triangles, one per block.
-__global__ void __launch_bounds__(EMIT_CHUNK) k_emit_chunked(
+// One level of the emit (emit_level), one block per run of items.
+template <int C>
+__global__ void __launch_bounds__(C) k_emit_level(
     uint32_t n, const uint32_t* __restrict__ skeys, const float4* __restrict__ leafbox,
-    float4* __restrict__ nodes, uint32_t* __restrict__ flags, uint32_t* __restrict__ rangeL,
-    uint32_t* __restrict__ rangeR, int min_leaf, BvhHeader* __restrict__ hdr,
-    uint32_t* __restrict__ status) {
+    const EmitItem* __restrict__ in, const uint32_t* __restrict__ in_count, uint32_t n_in,
+    EmitItem* __restrict__ out, uint32_t* __restrict__ out_count, float4* __restrict__ nodes,
+    int min_leaf, BvhHeader* __restrict__ hdr, uint32_t* __restrict__ status) {
     extern __shared__ __align__(16) unsigned char emit_smem[];
-    __shared__ uint64_t s_warp[32];
-    auto& S = *reinterpret_cast<EmitSmem<EMIT_CHUNK>*>(emit_smem);
-    emit_chunk<EMIT_CHUNK>(S, s_warp, blockIdx.x * (uint32_t)EMIT_CHUNK, n, skeys, leafbox, nodes,
-                           flags, rangeL, rangeR, min_leaf, hdr, status);
+    auto& S = *reinterpret_cast<EmitSmem<C>*>(emit_smem);
+    emit_level<C>(S, blockIdx.x, n, skeys, leafbox, in, in_count, n_in, out, out_count, nodes,
+                  min_leaf, hdr, status);
 }
 
-static cudaError_t launch_emit(const LbvhArgs& a, cudaStream_t s) {
+// Blocks of level 0 and of level 1 (the two item buffers are sized for them).
+static uint32_t emit_blocks0(uint32_t n) { return (n + EMIT_C0 - 1) / EMIT_C0; }
+static uint32_t emit_blocks1(uint32_t n) { return (emit_blocks0(n) + EMIT_GROUP - 1) / EMIT_GROUP; }
+
+static size_t sort_scratch_bytes(uint32_t n, int passes) {
+    const size_t tiles = ((size_t)n + SORT_TILE - 1) / SORT_TILE;
+    return (sizeof(uint32_t) * (8 + 4 * 256 + 4 + (size_t)passes * tiles * 256) + 255) & ~(size_t)255;
+}
+
+static size_t emit_scratch_bytes(uint32_t n) {
+    const size_t blocks = (size_t)emit_blocks0(n) + emit_blocks1(n);
+    return blocks * EMIT_FMAX * sizeof(EmitItem) + ((blocks * sizeof(uint32_t) + 255) & ~(size_t)255);
+}
+
+// The emit's levels: level 0 over triangles, then levels over the items left
+// by EMIT_GROUP blocks each until a single block reaches the root.  Item
+// buffers alternate: A holds level 0, 2, ... and B level 1, 3, ....
+static cudaError_t launch_emit(const LbvhArgs& a, uint8_t* emit_scratch, cudaStream_t s) {
     const uint32_t n = a.n;
-    static const cudaError_t attr = cudaFuncSetAttribute(
-        k_emit_chunked, cudaFuncAttributeMaxDynamicSharedMemorySize,
-        (int)sizeof(EmitSmem<EMIT_CHUNK>));
-    if (attr != cudaSuccess) return attr;
-    if (n > 1) {
-        cudaError_t e = cudaMemsetAsync(a.flags, 0, sizeof(uint32_t) * (n - 1), s);
-        if (e) return e;
+    static const cudaError_t attr0 = cudaFuncSetAttribute(
+        k_emit_level<EMIT_C0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        (int)sizeof(EmitSmem<EMIT_C0>));
+    static const cudaError_t attr1 = cudaFuncSetAttribute(
+        k_emit_level<EMIT_C1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        (int)sizeof(EmitSmem<EMIT_C1>));
+    if (attr0 != cudaSuccess) return attr0;
+    if (attr1 != cudaSuccess) return attr1;
+    const uint32_t nb0 = emit_blocks0(n), nb1 = emit_blocks1(n);
+    EmitItem* items[2];
+    uint32_t* counts[2];
+    items[0] = reinterpret_cast<EmitItem*>(emit_scratch);
+    items[1] = items[0] + (size_t)nb0 * EMIT_FMAX;
+    counts[0] = reinterpret_cast<uint32_t*>(items[1] + (size_t)nb1 * EMIT_FMAX);
+    counts[1] = counts[0] + nb0;
+    k_emit_level<EMIT_C0><<<nb0, EMIT_C0, sizeof(EmitSmem<EMIT_C0>), s>>>(
+        n, a.keys_sorted, a.leafbox, nullptr, nullptr, 0, items[0], counts[0], a.nodes,
+        a.min_leaf, a.hdr, a.status);
+    uint32_t n_in = nb0;
+    int src = 0;
+    while (n_in > 1) {
+        const uint32_t g = (n_in + EMIT_GROUP - 1) / EMIT_GROUP;
+        k_emit_level<EMIT_C1><<<g, EMIT_C1, sizeof(EmitSmem<EMIT_C1>), s>>>(
+            n, a.keys_sorted, a.leafbox, items[src], counts[src], n_in, items[src ^ 1],
+            counts[src ^ 1], a.nodes, a.min_leaf, a.hdr, a.status);
+        n_in = g;
+        src ^= 1;
     }
-    k_emit_chunked<<<(n + EMIT_CHUNK - 1) / EMIT_CHUNK, EMIT_CHUNK, sizeof(EmitSmem<EMIT_CHUNK>),
-                     s>>>(n, a.keys_sorted, a.leafbox, a.nodes, a.flags, a.rangeL, a.rangeR,
-                          a.min_leaf, a.hdr, a.status);
     return cudaGetLastError();
 }
 
@@ -196,8 +231,7 @@ static int grid_for(uint32_t n, int threads, int max_blocks) {
 }
 
 size_t lbvh_scratch_bytes(uint32_t n, int passes) {
-    const size_t tiles = ((size_t)n + SORT_TILE - 1) / SORT_TILE;
-    return sizeof(uint32_t) * (8 + 4 * 256 + 4 + (size_t)passes * tiles * 256);
+    return sort_scratch_bytes(n, passes) + emit_scratch_bytes(n);
 }
 
 cudaError_t lbvh_build(const LbvhArgs& a, cudaStream_t s) {
@@ -210,7 +244,7 @@ cudaError_t lbvh_build(const LbvhArgs& a, cudaStream_t s) {
     uint32_t* tile_ctr = hist + 4 * 256;
     uint32_t* lookback = tile_ctr + 4;
     cudaError_t e;
-    e = cudaMemsetAsync(a.scratch, 0, lbvh_scratch_bytes(n, passes), s);
+    e = cudaMemsetAsync(a.scratch, 0, sort_scratch_bytes(n, passes), s);
     if (e) return e;
     // bounds init: lo = ordered(+big) via 0xFF.. (max), hi = 0 (min)
     e = cudaMemsetAsync(bounds, 0xff, 3 * sizeof(uint32_t), s);
@@ -235,7 +269,7 @@ cudaError_t lbvh_build(const LbvhArgs& a, cudaStream_t s) {
     k_permute<<<grid_for(n, 256, sms * 16), 256, 0, s>>>(n, a.vals_sorted, a.idx_in, a.map_in,
                                                          a.orig_in, a.pos, a.idx_out, a.map_out,
                                                          a.orig_out, a.tris, a.leafbox);
-    return launch_emit(a, s);
+    return launch_emit(a, reinterpret_cast<uint8_t*>(a.scratch) + sort_scratch_bytes(n, passes), s);
 }
 
 size_t radix_scratch_words(uint32_t n, int passes) {
@@ -278,8 +312,9 @@ cudaError_t lbvh_refit(const LbvhArgs& a, cudaStream_t s) {
     k_refit_leaves<<<grid_for(n, 256, a.num_sms * 16), 256, 0, s>>>(n, a.idx_out, a.pos, a.tris,
                                                                     a.leafbox);
     // the climb is deterministic in the sorted keys, so rerunning it on the
-    // same keys reproduces the same topology with the new boxes
-    return launch_emit(a, s);
+    // same keys reproduces the same topology with the new boxes; the emit's
+    // item buffers follow the sort scratch of the build (4 passes)
+    return launch_emit(a, reinterpret_cast<uint8_t*>(a.scratch) + sort_scratch_bytes(n, 4), s);
 }
 
 }  // namespace rt

@@ -383,32 +383,52 @@ __device__ __forceinline__ void emit_climb(uint32_t i, uint32_t n,
 }
 
 // ---------------------------------------------------------------------------
-// Chunked emit + refit.  A block takes the C sorted triangles [b0, b1] and
-// starts one climber per triangle, as emit_climb does.  While a climber's
-// parent lies wholly inside the chunk, the node is assembled in shared memory
-// (each child writes its half, as in emit_climb), the arrival counter is a
-// shared atomic and the keys come from a shared copy, so that climb touches
-// no global memory; the chunk's nodes are written out at the end with
-// coalesced stores.  Only nodes whose range crosses a chunk boundary (about
-// depth x n / C of them) use the global records and counters of emit_climb.
-// The tree is the same: which climber finishes a node never changes it.
+// Multi-level emit + refit, warp-synchronous.  The tree is built bottom-up
+// in a few launches ("levels").  Within a block, runs of consecutive items
+// are joined by warps: a warp holds up to 32 consecutive items, one per lane
+// (at level 0 the items are the sorted triangles).  Each lane owns the run
+// of items that starts at it; in a round, a run that is a left child (its
+// parent's split is its right boundary) takes over the run that starts at
+// the next lane if that run is the matching right child, writes the 64-byte
+// node (left half its own, right half the sibling's, shuffled across) and
+// carries on with the merged box; the absorbed lane drops out.  No shared
+// memory, barrier or fence is involved.  A run whose parent lies outside the
+// warp's items is left over; the block gathers the leftovers of its warps in
+// order and joins them again, 32 at a time, until one warp holds them all.
+// What is left then has its parent outside the block and becomes an item of
+// the next level, which gathers the items of EMIT_GROUP blocks, until one
+// block reaches the root.  A block leaves at most EMIT_FMAX items: they hang
+// off the chains of nodes crossing its two ends, each at most 64 deep (32
+// key bits + 32 index bits).
 //
-// Whether the parent stays inside is known before arriving.  With D(k) the
-// augmented delta of boundary k (D(-1) = D(n-1) = max), a left child [l, r]
-// has parent p = r whose range ends at the first k > r with D(k) > D(r), so
-// the parent is inside iff max D(r+1..b1) > D(r); a right child's parent
-// p = l-1 is inside iff max D(b0-1..l-2) > D(l-1).  Both children of a node
-// get the same answer from the chunk's prefix and suffix maxima of D.
+// The tree is the one of emit_climb.  With d[j] the augmented delta of the
+// boundary before item j of a chunk and d[c] the boundary after its last
+// item (D(-1) = D(n-1) = max), a run j..b is a left child iff d[b+1] < d[j];
+// its parent stays in the chunk iff max d[b+2..c] > d[b+1] (the parent's
+// range ends at the first boundary above d[b+1]); a right child's parent
+// stays iff max d[0..j-1] > d[j].  Above the leftovers of a chunk, the
+// boundaries between consecutive items are exactly the splits of the
+// remaining nodes (a node's inner boundaries all lie below its end
+// boundaries), so chunks and levels compose.
 // ---------------------------------------------------------------------------
-template <int C>
-struct EmitSmem {
-    uint64_t d[C + 1];     // D(b0 - 1 + j)
-    uint64_t pre[C + 1];   // max D(b0 - 1 .. b0 - 1 + j)
-    uint64_t suf[C + 1];   // max D(b0 - 1 + j .. b1)
-    float4 node[C][4];     // nodes p = b0 + q, in the global layout
-    uint32_t key[C];       // sorted keys b0..b1
-    uint32_t bound[2][C];  // left child's l, right child's r
-    uint32_t flag[C];      // arrivals at node b0 + q
+constexpr int EMIT_FMAX = 128;   // items a block may leave
+constexpr int EMIT_GROUP = 8;    // blocks of one level gathered by a block of the next
+
+// An item: leaf range, keys at its ends, box, ref / count, and the augmented
+// delta of the boundary before it.
+struct __align__(16) EmitItem {
+    uint32_t l, r, kl, kr;
+    float lo[3], hi[3];
+    int32_t ref, cnt;
+    uint64_t db;
+    uint32_t pad[2];
+};
+
+struct WarpItem {
+    uint32_t l, r, kl, kr;
+    float lox, loy, loz, hix, hiy, hiz;
+    int32_t ref, cnt;
+    uint64_t db;
 };
 
 __device__ __forceinline__ uint64_t delta_or_max(const uint32_t* __restrict__ k, int64_t i,
@@ -416,177 +436,251 @@ __device__ __forceinline__ uint64_t delta_or_max(const uint32_t* __restrict__ k,
     return (i < 0 || i >= (int64_t)n - 1) ? ~0ull : delta(k, (uint32_t)i);
 }
 
-// Inclusive max-scan over the block (C threads, one value each).
-template <int C>
-__device__ __forceinline__ uint64_t block_max_scan(uint64_t v, uint64_t* s_warp) {
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+__device__ __forceinline__ void item_to_reg(const EmitItem& e, WarpItem& w) {
+    w.l = e.l; w.r = e.r; w.kl = e.kl; w.kr = e.kr;
+    w.lox = e.lo[0]; w.loy = e.lo[1]; w.loz = e.lo[2];
+    w.hix = e.hi[0]; w.hiy = e.hi[1]; w.hiz = e.hi[2];
+    w.ref = e.ref; w.cnt = e.cnt; w.db = e.db;
+}
+
+__device__ __forceinline__ void reg_to_item(const WarpItem& w, EmitItem& e) {
+    e.l = w.l; e.r = w.r; e.kl = w.kl; e.kr = w.kr;
+    e.lo[0] = w.lox; e.lo[1] = w.loy; e.lo[2] = w.loz;
+    e.hi[0] = w.hix; e.hi[1] = w.hiy; e.hi[2] = w.hiz;
+    e.ref = w.ref; e.cnt = w.cnt; e.db = w.db;
+}
+
+// Joins the items of lanes 0..cnt-1 of the warp (all 32 lanes call it) whose
+// parents lie inside these items; `edge` is the boundary after the last item.
+// Returns true for a lane that still holds a run afterwards (its parent is
+// outside).  A run that reaches [0, n-1] writes the header instead.
+__device__ __forceinline__ bool warp_join(WarpItem& it, uint32_t cnt, uint64_t edge, uint32_t n,
+                                          int min_leaf, float4* __restrict__ nodes,
+                                          BvhHeader* __restrict__ hdr,
+                                          uint32_t* __restrict__ status) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const unsigned FULL = 0xffffffffu;
+    bool on = lane < cnt;
+    // prefix maxima of d[0..lane] and suffix maxima of d[lane..cnt]
+    const uint64_t dv = on ? it.db : 0ull;
+    uint64_t pre = dv, suf = dv;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-        const uint64_t u = __shfl_up_sync(0xffffffffu, v, o);
-        if (lane >= o) v = v > u ? v : u;
+        const uint64_t u = __shfl_up_sync(FULL, pre, o);
+        const uint64_t w = __shfl_down_sync(FULL, suf, o);
+        if (lane >= (uint32_t)o) pre = pre > u ? pre : u;
+        if (lane + (uint32_t)o < 32u) suf = suf > w ? suf : w;
     }
-    if (lane == 31) s_warp[w] = v;
-    __syncthreads();
+    suf = suf > edge ? suf : edge;
+    const uint64_t pre_left = __shfl_up_sync(FULL, pre, 1);   // max d[0..lane-1]
+    uint32_t bl = lane;   // lane of the run's last item
+    for (int round = 0;; ++round) {
+        const uint32_t nb = bl + 1u;   // first lane after the run
+        const uint32_t src = nb < 32u ? nb : 31u;
+        const uint64_t dnext = __shfl_sync(FULL, it.db, src);
+        const uint32_t s2 = nb + 1u < 32u ? nb + 1u : 31u;
+        const uint64_t sufn = __shfl_sync(FULL, suf, s2);
+        const uint64_t dR = nb < cnt ? dnext : edge;
+        const bool is_left = dR < it.db;
+        const uint64_t far = nb + 1u < cnt ? sufn : edge;   // max d[bl+2..cnt]
+        const bool inside = is_left ? (nb < cnt && far > dR) : (lane > 0 && pre_left > it.db);
+        // the run at lane nb is the matching right child when it is a right
+        // child whose parent is inside (its parent is then this run's split)
+        const bool ready_right = on && !is_left && inside;
+        const bool partner = __shfl_sync(FULL, ready_right, src) && nb < cnt;
+        const bool absorb = on && is_left && inside && partner;
+        const uint32_t p_bl = __shfl_sync(FULL, bl, src);
+        const uint32_t p_r = __shfl_sync(FULL, it.r, src);
+        const uint32_t p_kr = __shfl_sync(FULL, it.kr, src);
+        const float plx = __shfl_sync(FULL, it.lox, src), ply = __shfl_sync(FULL, it.loy, src),
+                    plz = __shfl_sync(FULL, it.loz, src);
+        const float phx = __shfl_sync(FULL, it.hix, src), phy = __shfl_sync(FULL, it.hiy, src),
+                    phz = __shfl_sync(FULL, it.hiz, src);
+        const int32_t p_ref = __shfl_sync(FULL, it.ref, src), p_cnt = __shfl_sync(FULL, it.cnt, src);
+        const uint32_t gone = __reduce_or_sync(FULL, absorb ? (1u << src) : 0u);
+        if (gone == 0u) break;
+        if (round >= 64) {   // deeper than any tree of 64-bit augmented keys
+            if (lane == 0) atomicOr(status, RT_DEV_BADINDEX);
+            break;
+        }
+        if (absorb) {
+            const uint32_t p = it.r;   // global node index: the split
+            float4* np = nodes + 4 * (size_t)p;
+            np[0] = make_float4(it.lox, it.loy, it.loz, it.hix);
+            np[1] = make_float4(it.hiy, it.hiz, plx, ply);
+            np[2] = make_float4(plz, phx, phy, phz);
+            np[3] = make_float4(__int_as_float(it.ref), __int_as_float(p_ref),
+                                __int_as_float(it.cnt), __int_as_float(p_cnt));
+            // merge_bbox(left, right): fmin / fmax, left operand first
+            it.lox = fminf(it.lox, plx); it.loy = fminf(it.loy, ply); it.loz = fminf(it.loz, plz);
+            it.hix = fmaxf(it.hix, phx); it.hiy = fmaxf(it.hiy, phy); it.hiz = fmaxf(it.hiz, phz);
+            it.r = p_r;
+            it.kr = p_kr;
+            bl = p_bl;
+            const uint32_t count = it.r - it.l + 1;
+            const bool interior = count >= (uint32_t)min_leaf + 3u && it.kl != it.kr;
+            it.ref = interior ? (int32_t)p : (int32_t)it.l;
+            it.cnt = interior ? 0 : (int32_t)count;
+            if (it.l == 0 && it.r == n - 1) {
+                hdr->root_ref = it.ref;
+                hdr->root_cnt = it.cnt;
+                hdr->n_tris = n;
+                hdr->root_lo = make_float4(it.lox, it.loy, it.loz, 0.f);
+                hdr->root_hi = make_float4(it.hix, it.hiy, it.hiz, 0.f);
+                on = false;
+            }
+        }
+        if ((gone >> lane) & 1u) on = false;
+    }
+    return on;
+}
+
+// Shared state of one emit block: the items left over by its warps, in order.
+template <int C>
+struct EmitSmem {
+    EmitItem list[C];
+    uint32_t wcount[C / 32], woff[C / 32 + 1];
+    uint64_t edge;   // boundary after the block's last item
+};
+
+// Gathers, in order, the runs still held by the warps' lanes into S.list and
+// returns their number.  Call with all C threads; `keep` marks held runs.
+template <int C>
+__device__ __forceinline__ uint32_t gather_runs(EmitSmem<C>& S, const WarpItem& it, bool keep) {
+    const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
+    const unsigned bal = __ballot_sync(0xffffffffu, keep);
+    if (lane == 0) S.wcount[w] = __popc(bal);
+    __syncthreads();   // also: every warp has read its chunk of S.list
     if (w == 0) {
-        uint64_t x = lane < C / 32 ? s_warp[lane] : 0;
+        const uint32_t v = lane < (uint32_t)(C / 32) ? S.wcount[lane] : 0u;
+        uint32_t x = v;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            const uint64_t u = __shfl_up_sync(0xffffffffu, x, o);
-            if (lane >= o) x = x > u ? x : u;
+            const uint32_t u = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= (uint32_t)o) x += u;
         }
-        if (lane < C / 32) s_warp[lane] = x;
+        if (lane < (uint32_t)(C / 32)) S.woff[lane] = x - v;
+        if (lane == 31) S.woff[C / 32] = x;
     }
     __syncthreads();
-    if (w > 0) {
-        const uint64_t u = s_warp[w - 1];
-        v = v > u ? v : u;
-    }
-    __syncthreads();   // s_warp is reused by the next scan
-    return v;
+    if (keep) reg_to_item(it, S.list[S.woff[w] + __popc(bal & ((1u << lane) - 1u))]);
+    const uint32_t m = S.woff[C / 32];
+    __syncthreads();
+    return m;
 }
 
-// One child's half of node record `rec` (the layout emit_climb writes).
-__device__ __forceinline__ void write_half(float4* rec, bool is_left, float4 lo, float4 hi,
-                                           int32_t ref, int32_t cnt) {
-    float* f = reinterpret_cast<float*>(rec);
-    int* ri = reinterpret_cast<int*>(rec + 3);
-    if (is_left) {
-        rec[0] = make_float4(lo.x, lo.y, lo.z, hi.x);
-        *reinterpret_cast<float2*>(f + 4) = make_float2(hi.y, hi.z);
-        ri[0] = ref;
-        ri[2] = cnt;
-    } else {
-        *reinterpret_cast<float2*>(f + 6) = make_float2(lo.x, lo.y);
-        rec[2] = make_float4(lo.z, hi.x, hi.y, hi.z);
-        ri[1] = ref;
-        ri[3] = cnt;
-    }
-}
-
+// One level of the emit for block `blk` (C threads = C / 32 warps).  Level 0
+// (in == null): the items are triangles blk*C .. blk*C+C-1; otherwise the
+// items left by blocks blk*EMIT_GROUP .. of the previous level (in_count[k]
+// items at in[k * EMIT_FMAX]).  Leaves the block's own items at
+// out[blk * EMIT_FMAX] and their number in out_count[blk].
 template <int C>
-__device__ __forceinline__ void emit_chunk(EmitSmem<C>& S, uint64_t* s_warp, uint32_t b0,
-                                           uint32_t n, const uint32_t* __restrict__ skeys,
+__device__ __forceinline__ void emit_level(EmitSmem<C>& S, uint32_t blk, uint32_t n,
+                                           const uint32_t* __restrict__ skeys,
                                            const float4* __restrict__ leafbox,
-                                           float4* __restrict__ nodes,
-                                           uint32_t* __restrict__ flags,
-                                           uint32_t* __restrict__ rangeL,
-                                           uint32_t* __restrict__ rangeR, int min_leaf,
+                                           const EmitItem* __restrict__ in,
+                                           const uint32_t* __restrict__ in_count,
+                                           uint32_t n_in, EmitItem* __restrict__ out,
+                                           uint32_t* __restrict__ out_count,
+                                           float4* __restrict__ nodes, int min_leaf,
                                            BvhHeader* __restrict__ hdr,
                                            uint32_t* __restrict__ status) {
-    const uint32_t t = threadIdx.x;
-    const uint32_t b1 = min(b0 + (uint32_t)C - 1u, n - 1u);
-    const uint32_t m = b1 - b0 + 1;   // D entries 0..m cover boundaries b0-1..b1
-    // boundaries, their prefix maxima and (by a reversed scan) suffix maxima
-    const uint64_t dt = t <= m ? delta_or_max(skeys, (int64_t)b0 - 1 + t, n) : 0ull;
-    const uint64_t dC = m == (uint32_t)C ? delta_or_max(skeys, (int64_t)b0 - 1 + C, n) : 0ull;
-    S.d[t] = dt;
-    if (t == 0) S.d[C] = dC;
-    S.flag[t] = 0;
-    if (t < m) S.key[t] = __ldg(&skeys[b0 + t]);
-    const uint64_t pf = block_max_scan<C>(dt, s_warp);
-    S.pre[t] = pf;
-    const uint32_t tr = (uint32_t)C - 1u - t;   // reversed position
-    const uint64_t dr = tr <= m ? delta_or_max(skeys, (int64_t)b0 - 1 + tr, n) : 0ull;
-    uint64_t sf = block_max_scan<C>(dr, s_warp);
-    sf = sf > dC ? sf : dC;
-    S.suf[tr] = sf;
-    if (t == (uint32_t)C - 1u) {
-        S.pre[C] = pf > dC ? pf : dC;
-        S.suf[C] = dC;
-    }
-    __syncthreads();
-    const uint32_t i = b0 + t;
-    float4 lo = make_float4(0.f, 0.f, 0.f, 0.f), hi = lo;
-    bool climbing = i < n;
-    if (climbing) {
-        lo = leafbox[2 * (size_t)i];
-        hi = leafbox[2 * (size_t)i + 1];
-    }
-    if (climbing && n == 1) {
-        hdr->root_ref = 0;
-        hdr->root_cnt = 1;
-        hdr->n_tris = 1;
-        hdr->root_lo = lo;
-        hdr->root_hi = hi;
-        climbing = false;
-    }
-    uint32_t l = i, r = i;
-    int32_t ref = (int32_t)i, cnt = 1;
-    bool local = true;
-    while (climbing) {
-        uint64_t dl, dr2;   // D(l-1), D(r)
-        if (local) {
-            dl = S.d[l - b0];
-            dr2 = S.d[r - b0 + 1];
-        } else {
-            dl = delta_or_max(skeys, (int64_t)l - 1, n);
-            dr2 = delta_or_max(skeys, (int64_t)r, n);
+    static_assert(C % 32 == 0 && C >= EMIT_FMAX, "block size");
+    const uint32_t t = threadIdx.x, lane = t & 31u, w = t >> 5;
+    WarpItem it;
+    bool keep;
+    uint32_t m;
+    if (!in) {
+        // level 0: warp w joins triangles b0 + 32w ..
+        const uint32_t b0 = blk * (uint32_t)C, i = b0 + t;
+        const uint32_t w0 = b0 + 32u * w;
+        const uint32_t cnt = w0 < n ? min(32u, n - w0) : 0u;
+        const bool have = i < n;
+        const uint32_t k = have ? __ldg(&skeys[i]) : 0u;
+        uint32_t kprev = __shfl_up_sync(0xffffffffu, k, 1);
+        if (lane == 0 && have && i > 0) kprev = __ldg(&skeys[i - 1]);
+        it.l = it.r = i;
+        it.kl = it.kr = k;
+        it.db = (!have || i == 0) ? ~0ull
+                                  : (((uint64_t)(kprev ^ k) << 32) | (uint64_t)((i - 1) ^ i));
+        float4 lo = make_float4(0.f, 0.f, 0.f, 0.f), hi = lo;
+        if (have) {
+            lo = leafbox[2 * (size_t)i];
+            hi = leafbox[2 * (size_t)i + 1];
         }
-        const bool is_left = dr2 < dl;
-        const uint32_t p = is_left ? r : l - 1;
-        if (local)
-            local = is_left ? (r < b1 && S.suf[r - b0 + 2] > dr2)
-                            : (l > b0 && S.pre[l - b0 - 1] > dl);
-        float4 n0, n1, n2;
-        uint32_t L, R, kL, kR;
-        if (local) {
-            const uint32_t q = p - b0;
-            write_half(S.node[q], is_left, lo, hi, ref, cnt);
-            S.bound[is_left ? 0 : 1][q] = is_left ? l : r;
-            __threadfence_block();
-            if (atomicAdd(&S.flag[q], 1u) == 0) break;   // the sibling finishes p
-            __threadfence_block();
-            n0 = S.node[q][0];
-            n1 = S.node[q][1];
-            n2 = S.node[q][2];
-            L = is_left ? l : S.bound[0][q];
-            R = is_left ? S.bound[1][q] : r;
-            kL = L >= b0 && L <= b1 ? S.key[L - b0] : 0u;
-            kR = R >= b0 && R <= b1 ? S.key[R - b0] : 0u;
-        } else {
-            write_half(nodes + 4 * (size_t)p, is_left, lo, hi, ref, cnt);
-            if (is_left)
-                rangeL[p] = l;
-            else
-                rangeR[p] = r;
-            if (atomic_add_acq_rel(&flags[p], 1u) == 0) break;
-            n0 = __ldcg(&nodes[4 * (size_t)p]);
-            n1 = __ldcg(&nodes[4 * (size_t)p + 1]);
-            n2 = __ldcg(&nodes[4 * (size_t)p + 2]);
-            L = is_left ? l : __ldcg(&rangeL[p]);
-            R = is_left ? __ldcg(&rangeR[p]) : r;
-            kL = L < n ? __ldg(&skeys[L]) : 0u;
-            kR = R < n ? __ldg(&skeys[R]) : 0u;
+        it.lox = lo.x; it.loy = lo.y; it.loz = lo.z;
+        it.hix = hi.x; it.hiy = hi.y; it.hiz = hi.z;
+        it.ref = (int32_t)i;
+        it.cnt = 1;
+        const uint64_t edge = cnt ? delta_or_max(skeys, (int64_t)w0 + cnt - 1, n) : 0ull;
+        if (n == 1) {
+            if (t == 0) {
+                hdr->root_ref = 0;
+                hdr->root_cnt = 1;
+                hdr->n_tris = 1;
+                hdr->root_lo = lo;
+                hdr->root_hi = hi;
+            }
+            if (t == 0 && out_count) out_count[blk] = 0;
+            return;
         }
-        // every step must strictly widen the range; anything else is a
-        // broken invariant, reported instead of climbing on
-        if (L > l || R < r || R - L <= r - l || R >= n) {
-            atomicOr(status, RT_DEV_BADINDEX);
-            break;
+        if (t == 0) S.edge = delta_or_max(skeys, (int64_t)min(b0 + (uint32_t)C, n) - 1, n);
+        keep = warp_join(it, cnt, edge, n, min_leaf, nodes, hdr, status);
+        m = gather_runs<C>(S, it, keep);
+    } else {
+        // the items left by EMIT_GROUP blocks of the previous level, in order
+        if (w == 0) {
+            const uint32_t k = blk * EMIT_GROUP + lane;
+            const uint32_t v = (lane < (uint32_t)EMIT_GROUP && k < n_in)
+                                   ? min(__ldg(&in_count[k]), (uint32_t)EMIT_FMAX) : 0u;
+            uint32_t x = v;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t u = __shfl_up_sync(0xffffffffu, x, o);
+                if (lane >= (uint32_t)o) x += u;
+            }
+            if (lane < (uint32_t)EMIT_GROUP) S.woff[lane] = x - v;
+            if (lane == 31) S.woff[EMIT_GROUP] = x;
         }
-        // merge_bbox(left, right) = fmin / fmax of the two boxes of the record
-        lo = make_float4(fminf(n0.x, n1.z), fminf(n0.y, n1.w), fminf(n0.z, n2.x), 0.f);
-        hi = make_float4(fmaxf(n0.w, n2.y), fmaxf(n1.x, n2.z), fmaxf(n1.y, n2.w), 0.f);
-        const uint32_t count = R - L + 1;
-        const bool interior = count >= (uint32_t)min_leaf + 3u && kL != kR;
-        ref = interior ? (int32_t)p : (int32_t)L;
-        cnt = interior ? 0 : (int32_t)count;
-        l = L;
-        r = R;
-        if (L == 0 && R == n - 1) {
-            hdr->root_ref = ref;
-            hdr->root_cnt = cnt;
-            hdr->n_tris = n;
-            hdr->root_lo = lo;
-            hdr->root_hi = hi;
-            break;
+        __syncthreads();
+        m = S.woff[EMIT_GROUP];
+        for (uint32_t e = t; e < m; e += C) {
+            int g = 0;
+            while (g + 1 < EMIT_GROUP && S.woff[g + 1] <= e) ++g;
+            S.list[e] = in[(size_t)(blk * EMIT_GROUP + g) * EMIT_FMAX + (e - S.woff[g])];
         }
+        __syncthreads();   // the last item may have been copied by another thread
+        if (t == 0 && m) S.edge = delta_or_max(skeys, (int64_t)S.list[m - 1].r, n);
+        __syncthreads();
     }
-    // the chunk's nodes that were joined here (both children arrived)
-    __syncthreads();
-    for (uint32_t e = t; e < 4u * (uint32_t)C; e += (uint32_t)C) {
-        const uint32_t q = e >> 2;
-        if (q + 1 < m && S.flag[q] == 2u) nodes[4 * ((size_t)b0 + q) + (e & 3u)] = S.node[q][e & 3u];
+    // join the gathered runs 32 at a time until one warp holds them all
+    for (int pass = 0;; ++pass) {
+        const uint32_t chunks = (m + 31u) / 32u;
+        if (chunks <= 1u || pass >= 64) {
+            if (pass >= 64 && t == 0) atomicOr(status, RT_DEV_BADINDEX);
+            if (w == 0) {
+                const uint32_t cnt = m;
+                if (lane < cnt) item_to_reg(S.list[lane], it);
+                keep = warp_join(it, min(cnt, 32u), S.edge, n, min_leaf, nodes, hdr, status);
+                const unsigned bal = __ballot_sync(0xffffffffu, keep);
+                const uint32_t nf = __popc(bal);
+                if (keep) {
+                    const uint32_t r = __popc(bal & ((1u << lane) - 1u));
+                    if (r < (uint32_t)EMIT_FMAX) reg_to_item(it, out[(size_t)blk * EMIT_FMAX + r]);
+                }
+                if (lane == 0) {
+                    if (nf > (uint32_t)EMIT_FMAX) atomicOr(status, RT_DEV_OVERFLOW);
+                    if (out_count) out_count[blk] = min(nf, (uint32_t)EMIT_FMAX);
+                }
+            }
+            return;
+        }
+        const uint32_t c0 = 32u * w;
+        const uint32_t cnt = c0 < m ? min(32u, m - c0) : 0u;
+        if (lane < cnt) item_to_reg(S.list[c0 + lane], it);
+        const uint64_t edge = c0 + 32u < m ? S.list[c0 + 32u].db : S.edge;
+        keep = warp_join(it, cnt, edge, n, min_leaf, nodes, hdr, status);
+        m = gather_runs<C>(S, it, keep);
     }
 }
 
