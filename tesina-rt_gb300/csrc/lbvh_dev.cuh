@@ -394,9 +394,9 @@ __device__ __forceinline__ void emit_climb(uint32_t i, uint32_t n,
 // carries on with the merged box; the absorbed lane drops out.  No shared
 // memory, barrier or fence is involved.  A run whose parent lies outside the
 // warp's items is left over; the block gathers the leftovers of its warps in
-// order and joins them again, 32 at a time, until one warp holds them all.
-// What is left then has its parent outside the block and becomes an item of
-// the next level, which gathers the items of EMIT_GROUP blocks, until one
+// order and joins them again, at most 32 per warp, until one warp holds them
+// all or no node inside the block is left.  What is left then has its parent
+// outside the block and becomes an item of the next level, which gathers the items of EMIT_GROUP blocks, until one
 // block reaches the root.  A block leaves at most EMIT_FMAX items: they hang
 // off the chains of nodes crossing its two ends, each at most 64 deep (32
 // key bits + 32 index bits).
@@ -653,34 +653,50 @@ __device__ __forceinline__ void emit_level(EmitSmem<C>& S, uint32_t blk, uint32_
         if (t == 0 && m) S.edge = delta_or_max(skeys, (int64_t)S.list[m - 1].r, n);
         __syncthreads();
     }
-    // join the gathered runs 32 at a time until one warp holds them all
-    for (int pass = 0;; ++pass) {
-        const uint32_t chunks = (m + 31u) / 32u;
-        if (chunks <= 1u || pass >= 64) {
-            if (pass >= 64 && t == 0) atomicOr(status, RT_DEV_BADINDEX);
+    // Join the gathered runs in chunks of at most 32, one chunk per warp,
+    // until one warp holds them all or none can be joined inside the block.
+    // A pass joins only nodes that lie inside one chunk, so passes alternate
+    // between chunks aligned at multiples of 32 and chunks shifted by 16: if
+    // a node inside the block is left, so is one whose two children are
+    // adjacent runs, and those share a chunk in one of the two layouts.  Two
+    // passes in a row without a join therefore mean that every run left has
+    // its parent outside the block.
+    uint32_t stalls = 0;
+    for (uint32_t pass = 0;; ++pass) {
+        if (m <= 32u) {
             if (w == 0) {
                 const uint32_t cnt = m;
                 if (lane < cnt) item_to_reg(S.list[lane], it);
-                keep = warp_join(it, min(cnt, 32u), S.edge, n, min_leaf, nodes, hdr, status);
+                keep = warp_join(it, cnt, S.edge, n, min_leaf, nodes, hdr, status);
                 const unsigned bal = __ballot_sync(0xffffffffu, keep);
-                const uint32_t nf = __popc(bal);
-                if (keep) {
-                    const uint32_t r = __popc(bal & ((1u << lane) - 1u));
-                    if (r < (uint32_t)EMIT_FMAX) reg_to_item(it, out[(size_t)blk * EMIT_FMAX + r]);
-                }
-                if (lane == 0) {
-                    if (nf > (uint32_t)EMIT_FMAX) atomicOr(status, RT_DEV_OVERFLOW);
-                    if (out_count) out_count[blk] = min(nf, (uint32_t)EMIT_FMAX);
-                }
+                if (keep) reg_to_item(it, out[(size_t)blk * EMIT_FMAX + __popc(bal & ((1u << lane) - 1u))]);
+                if (lane == 0 && out_count) out_count[blk] = __popc(bal);
             }
             return;
         }
-        const uint32_t c0 = 32u * w;
-        const uint32_t cnt = c0 < m ? min(32u, m - c0) : 0u;
+        if (stalls >= 2u || pass >= 2u * (uint32_t)C + 4u) {
+            if (stalls < 2u && t == 0) atomicOr(status, RT_DEV_BADINDEX);
+            // every run left has its parent outside the block: all of them,
+            // in order, are items of the next level
+            const uint32_t nf = min(m, (uint32_t)EMIT_FMAX);
+            for (uint32_t e = t; e < nf; e += (uint32_t)C) out[(size_t)blk * EMIT_FMAX + e] = S.list[e];
+            if (t == 0) {
+                if (m > (uint32_t)EMIT_FMAX) atomicOr(status, RT_DEV_OVERFLOW);
+                if (out_count) out_count[blk] = nf;
+            }
+            return;
+        }
+        // chunk w is [0, off) for w == 0, else [off + 32(w-1), off + 32w)
+        const uint32_t off = ((pass & 1u) && m + 16u <= (uint32_t)C) ? 16u : 32u;
+        const uint32_t c0 = w == 0 ? 0u : off + 32u * (w - 1u);
+        const uint32_t c1 = min(m, off + 32u * w);
+        const uint32_t cnt = c0 < m ? c1 - c0 : 0u;
         if (lane < cnt) item_to_reg(S.list[c0 + lane], it);
-        const uint64_t edge = c0 + 32u < m ? S.list[c0 + 32u].db : S.edge;
+        const uint64_t edge = c1 < m ? S.list[c1].db : S.edge;
         keep = warp_join(it, cnt, edge, n, min_leaf, nodes, hdr, status);
-        m = gather_runs<C>(S, it, keep);
+        const uint32_t m_new = gather_runs<C>(S, it, keep);
+        stalls = m_new == m ? stalls + 1u : 0u;
+        m = m_new;
     }
 }
 

@@ -130,6 +130,28 @@ def test_build_full_mid_scale_properties(ctx, orc):
     assert ctx.device_status() == 0
 
 
+@pytest.mark.parametrize("frame", [0, 11])
+def test_mid_scale_animated_frames_equal_oracle(ctx, orc, frame):
+    """The 1,240,576-triangle terrain at animation frames 0 and 11, rebuilt
+    from the previous frame's sorted order as the per-frame loop does: the
+    whole tree equals the oracle's.  Frame 11 has blocks of the emit whose
+    leftover runs outnumber a warp and all reach outside the block."""
+    ter = scenes.workload_mid()["terrain"]
+    g = capi.Scene(ctx, ter.scene(0))
+    g.build(30, 1)
+    pos, nrm = ter.frame_vertices(frame)
+    g.update_vertices(pos, nrm)
+    g.build(30, 1)
+    assert ctx.device_status() == 0
+    sc = scenes.Scene(pos, nrm, ter.idx, ter.mats, ter.mat_map, ter.lights)
+    o = orc.new_scene(sc)
+    o.build(30, 1, 0)
+    assert np.array_equal(g.sort_arrays()[2], o.sort_arrays()[2])
+    gc = g.canon()
+    assert_canon_equal(gc, o.canon())
+    tree_invariants(gc, sc.n_tris)
+
+
 def test_invalid_inputs_rejected(ctx):
     sc = scenes.soup(100, seed=1)
     bad = scenes.Scene(sc.pos4, sc.nrm4, sc.idx.copy(), sc.mats, sc.mat_map, sc.lights)
