@@ -48,7 +48,7 @@ def test_terrain_duplicates(ctx, orc, depth, min_leaf):
     _compare(g, o, sc.n_tris)
 
 
-@pytest.mark.parametrize("n", [1, 2, 3, 4, 5, 17, 4095, 4096, 4097, 8193])
+@pytest.mark.parametrize("n", [1, 2, 3, 4, 5, 17, 2047, 2048, 2049, 4095, 4096, 4097, 8193])
 def test_small_and_ragged_sizes(ctx, orc, n):
     sc = scenes.soup(n, seed=n)
     g, o = _both(ctx, orc, sc)
