@@ -210,6 +210,64 @@ def measure_batched(ctx, lib, torch, reps=5):
             "launches_per_batch": 3, "launches_plain": 10 * len(items)}
 
 
+def measure_stress(ctx, torch, builds=5):
+    """Plain method at stress scale: a 4096x2048-cell fBm field plus 1,000
+    mirror spheres (17,737,216 triangles), one LBVH build timed `builds`
+    times (median), then one 3840x2160 Whitted frame (3 point lights, depth
+    6) from each of 8 camera poses on a radius-10 sphere.  Build Mtri/s is
+    reported against the HBM roofline with the same 376 B/triangle model as
+    the main workload; Mrays/s counts primary + secondary rays (and,
+    separately, shadow rays too)."""
+    from rtgb import capi, scenes
+    wl = scenes.workload_stress()
+    t = time.time()
+    sc = wl["terrain"].scene(0)
+    log("stress: %d triangles made in %.1f s" % (sc.n_tris, time.time() - t))
+    stream = torch.cuda.Stream()
+    sh = C.c_void_p(stream.cuda_stream)
+    g = capi.Scene(ctx, sc)
+    w, h, nb = wl["width"], wl["height"], wl["max_bounces"]
+    rgba = ctx.alloc(4 * w * h)
+    stats = ctx.alloc(32)
+    ctx.sync()
+    t_build = []
+    for k in range(2 + builds):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        g.build(wl["depth"], wl["min_leaf"], stream=sh)
+        e1.record(stream)
+        stream.synchronize()
+        if k >= 2:
+            t_build.append(e0.elapsed_time(e1))
+    g.render(wl["cameras"][0], w, h, nb, rgba, None, None, stream=sh)   # warm-up
+    stats.zero(sh)
+    stream.synchronize()
+    t_render = []
+    for cam in wl["cameras"]:
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        g.render(cam, w, h, nb, rgba, None, stats, stream=sh)
+        e1.record(stream)
+        stream.synchronize()
+        t_render.append(e0.elapsed_time(e1))
+    st = stats.read(np.uint64)
+    rays, shadow = int(st[0] + st[1]), int(st[2])
+    hbm, kind = peaks()
+    mb = statistics.median(t_build)
+    ach = B_BUILD_PER_TRI * sc.n_tris / (mb * 1e-3) / 1e9
+    tr = sum(t_render)
+    return {"workload": wl["name"], "triangles": sc.n_tris, "width": w, "height": h,
+            "max_bounces": nb, "lights": 3, "poses": len(wl["cameras"]),
+            "build_ms": mb, "lbvh_mtri_s": sc.n_tris / (mb * 1e-3) / 1e6,
+            "build_roofline": {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
+                               "frac": ach / hbm, "bytes_per_tri": B_BUILD_PER_TRI,
+                               "peak_kind": kind},
+            "render_ms_per_pose": tr / len(t_render), "rays": rays, "shadow_rays": shadow,
+            "mrays_s": rays / (tr * 1e-3) / 1e6,
+            "mrays_all_incl_shadow": (rays + shadow) / (tr * 1e-3) / 1e6,
+            "device_status": ctx.device_status()}
+
+
 SERVED_KEYS = ("p50_ms", "p99_ms", "mean_ms", "max_ms", "mrays_s", "req_s", "rays", "span_ms",
                "launches", "mean_batch_views", "failed", "upload_failed", "upload_p50_ms",
                "evicted", "resident_scenes")
@@ -467,6 +525,12 @@ def run_gpu(args):
             batched = measure_batched(ctx, lib, torch)
         except Exception as e:
             batched = {"error": str(e)}
+    stress = None
+    if world == 1 and not args.no_stress:
+        try:
+            stress = measure_stress(ctx, torch)
+        except Exception as e:
+            stress = {"error": str(e)}
     served_leg = None
     if world == 1 and not args.no_served:
         try:
@@ -495,6 +559,7 @@ def run_gpu(args):
            "cpu_baseline": cpu,
            "batched": batched,
            "served": served_leg,
+           "stress": stress,
            "e2e": {"value": e2e_value, "unit": UNIT,
                    "h2d_bytes_per_step": 2 * 16 * V,
                    "d2h_bytes_per_step": 4 * w * h + 32,
@@ -521,6 +586,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-served", action="store_true")
+    ap.add_argument("--no-stress", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         log("warmup raised to 3")
