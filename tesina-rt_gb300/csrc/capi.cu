@@ -192,9 +192,31 @@ uint32_t* work_counter(rt_ctx* c, cudaStream_t s) {
 void release_work_counter(rt_ctx* c, cudaStream_t s) {
     std::lock_guard<std::mutex> lk(c->work_mu);
     auto it = c->work_by_stream.find(s);
-    if (it == c->work_by_stream.end()) return;
-    cudaFree(it->second);
-    c->work_by_stream.erase(it);
+    if (it != c->work_by_stream.end()) {
+        cudaFree(it->second);
+        c->work_by_stream.erase(it);
+    }
+    auto ia = c->accum_by_stream.find(s);
+    if (ia != c->accum_by_stream.end()) {
+        if (ia->second.first) cudaFreeAsync(ia->second.first, s);
+        c->accum_by_stream.erase(ia);
+    }
+}
+
+uint32_t* accum_buffer(rt_ctx* c, cudaStream_t s, size_t pixels) {
+    std::lock_guard<std::mutex> lk(c->work_mu);
+    auto& e = c->accum_by_stream[s];
+    if (e.first && e.second >= pixels) return e.first;
+    if (e.first) cudaFreeAsync(e.first, s);
+    e = {nullptr, 0};
+    uint32_t* p = nullptr;
+    if (cudaMallocAsync(reinterpret_cast<void**>(&p), 3 * sizeof(uint32_t) * (pixels ? pixels : 1),
+                        s) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    e = {p, pixels};
+    return p;
 }
 
 }  // namespace rt
@@ -279,6 +301,8 @@ int32_t rt_shutdown(rt_ctx* c) {
     dfree(c->d_status);
     dfree(c->d_work);
     for (auto& kv : c->work_by_stream) dfree(kv.second);
+    for (auto& kv : c->accum_by_stream)
+        if (kv.second.first) cudaFree(kv.second.first);
     dfree(c->d_sec_scratch);
     dfree(c->d_out);
     dfree(c->d_stats);
@@ -304,7 +328,7 @@ int32_t rt_stream_create(rt_ctx* c, rt_stream* s) {
 }
 
 int32_t rt_stream_destroy(rt_ctx* c, rt_stream s) {
-    (void)c;
+    if (c && s) rt::release_work_counter(c, (cudaStream_t)s);
     if (s) CU(cudaStreamDestroy((cudaStream_t)s));
     return RT_OK;
 }
@@ -778,6 +802,11 @@ static cudaError_t launch_render_cfg(rt_ctx* c, rt::RenderArgs a, const rt_rende
     if (grid > max_useful) grid = max_useful;
     if (grid < 1) grid = 1;
     a.chunk = cfg.chunk;
+    a.accum = nullptr;
+    if (rt::render_variant_pooled(cfg.variant)) {
+        a.accum = a.image_rgb ? a.image_rgb : rt::accum_buffer(c, cs, (size_t)pixels);
+        if (!a.accum) return cudaErrorMemoryAllocation;
+    }
     return rt::launch_render(a, cfg.variant, (int)grid, cs);
 }
 

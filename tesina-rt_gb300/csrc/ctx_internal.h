@@ -21,6 +21,9 @@ struct rt_ctx {
     // on one stream are ordered, so a counter is never shared by two
     // running kernels
     std::map<cudaStream_t, uint32_t*> work_by_stream;
+    // fixed-point sums of the pooled render variants, per stream, with the
+    // pixel count each holds (stream-ordered allocations)
+    std::map<cudaStream_t, std::pair<uint32_t*, size_t>> accum_by_stream;
     std::mutex work_mu;
     uint32_t* d_sec_scratch = nullptr;   // rt_gen_secondary block offsets
     size_t sec_scratch_bytes = 0;
@@ -85,6 +88,10 @@ uint32_t* work_counter(rt_ctx* c, cudaStream_t s);
 // Gives a new, empty scene a memory pool: its buffers are allocated and freed
 // in the order of `stream`, which must carry its uploads and builds.
 void scene_use_pool(rt_scene* s, cudaMemPool_t pool, cudaStream_t stream);
-// Frees the work counter of stream s (before the stream is destroyed).
+// Frees the work counter and the render sums of stream s (before the stream
+// is destroyed).
 void release_work_counter(rt_ctx* c, cudaStream_t s);
+// Render sums (3 x uint32 per pixel) for launches on stream s, at least
+// `pixels` long; grown in stream order.  nullptr if it cannot be allocated.
+uint32_t* accum_buffer(rt_ctx* c, cudaStream_t s, size_t pixels);
 }  // namespace rt

@@ -74,6 +74,182 @@ __global__ void __launch_bounds__(THREADS, MINB) k_render(RenderArgs a) {
 }
 
 // ---------------------------------------------------------------------------
+// k_render_pool: the same rays as k_render, scheduled so that a warp's lanes
+// stay busy.  A warp takes a tile of 32 pixels and traces their primary rays
+// together (coherent); the hits' shadow rays are traced as a dense list of
+// (hit, light) tasks; each hit is shaded and, if the path continues, its
+// reflection ray goes into the warp's pool in shared memory, which is traced
+// 32 rays at a time whichever pixels they come from.  A pixel's fixed-point
+// contributions are added into its accumulator (integer sums do not depend
+// on order) and k_fb_copy turns the sums into RGBA8 afterwards.  Every ray is
+// traversed and shaded exactly as in render_pixel, so the image is
+// bit-identical to k_render's.
+// ---------------------------------------------------------------------------
+namespace {
+constexpr int POOL = 64;   // reflection rays a warp can hold: < 32 left + 32 new
+
+struct WarpPool {
+    float ro[3][POOL], rd[3][POOL], rc[POOL];   // pooled rays: origin, direction, contribution
+    int rpix[POOL], rbounce[POOL];
+    float hp[3][32], hn[3][32], hd[3][32], hc[32];   // hits of the current step
+    int hid[32], hpix[32], hbounce[32];
+    unsigned hmask[32];
+    int pool_n;
+};
+}  // namespace
+
+template <int THREADS, int MINB>
+__global__ void __launch_bounds__(THREADS, MINB) k_render_pool(RenderArgs a) {
+    const SceneView S = a.scene;
+    __shared__ BvhHeader sH;
+    __shared__ rt_lights sL;
+    __shared__ WarpPool sQ[THREADS / 32];
+    if (threadIdx.x == 0) sH = *S.hdr;
+    for (int i = threadIdx.x; i < (int)(sizeof(rt_lights) / 4); i += blockDim.x)
+        reinterpret_cast<uint32_t*>(&sL)[i] = reinterpret_cast<const uint32_t*>(&a.lights)[i];
+    const int lane = threadIdx.x & 31;
+    WarpPool& Q = sQ[threadIdx.x >> 5];
+    if (lane == 0) Q.pool_n = 0;
+    __syncthreads();
+    const BvhHeader& H = sH;
+    const int pixels = a.width * a.height;
+    const unsigned lt = (1u << lane) - 1u;
+    uint64_t n_sec = 0, n_shadow = 0, n_hits = 0, n_prim = 0;
+    bool tiles = true;
+    for (;;) {
+        const int pn = Q.pool_n;
+        // 1. rays to trace: a full batch from the pool, else a new tile
+        //    of primary rays, else what is left in the pool
+        bool have = false;
+        f3 o = mk3(0.f, 0.f, 0.f), d = o;
+        float c = 1.0f, tmin = 0.0f, tmax = 1e36f;
+        int pix = 0, bounce = 0;
+        if (pn >= 32 || (!tiles && pn > 0)) {
+            const int k = min(32, pn);
+            const int j = pn - k + lane;
+            have = lane < k;
+            if (have) {
+                o = mk3(Q.ro[0][j], Q.ro[1][j], Q.ro[2][j]);
+                d = mk3(Q.rd[0][j], Q.rd[1][j], Q.rd[2][j]);
+                c = Q.rc[j];
+                pix = Q.rpix[j];
+                bounce = Q.rbounce[j];
+                tmin = 0.0001f;
+                tmax = 1e37f;
+            }
+            __syncwarp();
+            if (lane == 0) Q.pool_n = pn - k;
+        } else if (tiles) {
+            int base = 0;
+            if (lane == 0) base = (int)atomicAdd(a.work_counter, 32u);
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (base >= pixels) {
+                tiles = false;
+                continue;
+            }
+            const int gid = base + lane;
+            have = gid < pixels;
+            if (have) {
+                int x, y;
+                pixel_of(warp_tile_order(gid, a.width, a.height), a.width, a.height, 32, x, y);
+                pix = a.width * y + x;
+                o = mk3(a.cam.pos[0], a.cam.pos[1], a.cam.pos[2]);
+                d = primary_dir(a.cam, x, y, a.width, a.height, 0.0f, 0.0f);
+                ++n_prim;
+            }
+        } else {
+            break;
+        }
+        // 2. closest hits; the hits are listed in the warp's hit slots
+        bool hit_ok = false;
+        Hit hit{-1, 0.f, 0.f, 0.f};
+        if (have) {
+            const TRay r = make_tray(o, d, mk3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z), tmin);
+            hit = closest_hit(S, H, r, tmax, a.status);
+            hit_ok = hit.id >= 0;
+        }
+        const unsigned hm = __ballot_sync(0xffffffffu, hit_ok);
+        const int nh = __popc(hm);
+        if (hit_ok) {
+            const int k = __popc(hm & lt);
+            const HitInfo hi = complete_hit(S, o, d, hit);
+            Q.hp[0][k] = hi.hp.x; Q.hp[1][k] = hi.hp.y; Q.hp[2][k] = hi.hp.z;
+            Q.hn[0][k] = hi.n.x; Q.hn[1][k] = hi.n.y; Q.hn[2][k] = hi.n.z;
+            Q.hd[0][k] = d.x; Q.hd[1][k] = d.y; Q.hd[2][k] = d.z;
+            Q.hc[k] = c;
+            Q.hid[k] = hit.id;
+            Q.hpix[k] = pix;
+            Q.hbounce[k] = bounce;
+            Q.hmask[k] = 0u;
+        }
+        __syncwarp();
+        // 3. shadow rays of every hit and light, 32 at a time
+        const int nl = sL.count;
+        for (int t = lane; t < nh * nl; t += 32) {
+            const int k = t / nl, l = t - k * nl;
+            const f3 p = mk3(Q.hp[0][k], Q.hp[1][k], Q.hp[2][k]);
+            if (occluded(S, H, sL.light[l], p, a.status)) atomicOr(&Q.hmask[k], 1u << l);
+        }
+        __syncwarp();
+        // 4. shading; continuing paths put their reflection ray into the pool
+        bool push = false;
+        f3 np = mk3(0.f, 0.f, 0.f), nd = np;
+        float nc = 0.f;
+        int npix = 0, nbounce = 0;
+        if (lane < nh) {
+            const int k = lane;
+            const f3 p = mk3(Q.hp[0][k], Q.hp[1][k], Q.hp[2][k]);
+            const f3 n = mk3(Q.hn[0][k], Q.hn[1][k], Q.hn[2][k]);
+            const f3 dk = mk3(Q.hd[0][k], Q.hd[1][k], Q.hd[2][k]);
+            const float ck = Q.hc[k];
+            const rt_material mat = S.mats[__ldg(&S.map[Q.hid[k]])];
+            const uint3 col = shade_hit(sL, mat, p, n, dk, ck, Q.hmask[k]);
+            const int pk = Q.hpix[k];
+            atomicAdd(&a.accum[3 * (size_t)pk], col.x);
+            atomicAdd(&a.accum[3 * (size_t)pk + 1], col.y);
+            atomicAdd(&a.accum[3 * (size_t)pk + 2], col.z);
+            ++n_hits;
+            n_shadow += (uint32_t)nl;
+            const int bk = Q.hbounce[k];
+            if (bk != a.max_bounces && mat.reflectiveness > 0.0f) {
+                reflect_ray(dk, n, nd);
+                np = p;
+                nc = ck * mat.reflectiveness * 1.0f;
+                npix = pk;
+                nbounce = bk + 1;
+                push = true;
+                ++n_sec;
+            }
+        }
+        const unsigned pm = __ballot_sync(0xffffffffu, push);
+        const int pbase = Q.pool_n;
+        if (push) {
+            const int j = pbase + __popc(pm & lt);
+            Q.ro[0][j] = np.x; Q.ro[1][j] = np.y; Q.ro[2][j] = np.z;
+            Q.rd[0][j] = nd.x; Q.rd[1][j] = nd.y; Q.rd[2][j] = nd.z;
+            Q.rc[j] = nc;
+            Q.rpix[j] = npix;
+            Q.rbounce[j] = nbounce;
+        }
+        __syncwarp();
+        if (lane == 0) Q.pool_n = pbase + __popc(pm);
+        __syncwarp();
+    }
+    if (a.stats) {
+        n_prim = __reduce_add_sync(0xffffffffu, (unsigned)n_prim);
+        n_sec = __reduce_add_sync(0xffffffffu, (unsigned)n_sec);
+        n_shadow = __reduce_add_sync(0xffffffffu, (unsigned)n_shadow);
+        n_hits = __reduce_add_sync(0xffffffffu, (unsigned)n_hits);
+        if (lane == 0) {
+            atomicAdd((unsigned long long*)&a.stats->primary_rays, (unsigned long long)n_prim);
+            atomicAdd((unsigned long long*)&a.stats->secondary_rays, (unsigned long long)n_sec);
+            atomicAdd((unsigned long long*)&a.stats->shadow_rays, (unsigned long long)n_shadow);
+            atomicAdd((unsigned long long*)&a.stats->hits, (unsigned long long)n_hits);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // stage-wise kernels on reference-layout buffers
 // ---------------------------------------------------------------------------
 __global__ void k_gen_primary(rt_camera cam, int w, int h, int q, const rt_pixel_sample* ps,
@@ -287,11 +463,15 @@ static unsigned blocks(size_t n, int t) { return (unsigned)((n + t - 1) / t); }
 struct RenderVariant {
     int threads, min_blocks;
     void (*fn)(RenderArgs);
+    bool pooled;
 };
 static const RenderVariant kVariants[] = {
-    {64, 8, k_render<64, 8>},    {64, 12, k_render<64, 12>},  {128, 4, k_render<128, 4>},
-    {128, 6, k_render<128, 6>},  {128, 8, k_render<128, 8>},  {256, 2, k_render<256, 2>},
-    {256, 3, k_render<256, 3>},  {256, 4, k_render<256, 4>},
+    {64, 8, k_render<64, 8>, false},    {64, 12, k_render<64, 12>, false},
+    {128, 4, k_render<128, 4>, false},  {128, 6, k_render<128, 6>, false},
+    {128, 8, k_render<128, 8>, false},  {256, 2, k_render<256, 2>, false},
+    {256, 3, k_render<256, 3>, false},  {256, 4, k_render<256, 4>, false},
+    {128, 6, k_render_pool<128, 6>, true}, {128, 8, k_render_pool<128, 8>, true},
+    {256, 3, k_render_pool<256, 3>, true}, {256, 4, k_render_pool<256, 4>, true},
 };
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
@@ -305,9 +485,20 @@ int render_variant_info(int v, int* threads, int* min_blocks, const void** fn) {
     return 0;
 }
 
+bool render_variant_pooled(int v) { return v >= 0 && v < kNumVariants && kVariants[v].pooled; }
+
 cudaError_t launch_render(const RenderArgs& a, int variant, int grid, cudaStream_t s) {
     if (variant < 0 || variant >= kNumVariants) return cudaErrorInvalidValue;
+    const size_t px = (size_t)a.width * a.height;
+    if (kVariants[variant].pooled) {
+        if (!a.accum) return cudaErrorInvalidValue;
+        cudaError_t e = cudaMemsetAsync(a.accum, 0, 3 * sizeof(uint32_t) * px, s);
+        if (e != cudaSuccess) return e;
+    }
     kVariants[variant].fn<<<grid, kVariants[variant].threads, 0, s>>>(a);
+    if (kVariants[variant].pooled && px)
+        k_fb_copy<<<blocks(px, 256), 256, 0, s>>>(a.accum, reinterpret_cast<uchar4*>(a.rgba), px,
+                                                  a.inv1e6);
     return cudaGetLastError();
 }
 

@@ -20,11 +20,14 @@ struct RenderArgs {
     uint32_t* work_counter;       // zeroed before launch
     uint32_t* status;
     int chunk;                    // pixels per warp work fetch, multiple of 32
+    uint32_t* accum;              // pooled variants: fixed-point sums (3 per pixel)
 };
 
 // Render kernel variants (block size, minimum blocks per SM) for the autotuner.
 int render_variant_count();
 int render_variant_info(int v, int* threads, int* min_blocks, const void** fn);
+// True for variants that accumulate into RenderArgs::accum (k_render_pool).
+bool render_variant_pooled(int v);
 cudaError_t launch_render(const RenderArgs& a, int variant, int grid, cudaStream_t s);
 cudaError_t launch_gen_primary(const rt_camera& cam, int w, int h, int q, const rt_pixel_sample* ps,
                                size_t count, size_t offset, rt_sample* out, cudaStream_t s);
