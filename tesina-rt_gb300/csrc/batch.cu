@@ -9,8 +9,10 @@
 // scene's own buffers, exactly as a one-scene build would write them.
 //
 // rt_batch_render renders every view of the batch in ONE persistent launch:
-// warps fetch chunks of the concatenated pixel space of all images and run
-// the same per-pixel Whitted path as rt_render (trace_dev.cuh).
+// warps fetch chunks of the concatenated pixel space of all images and trace
+// the same rays as rt_render (trace_dev.cuh), either one pixel path per lane
+// (k_render_batch, used by the request loop) or with reflection rays pooled
+// per warp (k_render_batch_pool, used by rt_batch).
 //
 // rt_batch_capture records build + render in a CUDA graph that
 // rt_batch_replay relaunches.
@@ -324,14 +326,230 @@ __global__ void __launch_bounds__(THREADS, MINB) k_render_batch(BatchRenderArgs 
     }
 }
 
+// ---------------------------------------------------------------------------
+// k_render_batch_pool: the rays of k_render_batch scheduled as in
+// k_render_pool (trace.cu): warp tiles of primary rays, dense (hit, light)
+// shadow tasks, and a per-warp pool of reflection rays traced 32 at a time,
+// whichever views and pixels they belong to.  Fixed-point contributions are
+// summed into A.accum (3 per pixel of the launch's concatenated pixel space,
+// integer sums being independent of order) and k_batch_fb writes RGBA8 at
+// each view's offset afterwards.  Bit-identical to k_render_batch.
+// ---------------------------------------------------------------------------
+namespace {
+constexpr int BPOOL = 64;
+
+struct WarpPoolB {
+    float ro[3][BPOOL], rd[3][BPOOL], rc[BPOOL];
+    int rv[BPOOL], rai[BPOOL], rbounce[BPOOL];   // view, sum index, bounce
+    float hp[3][32], hn[3][32], hd[3][32], hc[32];
+    int hid[32], hv[32], hai[32], hbounce[32], hoff[33];
+    unsigned hmask[32];
+    int pool_n;
+};
+}  // namespace
+
+template <int THREADS, int MINB>
+__global__ void __launch_bounds__(THREADS, MINB) k_render_batch_pool(BatchRenderArgs A) {
+    __shared__ uint32_t s_poff[kMaxBatchViews + 1];
+    __shared__ WarpPoolB sQ[THREADS / 32];
+    for (int i = threadIdx.x; i <= A.count; i += blockDim.x) s_poff[i] = A.pix_off[i];
+    const int lane = threadIdx.x & 31;
+    WarpPoolB& Q = sQ[threadIdx.x >> 5];
+    if (lane == 0) Q.pool_n = 0;
+    __syncthreads();
+    const uint32_t total = s_poff[A.count];
+    const unsigned lt = (1u << lane) - 1u;
+    uint32_t n_prim = 0, n_sec = 0, n_shadow = 0, n_hits = 0;
+    bool tiles = true;
+    for (;;) {
+        const int pn = Q.pool_n;
+        bool have = false;
+        f3 o = mk3(0.f, 0.f, 0.f), d = o;
+        float c = 1.0f, tmin = 0.0f, tmax = 1e36f;
+        int v = 0, ai = 0, bounce = 0;
+        if (pn >= 32 || (!tiles && pn > 0)) {
+            const int k = min(32, pn);
+            const int j = pn - k + lane;
+            have = lane < k;
+            if (have) {
+                o = mk3(Q.ro[0][j], Q.ro[1][j], Q.ro[2][j]);
+                d = mk3(Q.rd[0][j], Q.rd[1][j], Q.rd[2][j]);
+                c = Q.rc[j];
+                v = Q.rv[j];
+                ai = Q.rai[j];
+                bounce = Q.rbounce[j];
+                tmin = 0.0001f;
+                tmax = 1e37f;
+            }
+            __syncwarp();
+            if (lane == 0) Q.pool_n = pn - k;
+        } else if (tiles) {
+            uint32_t base = 0;
+            if (lane == 0) base = atomicAdd(A.work_counter, 32u);
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (base >= total) {
+                tiles = false;
+                continue;
+            }
+            const uint32_t g = base + lane;
+            const int v0 = find_segment(s_poff, A.count, base);
+            have = g < total;
+            if (have) {
+                v = g < s_poff[v0 + 1] ? v0 : find_segment(s_poff, A.count, g);
+                const BatchView& V = A.views[v];
+                int x, y;
+                pixel_of(warp_tile_order((int)(g - s_poff[v]), V.width, V.height), V.width,
+                         V.height, 32, x, y);
+                ai = (int)s_poff[v] + V.width * y + x;
+                o = mk3(V.cam.pos[0], V.cam.pos[1], V.cam.pos[2]);
+                d = primary_dir(V.cam, x, y, V.width, V.height, 0.0f, 0.0f);
+                ++n_prim;
+            }
+        } else {
+            break;
+        }
+        bool hit_ok = false;
+        Hit hit{-1, 0.f, 0.f, 0.f};
+        if (have) {
+            const BatchView& V = A.views[v];
+            const BvhHeader H = *V.scene.hdr;
+            const TRay r = make_tray(o, d, mk3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z), tmin);
+            hit = closest_hit(V.scene, H, r, tmax, A.status);
+            hit_ok = hit.id >= 0;
+        }
+        const unsigned hm = __ballot_sync(0xffffffffu, hit_ok);
+        const int nh = __popc(hm);
+        int nl = 0;
+        if (hit_ok) {
+            const int k = __popc(hm & lt);
+            const HitInfo hi = complete_hit(A.views[v].scene, o, d, hit);
+            Q.hp[0][k] = hi.hp.x; Q.hp[1][k] = hi.hp.y; Q.hp[2][k] = hi.hp.z;
+            Q.hn[0][k] = hi.n.x; Q.hn[1][k] = hi.n.y; Q.hn[2][k] = hi.n.z;
+            Q.hd[0][k] = d.x; Q.hd[1][k] = d.y; Q.hd[2][k] = d.z;
+            Q.hc[k] = c;
+            Q.hid[k] = hit.id;
+            Q.hv[k] = v;
+            Q.hai[k] = ai;
+            Q.hbounce[k] = bounce;
+            Q.hmask[k] = 0u;
+            nl = A.views[v].lights->count;
+        }
+        // shadow tasks: hit k owns tasks hoff[k] .. hoff[k+1]-1 (one per light)
+        int ex = nl;
+#pragma unroll
+        for (int s = 1; s < 32; s <<= 1) {
+            const int u = __shfl_up_sync(0xffffffffu, ex, s);
+            if (lane >= s) ex += u;
+        }
+        const int ntask = __shfl_sync(0xffffffffu, ex, 31);
+        if (hit_ok) Q.hoff[__popc(hm & lt)] = ex - nl;
+        if (lane == 0) Q.hoff[nh] = ntask;
+        __syncwarp();
+        for (int t = lane; t < ntask; t += 32) {
+            int lo = 0, hi2 = nh - 1;   // the hit whose tasks contain t
+            while (lo < hi2) {
+                const int mid = (lo + hi2 + 1) >> 1;
+                if (Q.hoff[mid] <= t)
+                    lo = mid;
+                else
+                    hi2 = mid - 1;
+            }
+            const int l = t - Q.hoff[lo];
+            const BatchView& V = A.views[Q.hv[lo]];
+            const BvhHeader H = *V.scene.hdr;
+            const f3 p = mk3(Q.hp[0][lo], Q.hp[1][lo], Q.hp[2][lo]);
+            if (occluded(V.scene, H, V.lights->light[l], p, A.status))
+                atomicOr(&Q.hmask[lo], 1u << l);
+        }
+        __syncwarp();
+        bool push = false;
+        f3 np = mk3(0.f, 0.f, 0.f), nd = np;
+        float nc = 0.f;
+        int nv = 0, nai = 0, nbounce = 0;
+        if (lane < nh) {
+            const int k = lane;
+            const BatchView& V = A.views[Q.hv[k]];
+            const f3 p = mk3(Q.hp[0][k], Q.hp[1][k], Q.hp[2][k]);
+            const f3 n = mk3(Q.hn[0][k], Q.hn[1][k], Q.hn[2][k]);
+            const f3 dk = mk3(Q.hd[0][k], Q.hd[1][k], Q.hd[2][k]);
+            const float ck = Q.hc[k];
+            const rt_material mat = V.scene.mats[__ldg(&V.scene.map[Q.hid[k]])];
+            const uint3 col = shade_hit(*V.lights, mat, p, n, dk, ck, Q.hmask[k]);
+            const int ak = Q.hai[k];
+            atomicAdd(&A.accum[3 * (size_t)ak], col.x);
+            atomicAdd(&A.accum[3 * (size_t)ak + 1], col.y);
+            atomicAdd(&A.accum[3 * (size_t)ak + 2], col.z);
+            ++n_hits;
+            n_shadow += (uint32_t)V.lights->count;
+            const int bk = Q.hbounce[k];
+            if (bk != V.max_bounces && mat.reflectiveness > 0.0f) {
+                reflect_ray(dk, n, nd);
+                np = p;
+                nc = ck * mat.reflectiveness * 1.0f;
+                nv = Q.hv[k];
+                nai = ak;
+                nbounce = bk + 1;
+                push = true;
+                ++n_sec;
+            }
+        }
+        const unsigned pm = __ballot_sync(0xffffffffu, push);
+        const int pbase = Q.pool_n;
+        if (push) {
+            const int j = pbase + __popc(pm & lt);
+            Q.ro[0][j] = np.x; Q.ro[1][j] = np.y; Q.ro[2][j] = np.z;
+            Q.rd[0][j] = nd.x; Q.rd[1][j] = nd.y; Q.rd[2][j] = nd.z;
+            Q.rc[j] = nc;
+            Q.rv[j] = nv;
+            Q.rai[j] = nai;
+            Q.rbounce[j] = nbounce;
+        }
+        __syncwarp();
+        if (lane == 0) Q.pool_n = pbase + __popc(pm);
+        __syncwarp();
+    }
+    if (A.stats) {
+        n_prim = __reduce_add_sync(0xffffffffu, n_prim);
+        n_sec = __reduce_add_sync(0xffffffffu, n_sec);
+        n_shadow = __reduce_add_sync(0xffffffffu, n_shadow);
+        n_hits = __reduce_add_sync(0xffffffffu, n_hits);
+        if (lane == 0) {
+            atomicAdd((unsigned long long*)&A.stats->primary_rays, (unsigned long long)n_prim);
+            atomicAdd((unsigned long long*)&A.stats->secondary_rays, (unsigned long long)n_sec);
+            atomicAdd((unsigned long long*)&A.stats->shadow_rays, (unsigned long long)n_shadow);
+            atomicAdd((unsigned long long*)&A.stats->hits, (unsigned long long)n_hits);
+        }
+    }
+}
+
+// RGBA8 of the pooled sums: pixel i of the launch belongs to view v and goes
+// to rgba[v.rgba_offset + i - pix_off[v]].
+__global__ void k_batch_fb(BatchRenderArgs A) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= A.total) return;
+    const int v = find_segment(A.pix_off, A.count, i);
+    uchar4 o;
+    o.x = to_unorm8(A.accum[3 * (size_t)i], A.inv1e6);
+    o.y = to_unorm8(A.accum[3 * (size_t)i + 1], A.inv1e6);
+    o.z = to_unorm8(A.accum[3 * (size_t)i + 2], A.inv1e6);
+    o.w = 255;
+    reinterpret_cast<uchar4*>(A.rgba)[(size_t)A.views[v].rgba_offset + (i - A.pix_off[v])] = o;
+}
+
 struct BatchRenderVariant {
     int threads, min_blocks;
     void (*fn)(BatchRenderArgs);
+    bool pooled;
 };
+// Variant 0 serves the request loop (many short launches, where the unpooled
+// kernel measured faster); rt_batch takes the first pooled one (one large
+// launch, where the pool keeps lanes busy).
 static const BatchRenderVariant kBatchVariants[] = {
-    {128, 8, k_render_batch<128, 8>},
-    {256, 4, k_render_batch<256, 4>},
-    {128, 6, k_render_batch<128, 6>},
+    {128, 8, k_render_batch<128, 8>, false},
+    {128, 6, k_render_batch_pool<128, 6>, true},
+    {256, 4, k_render_batch<256, 4>, false},
+    {128, 6, k_render_batch<128, 6>, false},
+    {128, 8, k_render_batch_pool<128, 8>, true},
 };
 
 int batch_render_variant_count() { return (int)(sizeof(kBatchVariants) / sizeof(kBatchVariants[0])); }
@@ -343,8 +561,20 @@ int batch_render_variant_info(int v, int* threads, const void** fn) {
     return 0;
 }
 
+bool batch_render_variant_pooled(int v) {
+    return v >= 0 && v < batch_render_variant_count() && kBatchVariants[v].pooled;
+}
+
 cudaError_t launch_batch_render(const BatchRenderArgs& a, int variant, int grid, cudaStream_t s) {
+    if (variant < 0 || variant >= batch_render_variant_count()) return cudaErrorInvalidValue;
+    const bool pooled = kBatchVariants[variant].pooled;
+    if (pooled) {
+        if (!a.accum) return cudaErrorInvalidValue;
+        cudaError_t e = cudaMemsetAsync(a.accum, 0, 3 * sizeof(uint32_t) * (size_t)a.total, s);
+        if (e != cudaSuccess) return e;
+    }
     kBatchVariants[variant].fn<<<grid, kBatchVariants[variant].threads, 0, s>>>(a);
+    if (pooled && a.total) k_batch_fb<<<(a.total + 255) / 256, 256, 0, s>>>(a);
     return cudaGetLastError();
 }
 

@@ -68,6 +68,8 @@ struct BatchRenderArgs {
     uint32_t* status;
     int chunk;
     float inv1e6;
+    uint32_t* accum;            // pooled variants: 3 sums per pixel of the launch
+    uint32_t total;             // pixels of the launch (pix_off[count])
 };
 
 const void* batch_build_kernel();
@@ -77,6 +79,8 @@ int sort_tile_size();
 cudaError_t launch_batch_build(const BatchBuildArgs& a, int grid, cudaStream_t s);
 int batch_render_variant_count();
 int batch_render_variant_info(int v, int* threads, const void** fn);
+// True for variants that sum into BatchRenderArgs::accum before RGBA8.
+bool batch_render_variant_pooled(int v);
 cudaError_t launch_batch_render(const BatchRenderArgs& a, int variant, int grid, cudaStream_t s);
 
 }  // namespace rt

@@ -39,6 +39,7 @@ struct rt_batch {
     std::vector<size_t> scratch_at;         // word offset of each scene's scratch
     rt::BatchView* d_views = nullptr;
     uint32_t* d_pix_off = nullptr;
+    uint32_t* d_accum = nullptr;            // render sums, 3 per pixel (pooled render)
     rt_lights* d_lights = nullptr;          // one per distinct scene
     int build_grid = 0;
     int render_variant = 0, render_grid = 0, render_chunk = 32;
@@ -64,6 +65,7 @@ void free_tables(rt_batch* b) {
     dfree(b->d_scratch);
     dfree(b->d_views);
     dfree(b->d_pix_off);
+    dfree(b->d_accum);
     dfree(b->d_lights);
     dfree(b->d_stage);
     if (b->exec) cudaGraphExecDestroy(b->exec);
@@ -165,6 +167,8 @@ rt::BatchRenderArgs render_args(rt_ctx* c, rt_batch* b, uint8_t* rgba, rt_render
     a.status = c->d_status;
     a.chunk = b->render_chunk;
     a.inv1e6 = c->inv1e6;
+    a.accum = b->d_accum;
+    a.total = b->total_pixels;
     return a;
 }
 
@@ -258,6 +262,7 @@ int32_t rt_batch_set(rt_ctx* c, rt_batch* b, const rt_batch_view* views, int32_t
         cudaMalloc(&b->d_ctr, 4 * 8) || cudaMalloc(&b->d_scratch, 4 * words) ||
         cudaMalloc(&b->d_views, sizeof(rt::BatchView) * count) ||
         cudaMalloc(&b->d_pix_off, 4 * (count + 1)) ||
+        cudaMalloc(&b->d_accum, 3 * sizeof(uint32_t) * std::max<size_t>(1, poff.back())) ||
         cudaMalloc(&b->d_lights, sizeof(rt_lights) * ns) ||
         cudaMalloc(&b->d_stage, sizeof(unsigned long long) * 8)) {
         cudaGetLastError();
@@ -278,11 +283,17 @@ int32_t rt_batch_set(rt_ctx* c, rt_batch* b, const rt_batch_view* views, int32_t
                                                      rt::batch_build_threads(), 0));
     if (bps < 1) return fail(RT_ERR_CUDA, "rt_batch_set: build kernel cannot be resident");
     b->build_grid = bps * c->num_sms;
-    // render: the context's tuned block shape when it matches a batch variant
+    // render: the pooled many-view kernel (one large launch keeps its lanes
+    // busy by pooling reflection rays across views)
     int threads = 0;
     const void* fn = nullptr;
     b->render_variant = 0;
-    rt::batch_render_variant_info(0, &threads, &fn);
+    for (int v = 0; v < rt::batch_render_variant_count(); ++v)
+        if (rt::batch_render_variant_pooled(v)) {
+            b->render_variant = v;
+            break;
+        }
+    rt::batch_render_variant_info(b->render_variant, &threads, &fn);
     int rbps = 0;
     CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&rbps, fn, threads, 0));
     b->render_grid = std::max(1, rbps) * c->num_sms;

@@ -443,7 +443,7 @@ bool launch_renders(rt_server* S) {
         const uint64_t need = (launch_px + S->render_threads - 1) / S->render_threads;
         // while an upload builds, two block slots per SM stay free for its
         // kernels: a persistent launch would otherwise hold every SM until
-        // it ends and the build's nine kernels would each wait for a gap
+        // it ends and each of the build's kernels would wait for a gap
         bool building = false;
         for (auto& kv : S->scenes) building |= kv.second.admitted && !kv.second.ready;
         const int cap = building && S->render_bps > 2
