@@ -507,15 +507,23 @@ def run_gpu(args):
     render_gbs = render_bytes / (med_render * 1e-3) / 1e9
     build_bytes = n_tris * B_BUILD_PER_TRI
     build_gbs = build_bytes / (med_build * 1e-3) / 1e9
-    roofline = {"kernel": "k_render (fused trace + shadow + shade + reflect)", "bound": "hbm",
+    pooled = ctx.variant_pooled(tuned.variant)
+    roofline = {"kernel": ("k_render_pool (pooled trace + shadow + shade + reflect)" if pooled
+                           else "k_render (fused trace + shadow + shade + reflect)"), "bound": "hbm",
                 "achieved": render_gbs, "peak": peak, "unit": "GB/s",
                 "frac": render_gbs / peak, "traffic": None,
                 "peak_kind": peak_kind,
                 "algorithmic_bytes_per_launch": render_bytes,
                 "note": "traversal is latency/L2-bound; algorithmic bytes = 88 B per traced "
                         "ray + 25 B per shadow ray"}
+    # the emit's levels: 512 triangles per level-0 block, then 8 blocks per block
+    emit_levels, nb = 1, (n_tris + 511) // 512
+    while nb > 1:
+        nb, emit_levels = (nb + 7) // 8, emit_levels + 1
+    launches_per_frame = 7 + emit_levels + (2 if pooled else 1)
     build_roofline = {"kernels": "k_bounds + k_morton_hist + 4x k_onesweep + k_permute + "
-                                 "k_emit_refit", "bound": "hbm", "achieved": build_gbs,
+                                 "%dx k_emit_level" % emit_levels, "bound": "hbm",
+                      "achieved": build_gbs,
                       "peak": peak, "unit": "GB/s", "frac": build_gbs / peak,
                       "bytes_per_tri": B_BUILD_PER_TRI, "peak_kind": peak_kind,
                       "ms": med_build, "lbvh_mtri_s": n_tris / (med_build * 1e-3) / 1e6}
@@ -564,7 +572,7 @@ def run_gpu(args):
                    "h2d_bytes_per_step": 2 * 16 * V,
                    "d2h_bytes_per_step": 4 * w * h + 32,
                    "ms_per_step": e2e_total / args.steps},
-           "gpu_launches": 9 * args.steps,
+           "gpu_launches": launches_per_frame * args.steps,
            "render_config": {"variant": tuned.variant, "threads": ctx.variants()[tuned.variant][0],
                              "min_blocks_per_sm": ctx.variants()[tuned.variant][1],
                              "blocks_per_sm": tuned.blocks_per_sm, "chunk": tuned.chunk,

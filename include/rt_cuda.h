@@ -321,6 +321,10 @@ RT_API int32_t rt_render_variants(int32_t* count);
  * blocks per SM the occupancy calculator allows on this context's GPU. */
 RT_API int32_t rt_render_variant_info(rt_ctx* ctx, int32_t variant, int32_t* threads,
                                       int32_t* min_blocks, int32_t* occupancy_blocks);
+/* *pooled = 1 for the variants that pool shadow and reflection rays per warp
+ * and sum per pixel before writing RGBA8 (two kernels per render), 0 for the
+ * one-path-per-lane variants.  Same image either way. */
+RT_API int32_t rt_render_variant_pooled(int32_t variant, int32_t* pooled);
 RT_API int32_t rt_set_render_config(rt_ctx* ctx, const rt_render_config* cfg);
 RT_API int32_t rt_get_render_config(rt_ctx* ctx, rt_render_config* cfg);
 /* Times every variant x resident-block count x chunk on this scene and

@@ -833,6 +833,14 @@ int32_t rt_render_variant_info(rt_ctx* c, int32_t v, int32_t* threads, int32_t* 
     return RT_OK;
 }
 
+int32_t rt_render_variant_pooled(int32_t v, int32_t* pooled) {
+    if (!pooled) return fail(RT_ERR_INVALID, "rt_render_variant_pooled: null argument");
+    if (v < 0 || v >= rt::render_variant_count())
+        return fail(RT_ERR_INVALID, "rt_render_variant_pooled: no variant %d", v);
+    *pooled = rt::render_variant_pooled(v) ? 1 : 0;
+    return RT_OK;
+}
+
 int32_t rt_set_render_config(rt_ctx* c, const rt_render_config* cfg) {
     if (!c || !cfg) return fail(RT_ERR_INVALID, "rt_set_render_config: null argument");
     if (!valid_cfg(*cfg)) return fail(RT_ERR_INVALID, "rt_set_render_config: invalid configuration");

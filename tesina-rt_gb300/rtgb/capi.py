@@ -58,6 +58,7 @@ SIGNATURES = {
     "rt_sort_pairs_noalloc": (I32, [P, P, P, P, P, U32, I32, P]),
     "rt_render_variants": (I32, [C.POINTER(I32)]),
     "rt_render_variant_info": (I32, [P, I32, C.POINTER(I32), C.POINTER(I32), C.POINTER(I32)]),
+    "rt_render_variant_pooled": (I32, [I32, C.POINTER(I32)]),
     "rt_set_render_config": (I32, [P, P]),
     "rt_get_render_config": (I32, [P, P]),
     "rt_autotune_render": (I32, [P, P, P, I32, I32, I32, I32, P, C.POINTER(F)]),
@@ -184,6 +185,11 @@ class Context:
                                                             C.byref(o)))
             out.append((t.value, m.value, o.value))
         return out
+
+    def variant_pooled(self, v):
+        p = I32(0)
+        check(self.lib, self.lib.rt_render_variant_pooled(v, C.byref(p)))
+        return bool(p.value)
 
     def fb_copy(self, img_buf, rgba_buf, pixels, stream=None):
         check(self.lib, self.lib.rt_fb_copy(self.h, img_buf.ptr, rgba_buf.ptr, pixels, stream))
