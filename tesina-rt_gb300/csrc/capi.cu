@@ -133,6 +133,81 @@ int32_t check_lights(const rt_lights* L) {
 
 cudaStream_t st(rt_ctx* c, rt_stream s) { return s ? (cudaStream_t)s : c->stream; }
 
+// Calls on one scene behave as on one in-order queue, whatever streams they
+// name (the reference runs every call on one command queue): a call that
+// writes the scene (upload, vertex update, build, refit) waits on the device
+// for every earlier call on other streams, a call that reads it (trace,
+// shade, render, ...) for the last writing call, and host reads of the scene
+// for its last writing call.  Reading calls on several streams may overlap.
+static cudaError_t order_event(cudaEvent_t* e) {
+    return *e ? cudaSuccess : cudaEventCreateWithFlags(e, cudaEventDisableTiming);
+}
+
+cudaError_t scene_write_begin(rt_scene* s, cudaStream_t cs) {
+    if (s->write_recorded && s->write_stream != cs) {
+        const cudaError_t e = cudaStreamWaitEvent(cs, s->ev_write, 0);
+        if (e != cudaSuccess) return e;
+    }
+    for (int i = 0; i < s->n_readers; ++i)
+        if (s->readers[i].stream != cs) {
+            const cudaError_t e = cudaStreamWaitEvent(cs, s->readers[i].ev, 0);
+            if (e != cudaSuccess) return e;
+        }
+    s->n_readers = 0;
+    return cudaSuccess;
+}
+
+cudaError_t scene_write_end(rt_scene* s, cudaStream_t cs) {
+    cudaError_t e = order_event(&s->ev_write);
+    if (e == cudaSuccess) e = cudaEventRecord(s->ev_write, cs);
+    if (e != cudaSuccess) return e;
+    s->write_stream = cs;
+    s->write_recorded = true;
+    return cudaSuccess;
+}
+
+cudaError_t scene_read_begin(rt_scene* s, cudaStream_t cs) {
+    if (s->write_recorded && s->write_stream != cs) return cudaStreamWaitEvent(cs, s->ev_write, 0);
+    return cudaSuccess;
+}
+
+cudaError_t scene_read_end(rt_scene* s, cudaStream_t cs) {
+    int k = 0;
+    while (k < s->n_readers && s->readers[k].stream != cs) ++k;
+    if (k == s->n_readers) {
+        if (k < 4) {
+            s->readers[k].stream = cs;
+            s->n_readers = k + 1;
+        } else {   // the last slot: cs takes over the work it covered
+            k = 3;
+            const cudaError_t e = cudaStreamWaitEvent(cs, s->readers[k].ev, 0);
+            if (e != cudaSuccess) return e;
+            s->readers[k].stream = cs;
+        }
+    }
+    const cudaError_t e = order_event(&s->readers[k].ev);
+    return e == cudaSuccess ? cudaEventRecord(s->readers[k].ev, cs) : e;
+}
+
+// Host side: waits for every call on the scene (reads too, when `all`).
+cudaError_t scene_host_wait(rt_scene* s, bool all) {
+    if (s->write_recorded) {
+        const cudaError_t e = cudaEventSynchronize(s->ev_write);
+        if (e != cudaSuccess) return e;
+    }
+    for (int i = 0; all && i < s->n_readers; ++i) {
+        const cudaError_t e = cudaEventSynchronize(s->readers[i].ev);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+static void destroy_order_events(rt_scene* s) {
+    if (s->ev_write) cudaEventDestroy(s->ev_write);
+    for (auto& r : s->readers)
+        if (r.ev) cudaEventDestroy(r.ev);
+}
+
 }  // namespace
 
 namespace rt {
@@ -196,27 +271,38 @@ void release_work_counter(rt_ctx* c, cudaStream_t s) {
         cudaFree(it->second);
         c->work_by_stream.erase(it);
     }
-    auto ia = c->accum_by_stream.find(s);
-    if (ia != c->accum_by_stream.end()) {
-        if (ia->second.first) cudaFreeAsync(ia->second.first, s);
-        c->accum_by_stream.erase(ia);
+    for (auto* m : {&c->accum_by_stream, &c->sec_by_stream}) {
+        auto ia = m->find(s);
+        if (ia != m->end()) {
+            if (ia->second.first) cudaFreeAsync(ia->second.first, s);
+            m->erase(ia);
+        }
     }
 }
 
-uint32_t* accum_buffer(rt_ctx* c, cudaStream_t s, size_t pixels) {
+// The buffer of stream s in `m`, at least `size` units of `unit` bytes.
+static uint32_t* stream_buffer(rt_ctx* c, std::map<cudaStream_t, std::pair<uint32_t*, size_t>>& m,
+                               cudaStream_t s, size_t size, size_t unit) {
     std::lock_guard<std::mutex> lk(c->work_mu);
-    auto& e = c->accum_by_stream[s];
-    if (e.first && e.second >= pixels) return e.first;
+    auto& e = m[s];
+    if (e.first && e.second >= size) return e.first;
     if (e.first) cudaFreeAsync(e.first, s);
     e = {nullptr, 0};
     uint32_t* p = nullptr;
-    if (cudaMallocAsync(reinterpret_cast<void**>(&p), 3 * sizeof(uint32_t) * (pixels ? pixels : 1),
-                        s) != cudaSuccess) {
+    if (cudaMallocAsync(reinterpret_cast<void**>(&p), unit * (size ? size : 1), s) != cudaSuccess) {
         cudaGetLastError();
         return nullptr;
     }
-    e = {p, pixels};
+    e = {p, size};
     return p;
+}
+
+uint32_t* accum_buffer(rt_ctx* c, cudaStream_t s, size_t pixels) {
+    return stream_buffer(c, c->accum_by_stream, s, pixels, 3 * sizeof(uint32_t));
+}
+
+uint32_t* sec_scratch(rt_ctx* c, cudaStream_t s, size_t bytes) {
+    return stream_buffer(c, c->sec_by_stream, s, bytes, 1);
 }
 
 }  // namespace rt
@@ -301,9 +387,9 @@ int32_t rt_shutdown(rt_ctx* c) {
     dfree(c->d_status);
     dfree(c->d_work);
     for (auto& kv : c->work_by_stream) dfree(kv.second);
-    for (auto& kv : c->accum_by_stream)
-        if (kv.second.first) cudaFree(kv.second.first);
-    dfree(c->d_sec_scratch);
+    for (auto* m : {&c->accum_by_stream, &c->sec_by_stream})
+        for (auto& kv : *m)
+            if (kv.second.first) cudaFree(kv.second.first);
     dfree(c->d_out);
     dfree(c->d_stats);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -398,9 +484,13 @@ int32_t rt_scene_create(rt_ctx* c, rt_scene** out) {
 int32_t rt_scene_destroy(rt_ctx* c, rt_scene* s) {
     if (!s) return RT_OK;
     // pool-allocated buffers are freed in order on the pool stream instead
-    if (c && !s->pool) cudaStreamSynchronize(c->stream);
+    if (c && !s->pool) {
+        scene_host_wait(s, true);
+        cudaStreamSynchronize(c->stream);
+    }
     free_build(s);
     free_geometry(s);
+    destroy_order_events(s);
     if (s->ev0) cudaEventDestroy(s->ev0);
     if (s->ev1) cudaEventDestroy(s->ev1);
     delete s;
@@ -437,6 +527,7 @@ int32_t rt_scene_upload(rt_ctx* c, rt_scene* s, const rt_scene_desc* d, rt_strea
     }
     CU(cudaSetDevice(c->device));
     cudaStream_t cs = st(c, stream);
+    CU(scene_write_begin(s, cs));
     CU(cudaStreamSynchronize(cs));
     if (s->capV < V || s->capN < N || s->capM < M) {
         free_geometry(s);
@@ -488,6 +579,7 @@ int32_t rt_scene_upload(rt_ctx* c, rt_scene* s, const rt_scene_desc* d, rt_strea
     }
     s->lights = d->lights;
     s->built = false;
+    CU(scene_write_end(s, cs));
     return RT_OK;
 }
 
@@ -496,8 +588,10 @@ int32_t rt_scene_update_vertices(rt_ctx* c, rt_scene* s, const float* pos4, cons
     if (!c || !s || !pos4) return fail(RT_ERR_INVALID, "rt_scene_update_vertices: null argument");
     if (V != s->V) return fail(RT_ERR_INVALID, "vertex count %u != scene's %u", V, s->V);
     cudaStream_t cs = st(c, stream);
+    CU(scene_write_begin(s, cs));
     CU(cudaMemcpyAsync(s->d_pos, pos4, 16 * (size_t)V, cudaMemcpyHostToDevice, cs));
     if (nrm4) CU(cudaMemcpyAsync(s->d_nrm, nrm4, 16 * (size_t)V, cudaMemcpyHostToDevice, cs));
+    CU(scene_write_end(s, cs));
     return RT_OK;
 }
 
@@ -506,8 +600,10 @@ int32_t rt_scene_update_vertices_device(rt_ctx* c, rt_scene* s, const float* pos
     if (!c || !s || !pos4) return fail(RT_ERR_INVALID, "rt_scene_update_vertices: null argument");
     if (V != s->V) return fail(RT_ERR_INVALID, "vertex count %u != scene's %u", V, s->V);
     cudaStream_t cs = st(c, stream);
+    CU(scene_write_begin(s, cs));
     CU(cudaMemcpyAsync(s->d_pos, pos4, 16 * (size_t)V, cudaMemcpyDeviceToDevice, cs));
     if (nrm4) CU(cudaMemcpyAsync(s->d_nrm, nrm4, 16 * (size_t)V, cudaMemcpyDeviceToDevice, cs));
+    CU(scene_write_end(s, cs));
     return RT_OK;
 }
 
@@ -534,6 +630,7 @@ int32_t rt_scene_read_sort(rt_ctx* c, rt_scene* s, uint32_t* keys, uint32_t* per
                            uint32_t* sorted) {
     if (!c || !s) return fail(RT_ERR_INVALID, "rt_scene_read_sort: null argument");
     if (!s->built) return fail(RT_ERR_NOT_BUILT, "rt_scene_read_sort: no BVH built");
+    CU(scene_host_wait(s, false));
     CU(cudaStreamSynchronize(c->stream));
     const size_t b = 4 * (size_t)s->N;
     if (keys) CU(cudaMemcpy(keys, s->d_keys_unsorted, b, cudaMemcpyDeviceToHost));
@@ -544,6 +641,7 @@ int32_t rt_scene_read_sort(rt_ctx* c, rt_scene* s, uint32_t* keys, uint32_t* per
 
 int32_t rt_scene_read_orig(rt_ctx* c, rt_scene* s, uint32_t* orig) {
     if (!c || !s || !orig) return fail(RT_ERR_INVALID, "rt_scene_read_orig: null argument");
+    CU(scene_host_wait(s, false));
     CU(cudaStreamSynchronize(c->stream));
     CU(cudaMemcpy(orig, s->d_orig[s->cur], 4 * (size_t)s->N, cudaMemcpyDeviceToHost));
     return RT_OK;
@@ -596,10 +694,12 @@ int32_t rt_bvh_build_lbvh(rt_ctx* c, rt_scene* s, const rt_bvh_cfg* cfg, rt_stre
     int32_t r = rt::scene_ensure_build(s);
     if (r) return r;
     cudaStream_t cs = st(c, stream);
+    CU(scene_write_begin(s, cs));
     CU(cudaEventRecord(s->ev0, cs));
     rt::LbvhArgs a = lbvh_args(c, s);
     CU(rt::lbvh_build(a, cs));
     CU(cudaEventRecord(s->ev1, cs));
+    CU(scene_write_end(s, cs));
     s->cur ^= 1;   // the sorted index buffer / material map are now current
     s->built = true;
     return RT_OK;
@@ -609,11 +709,13 @@ int32_t rt_bvh_refit_lbvh(rt_ctx* c, rt_scene* s, rt_stream stream) {
     if (!c || !s) return fail(RT_ERR_INVALID, "rt_bvh_refit_lbvh: null argument");
     if (!s->built) return fail(RT_ERR_NOT_BUILT, "rt_bvh_refit_lbvh: no BVH built");
     cudaStream_t cs = st(c, stream);
+    CU(scene_write_begin(s, cs));
     CU(cudaEventRecord(s->ev0, cs));
     rt::LbvhArgs a = lbvh_args(c, s);
     a.idx_out = s->d_idx[s->cur];   // refit keeps the current (sorted) order
     CU(rt::lbvh_refit(a, cs));
     CU(cudaEventRecord(s->ev1, cs));
+    CU(scene_write_end(s, cs));
     return RT_OK;
 }
 
@@ -627,6 +729,7 @@ int32_t rt_bvh_last_time_ms(rt_ctx* c, rt_scene* s, float* ms) {
 int32_t rt_bvh_export(rt_ctx* c, rt_scene* s, rt_canon_node* out, uint32_t cap, uint32_t* count) {
     if (!c || !s || !count) return fail(RT_ERR_INVALID, "rt_bvh_export: null argument");
     if (!s->built) return fail(RT_ERR_NOT_BUILT, "rt_bvh_export: no BVH built");
+    CU(scene_host_wait(s, false));
     CU(cudaStreamSynchronize(c->stream));
     rt::BvhHeader h;
     CU(cudaMemcpy(&h, s->d_hdr, sizeof(h), cudaMemcpyDeviceToHost));
@@ -723,7 +826,10 @@ int32_t rt_trace(rt_ctx* c, rt_scene* s, const rt_sample* smp, int32_t n, rt_hit
     if (!c || !smp || !hits) return fail(RT_ERR_INVALID, "rt_trace: null argument");
     int32_t r = need_built(s, "rt_trace");
     if (r) return r;
-    CU(rt::launch_trace(view_of(s), smp, n, hits, c->d_status, st(c, stream)));
+    cudaStream_t cs = st(c, stream);
+    CU(scene_read_begin(s, cs));
+    CU(rt::launch_trace(view_of(s), smp, n, hits, c->d_status, cs));
+    CU(scene_read_end(s, cs));
     return RT_OK;
 }
 
@@ -734,7 +840,10 @@ int32_t rt_shadow_trace(rt_ctx* c, rt_scene* s, const rt_sample* smp, int32_t n,
     if (!c || !hits) return fail(RT_ERR_INVALID, "rt_shadow_trace: null argument");
     int32_t r = need_built(s, "rt_shadow_trace");
     if (r) return r;
-    CU(rt::launch_shadow(view_of(s), s->lights, n, hits, c->d_status, st(c, stream)));
+    cudaStream_t cs = st(c, stream);
+    CU(scene_read_begin(s, cs));
+    CU(rt::launch_shadow(view_of(s), s->lights, n, hits, c->d_status, cs));
+    CU(scene_read_end(s, cs));
     return RT_OK;
 }
 
@@ -744,7 +853,10 @@ int32_t rt_shade(rt_ctx* c, rt_scene* s, const rt_sample* smp, const rt_hit* hit
     if (!c || !smp || !hits || !img) return fail(RT_ERR_INVALID, "rt_shade: null argument");
     int32_t r = need_built(s, "rt_shade");
     if (r) return r;
-    CU(rt::launch_shade(view_of(s), s->lights, smp, hits, n, img, st(c, stream)));
+    cudaStream_t cs = st(c, stream);
+    CU(scene_read_begin(s, cs));
+    CU(rt::launch_shade(view_of(s), s->lights, smp, hits, n, img, cs));
+    CU(scene_read_end(s, cs));
     return RT_OK;
 }
 
@@ -755,18 +867,12 @@ int32_t rt_gen_secondary(rt_ctx* c, rt_scene* s, const rt_sample* in, int32_t n,
         return fail(RT_ERR_INVALID, "rt_gen_secondary: null argument");
     int32_t r = need_built(s, "rt_gen_secondary");
     if (r) return r;
-    const size_t need = rt::gen_secondary_scratch_bytes(n);
-    if (c->sec_scratch_bytes < need) {
-        dfree(c->d_sec_scratch);
-        if (cudaMalloc(&c->d_sec_scratch, need)) {
-            cudaGetLastError();
-            c->sec_scratch_bytes = 0;
-            return fail(RT_ERR_OOM, "rt_gen_secondary: scratch allocation failed");
-        }
-        c->sec_scratch_bytes = need;
-    }
     cudaStream_t cs = st(c, stream);
-    CU(rt::launch_gen_secondary(view_of(s), in, n, hits, out, max_out, d_count, c->d_sec_scratch, cs));
+    uint32_t* scratch = rt::sec_scratch(c, cs, rt::gen_secondary_scratch_bytes(n));
+    if (!scratch) return fail(RT_ERR_OOM, "rt_gen_secondary: scratch allocation failed");
+    CU(scene_read_begin(s, cs));
+    CU(rt::launch_gen_secondary(view_of(s), in, n, hits, out, max_out, d_count, scratch, cs));
+    CU(scene_read_end(s, cs));
     if (h_count) {
         CU(cudaMemcpyAsync(h_count, d_count, sizeof(int32_t), cudaMemcpyDeviceToHost, cs));
         CU(cudaStreamSynchronize(cs));
@@ -881,7 +987,9 @@ int32_t rt_render(rt_ctx* c, rt_scene* s, const rt_camera* cam, int32_t w, int32
     a.stats = stats;
     a.work_counter = work;
     a.status = c->d_status;
+    CU(scene_read_begin(s, cs));
     CU(launch_render_cfg(c, a, c->render_cfg, cs));
+    CU(scene_read_end(s, cs));
     return RT_OK;
 }
 
@@ -914,6 +1022,7 @@ int32_t rt_autotune_render(rt_ctx* c, rt_scene* s, const rt_camera* cam, int32_t
         return RT_OK;
     }
     cudaStream_t cs = c->stream;
+    CU(scene_read_begin(s, cs));
     uint8_t* rgba = nullptr;
     CU(cudaMalloc(&rgba, 4 * (size_t)w * h));
     cudaEvent_t e0, e1;
@@ -970,6 +1079,7 @@ int32_t rt_autotune_render(rt_ctx* c, rt_scene* s, const rt_camera* cam, int32_t
     cudaEventDestroy(e1);
     cudaFree(rgba);
     CU(cudaGetLastError());
+    CU(scene_read_end(s, cs));
     c->render_cfg = bestc;
     c->tuned[key] = bestc;
     if (best) *best = bestc;

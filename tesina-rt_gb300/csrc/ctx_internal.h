@@ -25,8 +25,9 @@ struct rt_ctx {
     // pixel count each holds (stream-ordered allocations)
     std::map<cudaStream_t, std::pair<uint32_t*, size_t>> accum_by_stream;
     std::mutex work_mu;
-    uint32_t* d_sec_scratch = nullptr;   // rt_gen_secondary block offsets
-    size_t sec_scratch_bytes = 0;
+    // rt_gen_secondary block offsets, per stream, with their size in bytes
+    // (stream-ordered allocations)
+    std::map<cudaStream_t, std::pair<uint32_t*, size_t>> sec_by_stream;
     uint8_t* d_out = nullptr;            // rt_render_host image staging
     size_t d_out_cap = 0;
     rt_render_stats* d_stats = nullptr;  // rt_render_host counters
@@ -69,6 +70,18 @@ struct rt_scene {
     bool built = false;
     int depth = 30, min_leaf = 1;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // Order of the rt_* calls on this scene across streams: the completion
+    // of the last call that wrote it, and of the reading calls since, one
+    // event per stream (the last slot absorbs further streams).
+    struct Reader {
+        cudaStream_t stream;
+        cudaEvent_t ev;
+    };
+    cudaEvent_t ev_write = nullptr;
+    cudaStream_t write_stream = nullptr;
+    bool write_recorded = false;
+    Reader readers[4] = {};
+    int n_readers = 0;
     // stream-ordered allocation (served scenes): buffers come from `pool` in
     // the order of `pool_stream`; nullptr = cudaMalloc
     cudaMemPool_t pool = nullptr;
@@ -94,4 +107,7 @@ void release_work_counter(rt_ctx* c, cudaStream_t s);
 // Render sums (3 x uint32 per pixel) for launches on stream s, at least
 // `pixels` long; grown in stream order.  nullptr if it cannot be allocated.
 uint32_t* accum_buffer(rt_ctx* c, cudaStream_t s, size_t pixels);
+// rt_gen_secondary scratch for launches on stream s, at least `bytes` long;
+// grown in stream order.  nullptr if it cannot be allocated.
+uint32_t* sec_scratch(rt_ctx* c, cudaStream_t s, size_t bytes);
 }  // namespace rt

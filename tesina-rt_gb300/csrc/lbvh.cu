@@ -158,7 +158,7 @@ constexpr int EMIT_C1 = EMIT_GROUP * EMIT_FMAX;    // items per block above leve
 
 // One level of the emit (emit_level), one block per run of items.
 template <int C>
-__global__ void __launch_bounds__(C) k_emit_level(
+__global__ void __launch_bounds__(C, 1024 / C) k_emit_level(
     uint32_t n, const uint32_t* __restrict__ skeys, const float4* __restrict__ leafbox,
     const EmitItem* __restrict__ in, const uint32_t* __restrict__ in_count, uint32_t n_in,
     EmitItem* __restrict__ out, uint32_t* __restrict__ out_count, float4* __restrict__ nodes,

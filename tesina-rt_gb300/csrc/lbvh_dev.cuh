@@ -386,20 +386,18 @@ __device__ __forceinline__ void emit_climb(uint32_t i, uint32_t n,
 // Multi-level emit + refit, warp-synchronous.  The tree is built bottom-up
 // in a few launches ("levels").  Within a block, runs of consecutive items
 // are joined by warps: a warp holds up to 32 consecutive items, one per lane
-// (at level 0 the items are the sorted triangles).  Each lane owns the run
-// of items that starts at it; in a round, a run that is a left child (its
-// parent's split is its right boundary) takes over the run that starts at
-// the next lane if that run is the matching right child, writes the 64-byte
-// node (left half its own, right half the sibling's, shuffled across) and
-// carries on with the merged box; the absorbed lane drops out.  No shared
-// memory, barrier or fence is involved.  A run whose parent lies outside the
-// warp's items is left over; the block gathers the leftovers of its warps in
-// order and joins them again, at most 32 per warp, until one warp holds them
-// all or no node inside the block is left.  What is left then has its parent
-// outside the block and becomes an item of the next level, which gathers the items of EMIT_GROUP blocks, until one
-// block reaches the root.  A block leaves at most EMIT_FMAX items: they hang
-// off the chains of nodes crossing its two ends, each at most 64 deep (32
-// key bits + 32 index bits).
+// (at level 0 the items are the sorted triangles).  warp_join writes in one
+// step every node whose range lies inside the warp's items: the levels of
+// the boundaries between items, as seven ballots, give each node's range and
+// parent, and sparse tables in shared memory give its children's boxes.  A
+// run whose parent lies outside the warp's items is left over; the block
+// gathers the leftovers of its warps in order and joins them again, at most
+// 32 per warp, until one warp holds them all or no node inside the block is
+// left.  What is left then has its parent outside the block and becomes an
+// item of the next level, which gathers the items of EMIT_GROUP blocks,
+// until one block reaches the root.  A block leaves at most EMIT_FMAX items:
+// they hang off the chains of nodes crossing its two ends, each at most 64
+// deep (32 key bits + 32 index bits).
 //
 // The tree is the one of emit_climb.  With d[j] the augmented delta of the
 // boundary before item j of a chunk and d[c] the boundary after its last
@@ -450,95 +448,244 @@ __device__ __forceinline__ void reg_to_item(const WarpItem& w, EmitItem& e) {
     e.ref = w.ref; e.cnt = w.cnt; e.db = w.db;
 }
 
-// Joins the items of lanes 0..cnt-1 of the warp (all 32 lanes call it) whose
-// parents lie inside these items; `edge` is the boundary after the last item.
-// Returns true for a lane that still holds a run afterwards (its parent is
-// outside).  A run that reaches [0, n-1] writes the header instead.
+// Shared scratch of one warp for warp_join, 2048 bytes: the space of the 32
+// list items the warp's chunk takes.  st is a sparse table of one axis of
+// the items' boxes (level t at start i: min / max over items i .. i+2^t-1);
+// the arrays hold the items' ranges, end keys and references.  At the end
+// the first 1536 bytes hand the runs left over to the lanes they start at.
+struct __align__(16) WarpScratch {
+    float2 st[5][32];
+    uint32_t il[32], ir[32], ikl[32], ikr[32];
+    int32_t iref[32], icnt[32];
+};
+static_assert(sizeof(WarpScratch) == 32 * sizeof(EmitItem), "scratch aliases 32 items");
+
+// Level of a boundary delta: its highest set bit (the radix tree's level),
+// 64 for the virtual boundaries before the first and after the last
+// triangle.  Two boundaries of one level always have a higher one between
+// them, so the nearest boundary above another one is the same by level as
+// by delta, and levels order every pair of boundaries the tree compares.
+__device__ __forceinline__ uint32_t delta_level(uint64_t x) {
+    return x == ~0ull ? 64u : 63u - (uint32_t)__clzll(x);
+}
+
+// Lanes of `valid` whose level (bit planes P, most significant last) is
+// above L.
+__device__ __forceinline__ uint32_t levels_above(uint32_t L, const uint32_t P[7], uint32_t valid) {
+    uint32_t gt = 0u, eq = valid;
+#pragma unroll
+    for (int t = 6; t >= 0; --t) {
+        if ((L >> t) & 1u) {
+            eq &= P[t];
+        } else {
+            gt |= eq & P[t];
+            eq &= ~P[t];
+        }
+    }
+    return gt;
+}
+
+__device__ __forceinline__ uint32_t level_at(uint32_t k, const uint32_t P[7]) {
+    uint32_t L = 0u;
+#pragma unroll
+    for (int t = 0; t < 7; ++t) L |= ((P[t] >> k) & 1u) << t;
+    return L;
+}
+
+// The lane of the highest boundary in the non-empty mask m (unique: two of
+// one level have a higher one between them).
+__device__ __forceinline__ uint32_t top_level(uint32_t m, const uint32_t P[7]) {
+#pragma unroll
+    for (int t = 6; t >= 0; --t) {
+        const uint32_t c = m & P[t];
+        if (c) m = c;
+    }
+    return (uint32_t)__ffs(m) - 1u;
+}
+
+// min / max of one axis over items a..b (a <= b, b - a < 31) from the table.
+__device__ __forceinline__ float2 axis_range(const WarpScratch& W, uint32_t a, uint32_t b) {
+    const uint32_t t = 31u - (uint32_t)__clz(b - a + 1u);
+    const float2 u = W.st[t][a], v = W.st[t][b + 1u - (1u << t)];
+    return make_float2(fminf(u.x, v.x), fmaxf(u.y, v.y));
+}
+
+// Joins the items of lanes 0..cnt-1 of the warp (all 32 lanes call it):
+// every node whose range lies inside these items is written out, and the
+// runs left over (maximal subtrees whose parent lies outside) stay, each in
+// the lane of its first item (true for those lanes, `it` holding the run); a
+// run that reaches [0, n-1] writes the header instead.  `edge` is the
+// boundary after the last item.  With d[j] the boundary before item j, the
+// node split at boundary j spans from the nearest higher boundary on its
+// left to the one on its right, and its parent is split at the lower of
+// those two.  All of it comes from bit planes of the boundary levels, with
+// no rounds; the children's boxes come from sparse tables of the item boxes.
+// fminf / fmaxf order -0 below +0 and skip NaN whatever the operand order,
+// so any grouping of a range gives the bits of the bottom-up merge.
 __device__ __forceinline__ bool warp_join(WarpItem& it, uint32_t cnt, uint64_t edge, uint32_t n,
                                           int min_leaf, float4* __restrict__ nodes,
-                                          BvhHeader* __restrict__ hdr,
-                                          uint32_t* __restrict__ status) {
+                                          WarpScratch& W, BvhHeader* __restrict__ hdr) {
     const uint32_t lane = threadIdx.x & 31u;
     const unsigned FULL = 0xffffffffu;
-    bool on = lane < cnt;
-    // prefix maxima of d[0..lane] and suffix maxima of d[lane..cnt]
-    const uint64_t dv = on ? it.db : 0ull;
-    uint64_t pre = dv, suf = dv;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const uint64_t u = __shfl_up_sync(FULL, pre, o);
-        const uint64_t w = __shfl_down_sync(FULL, suf, o);
-        if (lane >= (uint32_t)o) pre = pre > u ? pre : u;
-        if (lane + (uint32_t)o < 32u) suf = suf > w ? suf : w;
+    if (cnt == 0u) return false;
+    const bool item = lane < cnt;
+    __syncwarp();   // the lanes have read their items out of this space
+    if (item) {
+        W.il[lane] = it.l;
+        W.ir[lane] = it.r;
+        W.ikl[lane] = it.kl;
+        W.ikr[lane] = it.kr;
+        W.iref[lane] = it.ref;
+        W.icnt[lane] = it.cnt;
     }
-    suf = suf > edge ? suf : edge;
-    const uint64_t pre_left = __shfl_up_sync(FULL, pre, 1);   // max d[0..lane-1]
-    uint32_t bl = lane;   // lane of the run's last item
-    for (int round = 0;; ++round) {
-        const uint32_t nb = bl + 1u;   // first lane after the run
-        const uint32_t src = nb < 32u ? nb : 31u;
-        const uint64_t dnext = __shfl_sync(FULL, it.db, src);
-        const uint32_t s2 = nb + 1u < 32u ? nb + 1u : 31u;
-        const uint64_t sufn = __shfl_sync(FULL, suf, s2);
-        const uint64_t dR = nb < cnt ? dnext : edge;
-        const bool is_left = dR < it.db;
-        const uint64_t far = nb + 1u < cnt ? sufn : edge;   // max d[bl+2..cnt]
-        const bool inside = is_left ? (nb < cnt && far > dR) : (lane > 0 && pre_left > it.db);
-        // the run at lane nb is the matching right child when it is a right
-        // child whose parent is inside (its parent is then this run's split)
-        const bool ready_right = on && !is_left && inside;
-        const bool partner = __shfl_sync(FULL, ready_right, src) && nb < cnt;
-        const bool absorb = on && is_left && inside && partner;
-        const uint32_t p_bl = __shfl_sync(FULL, bl, src);
-        const uint32_t p_r = __shfl_sync(FULL, it.r, src);
-        const uint32_t p_kr = __shfl_sync(FULL, it.kr, src);
-        const float plx = __shfl_sync(FULL, it.lox, src), ply = __shfl_sync(FULL, it.loy, src),
-                    plz = __shfl_sync(FULL, it.loz, src);
-        const float phx = __shfl_sync(FULL, it.hix, src), phy = __shfl_sync(FULL, it.hiy, src),
-                    phz = __shfl_sync(FULL, it.hiz, src);
-        const int32_t p_ref = __shfl_sync(FULL, it.ref, src), p_cnt = __shfl_sync(FULL, it.cnt, src);
-        const uint32_t gone = __reduce_or_sync(FULL, absorb ? (1u << src) : 0u);
-        if (gone == 0u) break;
-        if (round >= 64) {   // deeper than any tree of 64-bit augmented keys
-            if (lane == 0) atomicOr(status, RT_DEV_BADINDEX);
-            break;
-        }
-        if (absorb) {
-            const uint32_t p = it.r;   // global node index: the split
-            float4* np = nodes + 4 * (size_t)p;
-            np[0] = make_float4(it.lox, it.loy, it.loz, it.hix);
-            np[1] = make_float4(it.hiy, it.hiz, plx, ply);
-            np[2] = make_float4(plz, phx, phy, phz);
-            np[3] = make_float4(__int_as_float(it.ref), __int_as_float(p_ref),
-                                __int_as_float(it.cnt), __int_as_float(p_cnt));
-            // merge_bbox(left, right): fmin / fmax, left operand first
-            it.lox = fminf(it.lox, plx); it.loy = fminf(it.loy, ply); it.loz = fminf(it.loz, plz);
-            it.hix = fmaxf(it.hix, phx); it.hiy = fmaxf(it.hiy, phy); it.hiz = fmaxf(it.hiz, phz);
-            it.r = p_r;
-            it.kr = p_kr;
-            bl = p_bl;
-            const uint32_t count = it.r - it.l + 1;
-            const bool interior = count >= (uint32_t)min_leaf + 3u && it.kl != it.kr;
-            it.ref = interior ? (int32_t)p : (int32_t)it.l;
-            it.cnt = interior ? 0 : (int32_t)count;
-            if (it.l == 0 && it.r == n - 1) {
-                hdr->root_ref = it.ref;
-                hdr->root_cnt = it.cnt;
-                hdr->n_tris = n;
-                hdr->root_lo = make_float4(it.lox, it.loy, it.loz, 0.f);
-                hdr->root_hi = make_float4(it.hix, it.hiy, it.hiz, 0.f);
-                on = false;
+    // --- topology, from the levels of the boundaries
+    // the node split at boundary j = lane (1 <= j < cnt), when it lies
+    // inside: left child items A..j-1 (split at lsplit's right end), right
+    // child j..B (split at rsplit's)
+    bool local = false, out = false;
+    uint32_t A = lane, B = lane, lsplit = 0u, rsplit = 0u;
+    {
+        const uint32_t lev = item ? delta_level(it.db) : 0u;
+        uint32_t P[7];
+#pragma unroll
+        for (int t = 0; t < 7; ++t) P[t] = __ballot_sync(FULL, item && ((lev >> t) & 1u));
+        const uint32_t valid = cnt >= 32u ? FULL : ((1u << cnt) - 1u);
+        const uint32_t edge_lev = delta_level(edge);
+        if (item && lane >= 1u) {
+            const uint32_t gt = levels_above(lev, P, valid);
+            const uint32_t lm = gt & ((1u << lane) - 1u);
+            const uint32_t rm = gt & ~((2u << lane) - 1u);
+            if (lm != 0u && (rm != 0u || edge_lev > lev)) {
+                local = true;
+                A = 31u - (uint32_t)__clz(lm);
+                B = rm ? (uint32_t)__ffs(rm) - 2u : cnt - 1u;
+                const uint32_t lin = ((1u << lane) - 1u) & ~((2u << A) - 1u);   // A+1..j-1
+                const uint32_t rin = ((2u << B) - 1u) & ~((2u << lane) - 1u);   // j+1..B
+                lsplit = lin ? top_level(lin, P) - 1u : 0u;
+                rsplit = rin ? top_level(rin, P) - 1u : 0u;
             }
         }
-        if ((gone >> lane) & 1u) on = false;
+        const uint32_t LM = __ballot_sync(FULL, local);
+        // the part of this lane whose parent may lie outside (items A..B:
+        // its node if local, else its item) and whether it does
+        if (item) {
+            const uint32_t la = level_at(A, P);
+            const uint32_t lb = B + 1u < cnt ? level_at(B + 1u, P) : edge_lev;
+            const uint32_t p = lb < la ? B + 1u : A;   // the parent's split
+            out = p == 0u || p >= cnt || !((LM >> p) & 1u);
+        }
     }
-    return on;
+    // --- boxes: the children's for a local node, the item's otherwise
+    float llo[3], lhi[3], rlo[3], rhi[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float vlo = k == 0 ? it.lox : (k == 1 ? it.loy : it.loz);
+        const float vhi = k == 0 ? it.hix : (k == 1 ? it.hiy : it.hiz);
+        __syncwarp();   // the previous axis' queries are done
+        if (item) W.st[0][lane] = make_float2(vlo, vhi);
+#pragma unroll
+        for (int t = 1; t < 5; ++t) {
+            __syncwarp();
+            const uint32_t h = 1u << (t - 1);
+            if (lane + 2u * h <= cnt) {
+                const float2 u = W.st[t - 1][lane], v = W.st[t - 1][lane + h];
+                W.st[t][lane] = make_float2(fminf(u.x, v.x), fmaxf(u.y, v.y));
+            }
+        }
+        __syncwarp();
+        llo[k] = vlo;
+        lhi[k] = vhi;
+        rlo[k] = vlo;
+        rhi[k] = vhi;
+        if (local) {
+            const float2 l = axis_range(W, A, lane - 1u), r = axis_range(W, lane, B);
+            llo[k] = l.x; lhi[k] = l.y;
+            rlo[k] = r.x; rhi[k] = r.y;
+        }
+    }
+    // reference and leaf count of items a..b as one node (split at the
+    // right end of item `split`) or as the item itself
+    auto ref_of = [&](uint32_t a, uint32_t b, uint32_t split, int32_t& ref, int32_t& c) {
+        if (a == b) {
+            ref = W.iref[a];
+            c = W.icnt[a];
+            return;
+        }
+        const uint32_t L = W.il[a], count = W.ir[b] - L + 1u;
+        const bool interior = count >= (uint32_t)min_leaf + 3u && W.ikl[a] != W.ikr[b];
+        ref = interior ? (int32_t)W.ir[split] : (int32_t)L;
+        c = interior ? 0 : (int32_t)count;
+    };
+    if (local) {
+        int32_t lref, lcnt, rref, rcnt;
+        ref_of(A, lane - 1u, lsplit, lref, lcnt);
+        ref_of(lane, B, rsplit, rref, rcnt);
+        float4* np = nodes + 4 * (size_t)W.ir[lane - 1u];
+        np[0] = make_float4(llo[0], llo[1], llo[2], lhi[0]);
+        np[1] = make_float4(lhi[1], lhi[2], rlo[0], rlo[1]);
+        np[2] = make_float4(rlo[2], rhi[0], rhi[1], rhi[2]);
+        np[3] = make_float4(__int_as_float(lref), __int_as_float(rref), __int_as_float(lcnt),
+                            __int_as_float(rcnt));
+    }
+    float4 q0, q1, q2;
+    if (out) {
+        int32_t eref, ecnt;
+        ref_of(A, B, lane - 1u, eref, ecnt);
+        const float lx = local ? fminf(llo[0], rlo[0]) : llo[0],
+                    ly = local ? fminf(llo[1], rlo[1]) : llo[1],
+                    lz = local ? fminf(llo[2], rlo[2]) : llo[2];
+        const float hx = local ? fmaxf(lhi[0], rhi[0]) : lhi[0],
+                    hy = local ? fmaxf(lhi[1], rhi[1]) : lhi[1],
+                    hz = local ? fmaxf(lhi[2], rhi[2]) : lhi[2];
+        const uint32_t gl = W.il[A], gr = W.ir[B];
+        if (gl == 0u && gr == n - 1u) {   // the root
+            hdr->root_ref = eref;
+            hdr->root_cnt = ecnt;
+            hdr->n_tris = n;
+            hdr->root_lo = make_float4(lx, ly, lz, 0.f);
+            hdr->root_hi = make_float4(hx, hy, hz, 0.f);
+            out = false;
+        }
+        q0 = make_float4(__uint_as_float(gl), __uint_as_float(gr), __uint_as_float(W.ikl[A]),
+                         __uint_as_float(W.ikr[B]));
+        q1 = make_float4(lx, ly, lz, hx);
+        q2 = make_float4(hy, hz, __int_as_float(eref), __int_as_float(ecnt));
+    }
+    // hand each run left over to the lane of its first item
+    const uint32_t keep = __reduce_or_sync(FULL, out ? (1u << A) : 0u);
+    float4* stage = reinterpret_cast<float4*>(&W);
+    __syncwarp();   // every read of the scratch is done
+    if (out) {
+        stage[A] = q0;
+        stage[32 + A] = q1;
+        stage[64 + A] = q2;
+    }
+    __syncwarp();
+    const bool mine = (keep >> lane) & 1u;
+    if (mine) {
+        q0 = stage[lane];
+        q1 = stage[32 + lane];
+        q2 = stage[64 + lane];
+        it.l = __float_as_uint(q0.x);
+        it.r = __float_as_uint(q0.y);
+        it.kl = __float_as_uint(q0.z);
+        it.kr = __float_as_uint(q0.w);
+        it.lox = q1.x; it.loy = q1.y; it.loz = q1.z; it.hix = q1.w;
+        it.hiy = q2.x; it.hiz = q2.y;
+        it.ref = __float_as_int(q2.z);
+        it.cnt = __float_as_int(q2.w);   // it.db stays: the run starts at this lane
+    }
+    __syncwarp();   // the staged runs are read before the space is reused
+    return mine;
 }
 
 // Shared state of one emit block: the items left over by its warps, in order.
 template <int C>
 struct EmitSmem {
-    EmitItem list[C];
+    union {
+        EmitItem list[C];
+        WarpScratch scratch[C / 32];   // warp w's: list[32w .. 32w+31]
+    };
     uint32_t wcount[C / 32], woff[C / 32 + 1];
     uint64_t edge;   // boundary after the block's last item
 };
@@ -625,7 +772,7 @@ __device__ __forceinline__ void emit_level(EmitSmem<C>& S, uint32_t blk, uint32_
             return;
         }
         if (t == 0) S.edge = delta_or_max(skeys, (int64_t)min(b0 + (uint32_t)C, n) - 1, n);
-        keep = warp_join(it, cnt, edge, n, min_leaf, nodes, hdr, status);
+        keep = warp_join(it, cnt, edge, n, min_leaf, nodes, S.scratch[w], hdr);
         m = gather_runs<C>(S, it, keep);
     } else {
         // the items left by EMIT_GROUP blocks of the previous level, in order
@@ -667,7 +814,7 @@ __device__ __forceinline__ void emit_level(EmitSmem<C>& S, uint32_t blk, uint32_
             if (w == 0) {
                 const uint32_t cnt = m;
                 if (lane < cnt) item_to_reg(S.list[lane], it);
-                keep = warp_join(it, cnt, S.edge, n, min_leaf, nodes, hdr, status);
+                keep = warp_join(it, cnt, S.edge, n, min_leaf, nodes, S.scratch[0], hdr);
                 const unsigned bal = __ballot_sync(0xffffffffu, keep);
                 if (keep) reg_to_item(it, out[(size_t)blk * EMIT_FMAX + __popc(bal & ((1u << lane) - 1u))]);
                 if (lane == 0 && out_count) out_count[blk] = __popc(bal);
@@ -693,7 +840,8 @@ __device__ __forceinline__ void emit_level(EmitSmem<C>& S, uint32_t blk, uint32_
         const uint32_t cnt = c0 < m ? c1 - c0 : 0u;
         if (lane < cnt) item_to_reg(S.list[c0 + lane], it);
         const uint64_t edge = c1 < m ? S.list[c1].db : S.edge;
-        keep = warp_join(it, cnt, edge, n, min_leaf, nodes, hdr, status);
+        __syncthreads();   // the chunks are read: the list space becomes the warps' scratch
+        keep = warp_join(it, cnt, edge, n, min_leaf, nodes, S.scratch[w], hdr);
         const uint32_t m_new = gather_runs<C>(S, it, keep);
         stalls = m_new == m ? stalls + 1u : 0u;
         m = m_new;

@@ -155,6 +155,15 @@ class Context:
     def sync(self, stream=None):
         check(self.lib, self.lib.rt_stream_sync(self.h, stream))
 
+    def stream_create(self):
+        """A new non-blocking stream of the context (rt_stream handle)."""
+        s = P()
+        check(self.lib, self.lib.rt_stream_create(self.h, C.byref(s)))
+        return s
+
+    def stream_destroy(self, s):
+        check(self.lib, self.lib.rt_stream_destroy(self.h, s))
+
     def device_status(self):
         bits = U32(0)
         check(self.lib, self.lib.rt_device_status(self.h, C.byref(bits)))

@@ -152,6 +152,38 @@ def test_mid_scale_animated_frames_equal_oracle(ctx, orc, frame):
     tree_invariants(gc, sc.n_tris)
 
 
+def test_calls_on_one_scene_ordered_across_streams(ctx):
+    """Calls on one scene run in call order whatever streams they name: a
+    build of the 1,240,576-triangle terrain on the context's stream, two more
+    issued at once on two other streams, then a render on a third, give the
+    tree and image of the same calls on one stream."""
+    wl = scenes.workload_mid()
+    sc = wl["terrain"].scene(0)
+    w, h, nb, cam = 480, 270, 3, wl["camera"]
+    ref = capi.Scene(ctx, sc)
+    for _ in range(3):
+        ref.build(30, 1)
+    want = ctx.alloc(4 * w * h)
+    ref.render(cam, w, h, nb, want)
+    ctx.sync()
+    streams = [ctx.stream_create() for _ in range(3)]
+    try:
+        g = capi.Scene(ctx, sc)
+        g.build(30, 1)
+        g.build(30, 1, stream=streams[0])
+        g.build(30, 1, stream=streams[1])
+        got = ctx.alloc(4 * w * h)
+        g.render(cam, w, h, nb, got, stream=streams[2])
+        assert_canon_equal(g.canon(), ref.canon())
+        ctx.sync(streams[2])
+        assert np.array_equal(got.read(np.uint8), want.read(np.uint8))
+        assert np.array_equal(g.sort_arrays()[2], ref.sort_arrays()[2])
+    finally:
+        for s in streams:
+            ctx.stream_destroy(s)
+    assert ctx.device_status() == 0
+
+
 def test_invalid_inputs_rejected(ctx):
     sc = scenes.soup(100, seed=1)
     bad = scenes.Scene(sc.pos4, sc.nrm4, sc.idx.copy(), sc.mats, sc.mat_map, sc.lights)
