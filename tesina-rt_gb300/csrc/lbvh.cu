@@ -153,12 +153,20 @@ __global__ void __launch_bounds__(256) k_refit_leaves(uint32_t n, const uint32_t
     }
 }
 
-constexpr int EMIT_C0 = 512;                       // triangles per level-0 block
+#ifndef RT_EMIT_C0
+#define RT_EMIT_C0 512
+#endif
+#ifndef RT_EMIT_MINB0
+#define RT_EMIT_MINB0 2
+#endif
+constexpr int EMIT_C0 = RT_EMIT_C0;                // triangles per level-0 block
 constexpr int EMIT_C1 = EMIT_GROUP * EMIT_FMAX;    // items per block above level 0
 
-// One level of the emit (emit_level), one block per run of items.
+// One level of the emit (emit_level), one block per run of items; level-0
+// blocks are kept to a register budget that lets RT_EMIT_MINB0 of them
+// share an SM.
 template <int C>
-__global__ void __launch_bounds__(C, 1024 / C) k_emit_level(
+__global__ void __launch_bounds__(C, C == EMIT_C0 ? RT_EMIT_MINB0 : 1) k_emit_level(
     uint32_t n, const uint32_t* __restrict__ skeys, const float4* __restrict__ leafbox,
     const EmitItem* __restrict__ in, const uint32_t* __restrict__ in_count, uint32_t n_in,
     EmitItem* __restrict__ out, uint32_t* __restrict__ out_count, float4* __restrict__ nodes,

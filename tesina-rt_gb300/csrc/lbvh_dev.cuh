@@ -19,6 +19,7 @@ constexpr int SORT_ITEMS = 16;
 constexpr int SORT_TILE = SORT_THREADS * SORT_ITEMS;   // 4096 keys per tile
 constexpr uint32_t LB_AGG = 1u << 30, LB_PREFIX = 2u << 30, LB_MASK = (1u << 30) - 1;
 constexpr uint32_t LB_SPIN_LIMIT = 1u << 22;
+constexpr int LB_WINDOW = 8;   // look-back words read per round trip
 
 // float <-> order-preserving uint32 (min/max of the integers == fmin/fmax of
 // the floats for non-NaN values).
@@ -31,13 +32,16 @@ __device__ __forceinline__ float o2f(uint32_t o) {
     return __uint_as_float(u);
 }
 
-__device__ __forceinline__ uint32_t ld_acquire(const uint32_t* p) {
+// Relaxed GPU-scope accesses: coherent in L2, no ordering of other memory.
+// For words that carry their whole message (the radix look-back's flag and
+// count).
+__device__ __forceinline__ uint32_t ld_relaxed(const uint32_t* p) {
     uint32_t v;
-    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
     return v;
 }
-__device__ __forceinline__ void st_release(uint32_t* p, uint32_t v) {
-    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+__device__ __forceinline__ void st_relaxed(uint32_t* p, uint32_t v) {
+    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 // atomicAdd with acquire-release ordering at GPU scope: the caller's earlier
 // writes are visible to whoever reads the counter's new value, and the
@@ -85,6 +89,24 @@ __device__ __forceinline__ MortonParams morton_params(const uint32_t* bounds, in
     return m;
 }
 
+// Spreads the low 21 bits of v to every third bit (bit t to bit 3t): the
+// mask-and-shift bit interleave ("magic numbers") of Morton encoders.
+__device__ __forceinline__ uint64_t spread3(uint64_t v) {
+    v &= 0x1fffffull;
+    v = (v | (v << 32)) & 0x1f00000000ffffull;
+    v = (v | (v << 16)) & 0x1f0000ff0000ffull;
+    v = (v | (v << 8)) & 0x100f00f00f00f00full;
+    v = (v | (v << 4)) & 0x10c30c30c30c30c3ull;
+    v = (v | (v << 2)) & 0x1249249249249249ull;
+    return v;
+}
+
+// morton_encode's bit loop takes, for code bit b (b < depth), bit (b+off)/3
+// of the slice of axis (b+off+1) % 3.  With j = b + off, that is the
+// interleave I whose bit j is bit j/3 of axis (j+1) % 3 (y, z, x for
+// j = 0, 1, 2 mod 3), shifted down by off; the slices keep their low
+// ceil(depth/3) bits (a slice of 2^ceil(depth/3), from a centroid at the
+// upper bound, contributes nothing).
 __device__ __forceinline__ uint32_t morton_code(const MortonParams& P, const float lo[3],
                                                 const float hi[3]) {
     uint32_t m[3];
@@ -94,20 +116,14 @@ __device__ __forceinline__ uint32_t morton_code(const MortonParams& P, const flo
         float slice = (center - P.glo[k]) * P.inv[k];
         slice = fmaxf(0.0f, fminf(1.0f, slice));
         slice *= P.scale;
-        m[k] = (uint32_t)slice;   // truncation; slice == 2^k keeps only out-of-range bits
+        m[k] = (uint32_t)slice;   // truncation
     }
-    uint32_t code = 0;
-    int axis = (P.offset + 1) % 3;
-#pragma unroll
-    for (int bit = 0; bit < 32; ++bit) {
-        if (bit < P.depth) {
-            const int src = (bit + P.offset) / 3;
-            const uint32_t mv = axis == 0 ? m[0] : (axis == 1 ? m[1] : m[2]);
-            code |= ((mv >> src) & 1u) << bit;
-            axis = axis == 2 ? 0 : axis + 1;
-        }
-    }
-    return code;
+    const int bits = (P.depth + 2) / 3;
+    const uint32_t keep = (1u << bits) - 1u;
+    const uint64_t I = spread3(m[1] & keep) | (spread3(m[2] & keep) << 1) |
+                       (spread3(m[0] & keep) << 2);
+    const uint64_t code = I >> P.offset;
+    return P.depth >= 32 ? (uint32_t)code : (uint32_t)code & ((1u << P.depth) - 1u);
 }
 
 // Exclusive scan of one value per thread over a 256-thread block.
@@ -205,29 +221,46 @@ __device__ __forceinline__ void onesweep_tile(SortSmemT<ITEMS>& S, uint32_t tile
         S.whist[w][dgt] = cnt;
         cnt += c;
     }
+    // Decoupled look-back.  Each word holds its whole message (flag and
+    // count), so relaxed accesses suffice; the words of LB_WINDOW earlier
+    // tiles are read per round trip and summed nearest first, up to the first
+    // inclusive prefix or the first tile that has not published yet.
     uint32_t* my = &lookback[(size_t)tile * 256 + dgt];
     uint32_t excl = 0;
     if (tile == 0) {
-        st_release(my, LB_PREFIX | cnt);
+        st_relaxed(my, LB_PREFIX | cnt);
     } else {
-        st_release(my, LB_AGG | cnt);
+        st_relaxed(my, LB_AGG | cnt);
         int64_t p = (int64_t)tile - 1;
         uint32_t spins = 0;
-        while (p >= 0) {
-            const uint32_t s = ld_acquire(&lookback[(size_t)p * 256 + dgt]);
-            const uint32_t flag = s & ~LB_MASK;
-            if (flag == 0) {
-                if (++spins > LB_SPIN_LIMIT) {
-                    atomicOr(status, RT_DEV_TIMEOUT);
-                    break;
+        for (;;) {
+            uint32_t w[LB_WINDOW];
+#pragma unroll
+            for (int q = 0; q < LB_WINDOW; ++q)   // tile 0 is always a prefix: p - q < 0 is never summed
+                w[q] = p - q >= 0 ? ld_relaxed(&lookback[(size_t)(p - q) * 256 + dgt]) : LB_PREFIX;
+            int used = 0;
+            bool done = false, wait = false;
+#pragma unroll
+            for (int q = 0; q < LB_WINDOW; ++q) {
+                const uint32_t flag = w[q] & ~LB_MASK;
+                if (!done && !wait) {
+                    if (flag == 0) {
+                        wait = true;
+                    } else {
+                        excl += w[q] & LB_MASK;
+                        ++used;
+                        done = flag == LB_PREFIX;
+                    }
                 }
-                continue;
             }
-            excl += s & LB_MASK;
-            if (flag == LB_PREFIX) break;
-            --p;
+            if (done) break;
+            p -= used;
+            if (wait && ++spins > LB_SPIN_LIMIT) {
+                atomicOr(status, RT_DEV_TIMEOUT);
+                break;
+            }
         }
-        st_release(my, LB_PREFIX | (excl + cnt));
+        st_relaxed(my, LB_PREFIX | (excl + cnt));
     }
     const uint32_t gstart = block_excl_scan_256(__ldg(&hist[dgt]), S.scan);
     const uint32_t lstart = block_excl_scan_256(cnt, S.scan);
