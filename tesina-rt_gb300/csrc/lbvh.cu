@@ -159,6 +159,12 @@ __global__ void __launch_bounds__(256) k_refit_leaves(uint32_t n, const uint32_t
 #ifndef RT_EMIT_MINB0
 #define RT_EMIT_MINB0 2
 #endif
+#ifndef RT_EMIT_LEAVE0
+#define RT_EMIT_LEAVE0 128u   // runs a level-0 block may leave unjoined
+#endif
+#ifndef RT_EMIT_LEAVE1
+#define RT_EMIT_LEAVE1 64u    // the same above level 0
+#endif
 constexpr int EMIT_C0 = RT_EMIT_C0;                // triangles per level-0 block
 constexpr int EMIT_C1 = EMIT_GROUP * EMIT_FMAX;    // items per block above level 0
 
@@ -170,11 +176,11 @@ __global__ void __launch_bounds__(C, C == EMIT_C0 ? RT_EMIT_MINB0 : 1) k_emit_le
     uint32_t n, const uint32_t* __restrict__ skeys, const float4* __restrict__ leafbox,
     const EmitItem* __restrict__ in, const uint32_t* __restrict__ in_count, uint32_t n_in,
     EmitItem* __restrict__ out, uint32_t* __restrict__ out_count, float4* __restrict__ nodes,
-    int min_leaf, BvhHeader* __restrict__ hdr, uint32_t* __restrict__ status) {
+    int min_leaf, uint32_t leave, BvhHeader* __restrict__ hdr, uint32_t* __restrict__ status) {
     extern __shared__ __align__(16) unsigned char emit_smem[];
     auto& S = *reinterpret_cast<EmitSmem<C>*>(emit_smem);
     emit_level<C>(S, blockIdx.x, n, skeys, leafbox, in, in_count, n_in, out, out_count, nodes,
-                  min_leaf, hdr, status);
+                  min_leaf, leave, hdr, status);
 }
 
 // Blocks of level 0 and of level 1 (the two item buffers are sized for them).
@@ -211,16 +217,18 @@ static cudaError_t launch_emit(const LbvhArgs& a, uint8_t* emit_scratch, cudaStr
     items[1] = items[0] + (size_t)nb0 * EMIT_FMAX;
     counts[0] = reinterpret_cast<uint32_t*>(items[1] + (size_t)nb1 * EMIT_FMAX);
     counts[1] = counts[0] + nb0;
+    // level-0 blocks leave up to EMIT_FMAX runs to level 1 unless they are
+    // the only block
     k_emit_level<EMIT_C0><<<nb0, EMIT_C0, sizeof(EmitSmem<EMIT_C0>), s>>>(
         n, a.keys_sorted, a.leafbox, nullptr, nullptr, 0, items[0], counts[0], a.nodes,
-        a.min_leaf, a.hdr, a.status);
+        a.min_leaf, nb0 > 1 ? RT_EMIT_LEAVE0 : 32u, a.hdr, a.status);
     uint32_t n_in = nb0;
     int src = 0;
     while (n_in > 1) {
         const uint32_t g = (n_in + EMIT_GROUP - 1) / EMIT_GROUP;
         k_emit_level<EMIT_C1><<<g, EMIT_C1, sizeof(EmitSmem<EMIT_C1>), s>>>(
             n, a.keys_sorted, a.leafbox, items[src], counts[src], n_in, items[src ^ 1],
-            counts[src ^ 1], a.nodes, a.min_leaf, a.hdr, a.status);
+            counts[src ^ 1], a.nodes, a.min_leaf, g > 1 ? RT_EMIT_LEAVE1 : 32u, a.hdr, a.status);
         n_in = g;
         src ^= 1;
     }

@@ -753,7 +753,9 @@ __device__ __forceinline__ uint32_t gather_runs(EmitSmem<C>& S, const WarpItem& 
 // (in == null): the items are triangles blk*C .. blk*C+C-1; otherwise the
 // items left by blocks blk*EMIT_GROUP .. of the previous level (in_count[k]
 // items at in[k * EMIT_FMAX]).  Leaves the block's own items at
-// out[blk * EMIT_FMAX] and their number in out_count[blk].
+// out[blk * EMIT_FMAX] and their number in out_count[blk].  The block stops
+// joining once `leave` runs or fewer are left (leave <= EMIT_FMAX; 32: join
+// down to one warp's runs, as the root's level must).
 template <int C>
 __device__ __forceinline__ void emit_level(EmitSmem<C>& S, uint32_t blk, uint32_t n,
                                            const uint32_t* __restrict__ skeys,
@@ -763,7 +765,7 @@ __device__ __forceinline__ void emit_level(EmitSmem<C>& S, uint32_t blk, uint32_
                                            uint32_t n_in, EmitItem* __restrict__ out,
                                            uint32_t* __restrict__ out_count,
                                            float4* __restrict__ nodes, int min_leaf,
-                                           BvhHeader* __restrict__ hdr,
+                                           uint32_t leave, BvhHeader* __restrict__ hdr,
                                            uint32_t* __restrict__ status) {
     static_assert(C % 32 == 0 && C >= EMIT_FMAX, "block size");
     const uint32_t t = threadIdx.x, lane = t & 31u, w = t >> 5;
@@ -843,6 +845,14 @@ __device__ __forceinline__ void emit_level(EmitSmem<C>& S, uint32_t blk, uint32_
     // its parent outside the block.
     uint32_t stalls = 0;
     for (uint32_t pass = 0;; ++pass) {
+        if (m <= leave && leave > 32u) {
+            // few enough to be items of the next level as they are: the
+            // next level joins them (a block's passes get longer and emptier
+            // as its runs thin out)
+            for (uint32_t e = t; e < m; e += (uint32_t)C) out[(size_t)blk * EMIT_FMAX + e] = S.list[e];
+            if (t == 0 && out_count) out_count[blk] = m;
+            return;
+        }
         if (m <= 32u) {
             if (w == 0) {
                 const uint32_t cnt = m;
