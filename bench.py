@@ -413,8 +413,13 @@ def run_gpu(args):
     torch.cuda.synchronize()
     # the project's autotuner picks block shape, resident blocks and packet
     # width on this scene (outside the timed region)
-    tuned, tuned_ms = scene.autotune(wl["camera"], w, h, nb, trials=3)
-    log("autotuned", tuned, "%.3f ms" % tuned_ms)
+    if args.render_variant is None:
+        tuned, tuned_ms = scene.autotune(wl["camera"], w, h, nb, trials=3)
+        log("autotuned", tuned, "%.3f ms" % tuned_ms)
+    else:   # a fixed configuration (profiling runs: serialised launches mislead the tuner)
+        ctx.set_render_config(args.render_variant, args.render_blocks, args.render_chunk)
+        tuned, tuned_ms = ctx.render_config(), None
+        log("fixed render configuration", tuned)
     sampler = ClockSampler(local)
     if world > 1:
         torch.distributed.barrier()
@@ -595,6 +600,10 @@ def main():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--no-stress", action="store_true")
+    ap.add_argument("--render-variant", type=int, default=None,
+                    help="render kernel variant instead of the autotuner's pick")
+    ap.add_argument("--render-blocks", type=int, default=0, help="resident blocks per SM (0: all)")
+    ap.add_argument("--render-chunk", type=int, default=128, help="pixels per work-counter grab")
     args = ap.parse_args()
     if args.warmup < 3:
         log("warmup raised to 3")

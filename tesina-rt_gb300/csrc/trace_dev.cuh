@@ -60,6 +60,150 @@ __device__ __forceinline__ bool leaf_any(const SceneView& S, const TRay& r, int3
     return false;
 }
 
+// Traversal stack of the two-phase loop: node references with their leaf
+// counts and (DIST) the entry distances the closest-hit search prunes by.
+template <bool DIST>
+struct TravStack {
+    int32_t ref[STACK], cnt[STACK];
+    float a[DIST ? STACK : 1];
+    int sp = 0;
+    __device__ __forceinline__ bool push(int32_t r, int32_t c, float d) {
+        if (sp >= STACK) return false;
+        ref[sp] = r;
+        cnt[sp] = c;
+        if (DIST) a[sp] = d;
+        ++sp;
+        return true;
+    }
+    // The next entry (DIST: the next whose entry distance is within tmax)
+    // into cur / cur_cnt; cur = -1 when none is left.
+    __device__ __forceinline__ void pop(float tmax, int32_t& cur, int32_t& cur_cnt) {
+        cur = -1;
+        while (sp > 0) {
+            --sp;
+            if (!DIST || a[sp] <= tmax) {
+                cur = ref[sp];
+                cur_cnt = cnt[sp];
+                return;
+            }
+        }
+    }
+};
+
+// Traversal in two phases per round (Aila & Laine's "while-while" loop with
+// speculative traversal): a lane walks inner nodes, setting aside the first
+// leaf it reaches and walking on, until every lane of the warp holds a leaf;
+// then the lanes intersect their leaves.  Leaves are still intersected in
+// the depth-first order above.  Nodes walked past a set-aside leaf are
+// accepted against the tMax before that leaf; any of them the exact order
+// would have dropped starts beyond the final tMax, so none of its triangles
+// is accepted (t >= entry > tMax): the same hit, equal-t ties included.
+static __device__ Hit closest_hit_ww(const SceneView& S, const BvhHeader& H, const TRay& r,
+                                     float tmax, uint32_t* status) {
+    Hit best{-1, tmax, 0.f, 0.f};
+    float A;
+    if (!slab(r, best.t, H.root_lo.x, H.root_lo.y, H.root_lo.z, H.root_hi.x, H.root_hi.y,
+              H.root_hi.z, A))
+        return best;
+    if (H.root_cnt > 0) {
+        leaf_closest(S, r, H.root_ref, H.root_cnt, best);
+        return best;
+    }
+    TravStack<true> st;
+    // the next node (inner: cnt 0, leaf: cnt > 0, none: ref < 0) and the
+    // leaf set aside
+    int32_t cur = H.root_ref, cur_cnt = 0, lf = -1, lf_cnt = 0;
+    auto pop = [&]() { st.pop(best.t, cur, cur_cnt); };
+    for (;;) {
+        while (cur >= 0 && cur_cnt == 0) {
+            float4 n0, n1, n2;
+            int4 n3;
+            load_node(S.nodes, cur, n0, n1, n2, n3);
+            // c0 = left: lo (n0.x, n0.y, n0.z) hi (n0.w, n1.x, n1.y)
+            // c1 = right: lo (n1.z, n1.w, n2.x) hi (n2.y, n2.z, n2.w)
+            const f3 dl = mk3(n1.z - n0.x, n1.w - n0.y, n2.x - n0.z);
+            const bool left_first = dot(r.d, dl) > 0.0f;
+            float a0, a1;
+            const bool h0 = slab(r, best.t, n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, a0);
+            const bool h1 = slab(r, best.t, n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, a1);
+            const bool hf = left_first ? h0 : h1, hs = left_first ? h1 : h0;
+            if (hs && !st.push(left_first ? n3.y : n3.x, left_first ? n3.w : n3.z,
+                               left_first ? a1 : a0))
+                atomicOr(status, RT_DEV_OVERFLOW);
+            if (hf) {
+                cur = left_first ? n3.x : n3.y;
+                cur_cnt = left_first ? n3.z : n3.w;
+            } else {
+                pop();
+            }
+            if (cur >= 0 && cur_cnt > 0 && lf < 0) {   // set the leaf aside, walk on
+                lf = cur;
+                lf_cnt = cur_cnt;
+                pop();
+            }
+            if (__all_sync(__activemask(), lf >= 0)) break;
+        }
+        while (lf >= 0) {
+            leaf_closest(S, r, lf, lf_cnt, best);
+            lf = -1;
+            if (cur >= 0 && cur_cnt > 0) {
+                lf = cur;
+                lf_cnt = cur_cnt;
+                pop();
+            }
+        }
+        if (cur < 0) return best;
+    }
+}
+
+// Any hit ends the search, whatever the order: the same two-phase loop.
+static __device__ bool any_hit_ww(const SceneView& S, const BvhHeader& H, const TRay& r, float tmax,
+                                  uint32_t* status) {
+    if (!slab_shadow(r, tmax, H.root_lo.x, H.root_lo.y, H.root_lo.z, H.root_hi.x, H.root_hi.y,
+                     H.root_hi.z))
+        return false;
+    if (H.root_cnt > 0) return leaf_any(S, r, H.root_ref, H.root_cnt, tmax);
+    TravStack<false> st;
+    int32_t cur = H.root_ref, cur_cnt = 0, lf = -1, lf_cnt = 0;
+    auto pop = [&]() { st.pop(0.f, cur, cur_cnt); };
+    for (;;) {
+        while (cur >= 0 && cur_cnt == 0) {
+            float4 n0, n1, n2;
+            int4 n3;
+            load_node(S.nodes, cur, n0, n1, n2, n3);
+            const f3 dl = mk3(n1.z - n0.x, n1.w - n0.y, n2.x - n0.z);
+            const bool left_first = dot(r.d, dl) > 0.0f;
+            const bool h0 = slab_shadow(r, tmax, n0.x, n0.y, n0.z, n0.w, n1.x, n1.y);
+            const bool h1 = slab_shadow(r, tmax, n1.z, n1.w, n2.x, n2.y, n2.z, n2.w);
+            const bool hf = left_first ? h0 : h1, hs = left_first ? h1 : h0;
+            if (hs && !st.push(left_first ? n3.y : n3.x, left_first ? n3.w : n3.z, 0.f))
+                atomicOr(status, RT_DEV_OVERFLOW);
+            if (hf) {
+                cur = left_first ? n3.x : n3.y;
+                cur_cnt = left_first ? n3.z : n3.w;
+            } else {
+                pop();
+            }
+            if (cur >= 0 && cur_cnt > 0 && lf < 0) {
+                lf = cur;
+                lf_cnt = cur_cnt;
+                pop();
+            }
+            if (__all_sync(__activemask(), lf >= 0)) break;
+        }
+        while (lf >= 0) {
+            if (leaf_any(S, r, lf, lf_cnt, tmax)) return true;
+            lf = -1;
+            if (cur >= 0 && cur_cnt > 0) {
+                lf = cur;
+                lf_cnt = cur_cnt;
+                pop();
+            }
+        }
+        if (cur < 0) return false;
+    }
+}
+
 static __device__ Hit closest_hit(const SceneView& S, const BvhHeader& H, const TRay& r, float tmax,
                            uint32_t* status) {
     Hit best{-1, tmax, 0.f, 0.f};
@@ -207,6 +351,8 @@ __device__ __forceinline__ HitInfo complete_hit(const SceneView& S, f3 o, f3 d, 
 
 // Shadow ray of shadow_trace_single for one light (shadow-trace-bvh.cl:
 // 375-418); point lights as spot lights without a cone.
+// WW: the two-phase traversal (any_hit_ww) instead of any_hit.
+template <bool WW = false>
 __device__ __forceinline__ bool occluded(const SceneView& S, const BvhHeader& H, const rt_light& L,
                                          f3 hp, uint32_t* status) {
     f3 dir;
@@ -222,7 +368,7 @@ __device__ __forceinline__ bool occluded(const SceneView& S, const BvhHeader& H,
     }
     const f3 inv = mk3(1.0f / dir.x, 1.0f / dir.y, 1.0f / dir.z);
     const TRay r = make_tray(hp, dir, inv, 0.01f);
-    return any_hit(S, H, r, 1e37f, status);
+    return WW ? any_hit_ww(S, H, r, 1e37f, status) : any_hit(S, H, r, 1e37f, status);
 }
 
 // Local Whitted term of shade_sample, as the fixed-point increments that
@@ -341,6 +487,7 @@ struct PixelResult {
 // shadow ray per light, local shading, reflection ray while the material
 // reflects and the bounce budget lasts.  Integer accumulation of the
 // fixed-point contributions makes the sum independent of evaluation order.
+template <bool WW = false>
 __device__ __forceinline__ PixelResult render_pixel(const SceneView& S, const BvhHeader& H,
                                                     const rt_lights& L, const rt_camera& cam,
                                                     int x, int y, int w, int h, int max_bounces,
@@ -352,14 +499,14 @@ __device__ __forceinline__ PixelResult render_pixel(const SceneView& S, const Bv
     for (int bounce = 0;; ++bounce) {
         const f3 inv = mk3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
         const TRay r = make_tray(o, d, inv, tmin);
-        const Hit hit = closest_hit(S, H, r, tmax, status);
+        const Hit hit = WW ? closest_hit_ww(S, H, r, tmax, status) : closest_hit(S, H, r, tmax, status);
         if (hit.id < 0) break;
         ++res.hits;
         const HitInfo hi = complete_hit(S, o, d, hit);
         const rt_material mat = S.mats[__ldg(&S.map[hit.id])];
         uint32_t mask = 0;
         for (int l = 0; l < L.count; ++l)
-            if (occluded(S, H, L.light[l], hi.hp, status)) mask |= 1u << l;
+            if (occluded<WW>(S, H, L.light[l], hi.hp, status)) mask |= 1u << l;
         res.shadow += (uint32_t)L.count;
         const uint3 c = shade_hit(L, mat, hi.hp, hi.n, d, contribution, mask);
         res.r += c.x;
