@@ -7,7 +7,7 @@
 //   k_morton_hist   morton_encode (:181-252) fused with the digit histograms of
 //                   every radix pass;
 //   k_onesweep      stable LSD radix pass, 8-bit digits, warp-level
-//                   __match_any_sync ranking and decoupled look-back with a
+//                   ballot ranking and decoupled look-back with a
 //                   bounded spin (replaces the bitonic network of
 //                   bvh-builder-sort.cl and bvh-builder.cpp:361-454);
 //   k_permute       rearrange_indices / rearrange_map (:49-72) fused with the
@@ -113,7 +113,7 @@ __global__ void __launch_bounds__(256) k_radix_hist(const uint32_t* __restrict__
     }
 }
 
-__global__ void __launch_bounds__(SORT_THREADS) k_onesweep(
+__global__ void __launch_bounds__(SORT_THREADS, 3) k_onesweep(
     const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin, uint32_t* __restrict__ kout,
     uint32_t* __restrict__ vout, uint32_t n, int shift, const uint32_t* __restrict__ hist,
     uint32_t* __restrict__ lookback, uint32_t* __restrict__ tile_ctr, uint32_t* __restrict__ status) {

@@ -19,7 +19,7 @@ constexpr int SORT_ITEMS = 16;
 constexpr int SORT_TILE = SORT_THREADS * SORT_ITEMS;   // 4096 keys per tile
 constexpr uint32_t LB_AGG = 1u << 30, LB_PREFIX = 2u << 30, LB_MASK = (1u << 30) - 1;
 constexpr uint32_t LB_SPIN_LIMIT = 1u << 22;
-constexpr int LB_WINDOW = 8;   // look-back words read per round trip
+constexpr int LB_WINDOW = 32;  // look-back words read per round trip
 
 // float <-> order-preserving uint32 (min/max of the integers == fmin/fmax of
 // the floats for non-NaN values).
@@ -152,6 +152,11 @@ __device__ __forceinline__ uint32_t block_excl_scan_256(uint32_t v, uint32_t* s_
     return warp_base + x - v;
 }
 
+// Phase marks of a radix tile (k = 0..6), for timing harnesses; none by default.
+#ifndef RT_SORT_MARK
+#define RT_SORT_MARK(k)
+#endif
+
 template <int ITEMS>
 struct SortSmemT {
     uint32_t keys[SORT_THREADS * ITEMS];
@@ -165,7 +170,7 @@ struct SortSmemT {
 using SortSmem = SortSmemT<SORT_ITEMS>;
 
 // One tile of a stable LSD radix pass (8-bit digit at `shift`): warp-striped
-// loads, __match_any_sync ranking in index order, decoupled look-back over
+// loads, ballot ranking in index order, decoupled look-back over
 // the earlier tiles of the same sequence, shared-memory staging and a
 // coalesced scatter.  Must be called by all SORT_THREADS threads of a block;
 // a tile holds SORT_THREADS * ITEMS keys.
@@ -179,6 +184,7 @@ __device__ __forceinline__ void onesweep_tile(SortSmemT<ITEMS>& S, uint32_t tile
                                               uint32_t* __restrict__ lookback,
                                               uint32_t* __restrict__ status) {
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    RT_SORT_MARK(0);
     for (int i = tid; i < SORT_WARPS * 256; i += SORT_THREADS) (&S.whist[0][0])[i] = 0;
     __syncthreads();
     const size_t base = (size_t)tile * (SORT_THREADS * ITEMS);
@@ -197,12 +203,16 @@ __device__ __forceinline__ void onesweep_tile(SortSmemT<ITEMS>& S, uint32_t tile
         const size_t g = base + (size_t)warp * (ITEMS * 32) + j * 32 + lane;
         const bool ok = g < n;
         const uint32_t d = (k[j] >> shift) & 255u;
-        const uint32_t valid = __ballot_sync(0xffffffffu, ok);
-        uint32_t peers = 0, prev = 0;
-        if (ok) {
-            peers = __match_any_sync(valid, d);
-            prev = S.whist[warp][d];
+        // lanes holding the same digit: one ballot per digit bit (a fixed
+        // cost, where a match instruction grows with the distinct digits)
+        uint32_t peers = __ballot_sync(0xffffffffu, ok);
+#pragma unroll
+        for (int b = 0; b < 8; ++b) {
+            const uint32_t bit = __ballot_sync(0xffffffffu, (d >> b) & 1u);
+            peers &= ((d >> b) & 1u) ? bit : ~bit;
         }
+        uint32_t prev = 0;
+        if (ok) prev = S.whist[warp][d];
         __syncwarp();
         if (ok) {
             rank[j] = prev + __popc(peers & lanemask_lt);
@@ -213,6 +223,7 @@ __device__ __forceinline__ void onesweep_tile(SortSmemT<ITEMS>& S, uint32_t tile
     }
     __syncthreads();
 
+    RT_SORT_MARK(1);
     const uint32_t dgt = tid;   // 256 threads <-> 256 digits
     uint32_t cnt = 0;
 #pragma unroll
@@ -221,16 +232,30 @@ __device__ __forceinline__ void onesweep_tile(SortSmemT<ITEMS>& S, uint32_t tile
         S.whist[w][dgt] = cnt;
         cnt += c;
     }
+    uint32_t* my = &lookback[(size_t)tile * 256 + dgt];
+    st_relaxed(my, (tile == 0 ? LB_PREFIX : LB_AGG) | cnt);   // as early as the counts are known
+    const uint32_t lstart = block_excl_scan_256(cnt, S.scan);
+    S.lstart[dgt] = lstart;
+    __syncthreads();
+    // the tile in digit order in shared memory (frees the registers of the
+    // keys for the look-back's window)
+#pragma unroll
+    for (int j = 0; j < ITEMS; ++j) {
+        const size_t g = base + (size_t)warp * (ITEMS * 32) + j * 32 + lane;
+        if (g < n) {
+            const uint32_t d = (k[j] >> shift) & 255u;
+            const uint32_t p = S.lstart[d] + S.whist[warp][d] + rank[j];
+            S.keys[p] = k[j];
+            S.vals[p] = v[j];
+        }
+    }
     // Decoupled look-back.  Each word holds its whole message (flag and
     // count), so relaxed accesses suffice; the words of LB_WINDOW earlier
     // tiles are read per round trip and summed nearest first, up to the first
     // inclusive prefix or the first tile that has not published yet.
-    uint32_t* my = &lookback[(size_t)tile * 256 + dgt];
+    RT_SORT_MARK(2);
     uint32_t excl = 0;
-    if (tile == 0) {
-        st_relaxed(my, LB_PREFIX | cnt);
-    } else {
-        st_relaxed(my, LB_AGG | cnt);
+    if (tile > 0) {
         int64_t p = (int64_t)tile - 1;
         uint32_t spins = 0;
         for (;;) {
@@ -262,22 +287,11 @@ __device__ __forceinline__ void onesweep_tile(SortSmemT<ITEMS>& S, uint32_t tile
         }
         st_relaxed(my, LB_PREFIX | (excl + cnt));
     }
+    RT_SORT_MARK(3);
     const uint32_t gstart = block_excl_scan_256(__ldg(&hist[dgt]), S.scan);
-    const uint32_t lstart = block_excl_scan_256(cnt, S.scan);
     S.goff[dgt] = gstart + excl - lstart;
-    S.lstart[dgt] = lstart;
     __syncthreads();
-#pragma unroll
-    for (int j = 0; j < ITEMS; ++j) {
-        const size_t g = base + (size_t)warp * (ITEMS * 32) + j * 32 + lane;
-        if (g < n) {
-            const uint32_t d = (k[j] >> shift) & 255u;
-            const uint32_t p = S.lstart[d] + S.whist[warp][d] + rank[j];
-            S.keys[p] = k[j];
-            S.vals[p] = v[j];
-        }
-    }
-    __syncthreads();
+    RT_SORT_MARK(4);
     const uint32_t valid_n = (uint32_t)min((size_t)(SORT_THREADS * ITEMS), (size_t)n - base);
     for (uint32_t i = tid; i < valid_n; i += SORT_THREADS) {
         const uint32_t key = S.keys[i];
@@ -287,6 +301,7 @@ __device__ __forceinline__ void onesweep_tile(SortSmemT<ITEMS>& S, uint32_t tile
         vout[dst] = S.vals[i];
     }
     __syncthreads();   // the shared buffers are reused by the next tile
+    RT_SORT_MARK(5);
 }
 
 // rearrange_indices / rearrange_map (bvh-builder.cl:49-72) of sorted slot i,
