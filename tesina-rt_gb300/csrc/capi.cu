@@ -363,6 +363,7 @@ int32_t rt_init(rt_ctx** out, int32_t device) {
     cudaDeviceProp prop;
     CU(cudaGetDeviceProperties(&prop, device));
     c->num_sms = prop.multiProcessorCount;
+    c->smem_per_sm = (int)prop.sharedMemPerMultiprocessor;
     CU(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
     CU(cudaMalloc(&c->d_status, sizeof(uint32_t)));
     CU(cudaMemset(c->d_status, 0, sizeof(uint32_t)));
@@ -898,9 +899,26 @@ int32_t rt_fb_copy(rt_ctx* c, const uint32_t* img, uint8_t* rgba, size_t px, rt_
 static cudaError_t launch_render_cfg(rt_ctx* c, rt::RenderArgs a, const rt_render_config& cfg,
                                      cudaStream_t cs) {
     int threads = 0, minb = 0;
-    rt::render_variant_info(cfg.variant, &threads, &minb, nullptr);
+    const void* fn = nullptr;
+    rt::render_variant_info(cfg.variant, &threads, &minb, &fn);
     int bps = cfg.blocks_per_sm > 0 ? cfg.blocks_per_sm : c->variant_occupancy[cfg.variant];
     if (bps > c->variant_occupancy[cfg.variant]) bps = c->variant_occupancy[cfg.variant];
+    // Shared memory for just the launched blocks per SM: the rest of the
+    // SM's 256 KB of L1 / shared memory caches nodes, triangles and the
+    // traversal stacks.  Process-wide per kernel: set when it changes.
+    if (c->smem_per_sm > 0) {
+        cudaFuncAttributes fa;
+        if (cudaFuncGetAttributes(&fa, fn) == cudaSuccess) {
+            const int64_t need = (int64_t)bps * ((int64_t)fa.sharedSizeBytes + 1024);
+            int pct = (int)((need * 100 + c->smem_per_sm - 1) / c->smem_per_sm);
+            if (pct > 100) pct = 100;
+            if (pct != c->variant_carveout[cfg.variant] &&
+                cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, pct) ==
+                    cudaSuccess)
+                c->variant_carveout[cfg.variant] = pct;
+        }
+        cudaGetLastError();
+    }
     const int64_t pixels = (int64_t)a.width * a.height;
     const int64_t warps_needed = (pixels + cfg.chunk - 1) / cfg.chunk;
     int64_t grid = (int64_t)c->num_sms * bps;
@@ -1045,10 +1063,14 @@ int32_t rt_autotune_render(rt_ctx* c, rt_scene* s, const rt_camera* cam, int32_t
     float bestt = 1e30f;
     const int chunks[] = {32, 64, 128};
     for (int v = 0; v < rt::render_variant_count(); ++v) {
+        // full residency, one and two blocks fewer (more L1 per block:
+        // the carveout follows the launched blocks), and half residency
         const int occ = c->variant_occupancy[v];
-        const int bps_list[] = {occ, occ > 1 ? (occ + 1) / 2 : occ};
-        for (int bi = 0; bi < 2; ++bi) {
-            if (bi == 1 && bps_list[1] == bps_list[0]) continue;
+        int bps_list[4] = {occ, occ - 1, occ - 2, (occ + 1) / 2};
+        for (int bi = 0; bi < 4; ++bi) {
+            bool seen = bps_list[bi] < 1;
+            for (int bj = 0; bj < bi; ++bj) seen = seen || bps_list[bj] == bps_list[bi];
+            if (seen) continue;
             for (int ch : chunks) {
                 rt_render_config cfg = {v, bps_list[bi], ch, 32};
                 std::vector<float> ts;
