@@ -248,34 +248,37 @@ __global__ void __launch_bounds__(SORT_THREADS, 4) k_batch_build(BatchBuildArgs 
     }
     grid.sync();
     stamp(A, 5);
-    // ---- stage 5: bottom-up emit + refit -----------------------------------
-    // groups of 4 consecutive triangles of one scene per thread, climbed in
-    // lockstep (emit_climb_multi); groups never straddle scenes
-    constexpr int KC = 4;
-    {
-        // group g covers scene s's triangles [4j, 4j+4): enumerate groups of
-        // every scene in order
-        uint32_t ngroups = 0;
-        for (int sc = 0; sc < nsc; ++sc) ngroups += (s_toff[sc + 1] - s_toff[sc] + KC - 1) / KC;
-        for (uint32_t g = gtid; g < ngroups; g += gthreads) {
-            // find the scene of group g (linear scan over the per-scene group counts)
-            uint32_t acc = 0;
-            int s = 0;
-            for (; s < nsc; ++s) {
-                const uint32_t gs = (s_toff[s + 1] - s_toff[s] + KC - 1) / KC;
-                if (g < acc + gs) break;
-                acc += gs;
-            }
-            const BatchScene& B = A.scenes[s];
-            emit_climb_multi<KC>((g - acc) * KC, B.n, B.keys_sorted, B.leafbox, B.nodes, B.flags,
-                                 B.rangeL, B.rangeR, B.min_leaf, B.hdr);
-        }
-    }
-    if (A.stage_ns) {
-        grid.sync();
-        stamp(A, 6);
-    }
+    // ---- stage 5: the emit, level by level (k_batch_emit launches) ---------
 }
+
+// One level of the emit over every scene that still has blocks at it: the
+// one-scene emit's blocks (emit_level, the same items, buffers and leave
+// rule), with block j of the launch taken by the scene whose range of the
+// level's blocks holds j.
+template <int C>
+__global__ void __launch_bounds__(C, C == EMIT_C0 ? RT_EMIT_MINB0 : 1) k_batch_emit(
+    const BatchScene* __restrict__ scenes, int count, int level, const uint32_t* __restrict__ off,
+    uint32_t* __restrict__ status) {
+    extern __shared__ __align__(16) unsigned char emit_smem[];
+    auto& S = *reinterpret_cast<EmitSmem<C>*>(emit_smem);
+    const int s = find_segment(off, count, blockIdx.x);
+    const BatchScene& B = scenes[s];
+    const uint32_t job = blockIdx.x - off[s];
+    const EmitBuffers E = emit_buffers(B.n, B.emit);
+    uint32_t n_in = emit_blocks0(B.n);   // blocks of the level below
+    if (level == 0) {
+        emit_level<C>(S, job, B.n, B.keys_sorted, B.leafbox, nullptr, nullptr, 0, E.items[0],
+                      E.counts[0], B.nodes, B.min_leaf, emit_leave(0, n_in), B.hdr, status);
+        return;
+    }
+    for (int l = 2; l <= level; ++l) n_in = emit_next_level(n_in);
+    const int src = (level - 1) & 1;
+    emit_level<C>(S, job, B.n, B.keys_sorted, B.leafbox, E.items[src], E.counts[src], n_in,
+                  E.items[src ^ 1], E.counts[src ^ 1], B.nodes, B.min_leaf,
+                  emit_leave(level, emit_next_level(n_in)), B.hdr, status);
+}
+
+__global__ void k_batch_stamp(unsigned long long* t) { *t = globaltimer(); }
 
 // ---------------------------------------------------------------------------
 // many-image render
@@ -602,7 +605,28 @@ cudaError_t launch_batch_build(const BatchBuildArgs& a, int grid, cudaStream_t s
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, k_batch_build, a);
+    cudaError_t e = cudaLaunchKernelEx(&cfg, k_batch_build, a);
+    if (e != cudaSuccess) return e;
+    static const cudaError_t attr0 = cudaFuncSetAttribute(
+        k_batch_emit<EMIT_C0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        (int)sizeof(EmitSmem<EMIT_C0>));
+    static const cudaError_t attr1 = cudaFuncSetAttribute(
+        k_batch_emit<EMIT_C1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        (int)sizeof(EmitSmem<EMIT_C1>));
+    if (attr0 != cudaSuccess) return attr0;
+    if (attr1 != cudaSuccess) return attr1;
+    for (int L = 0; L < a.emit_levels; ++L) {
+        if (a.emit_jobs[L] == 0) continue;
+        const uint32_t* off = a.emit_off + (size_t)L * (a.count + 1);
+        if (L == 0)
+            k_batch_emit<EMIT_C0><<<a.emit_jobs[L], EMIT_C0, sizeof(EmitSmem<EMIT_C0>), s>>>(
+                a.scenes, a.count, L, off, a.status);
+        else
+            k_batch_emit<EMIT_C1><<<a.emit_jobs[L], EMIT_C1, sizeof(EmitSmem<EMIT_C1>), s>>>(
+                a.scenes, a.count, L, off, a.status);
+    }
+    if (a.stage_ns) k_batch_stamp<<<1, 1, 0, s>>>(a.stage_ns + 6);
+    return cudaGetLastError();
 }
 
 }  // namespace rt

@@ -37,7 +37,10 @@ struct BatchScene {
     uint32_t* bounds;     // 8 words
     uint32_t* hist;       // 4 * 256 words
     uint32_t* lookback;   // passes * tiles * 256 words
+    uint8_t* emit;        // the scene's emit item buffers (emit_buffers)
 };
+
+constexpr int kMaxEmitLevels = 16;
 
 struct BatchBuildArgs {
     const BatchScene* scenes;
@@ -48,6 +51,11 @@ struct BatchBuildArgs {
     uint32_t* tile_ctr;         // one counter per pass
     uint32_t* status;
     unsigned long long* stage_ns;   // optional: globaltimer after each stage (8 entries)
+    // the emit's levels over all scenes: level L has emit_jobs[L] blocks, the
+    // blocks of scene s being emit_off[L * (count + 1) + s] ..
+    const uint32_t* emit_off;
+    int emit_levels;
+    uint32_t emit_jobs[kMaxEmitLevels];
 };
 
 struct BatchView {

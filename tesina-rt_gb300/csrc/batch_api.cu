@@ -12,6 +12,8 @@
 #include "../../include/rt_cuda.h"
 #include "batch.cuh"
 #include "ctx_internal.h"
+#include "lbvh.cuh"
+#include "lbvh_dev.cuh"
 
 #define fail rt::set_error
 
@@ -47,6 +49,10 @@ struct rt_batch {
     cudaGraphExec_t exec = nullptr;
     unsigned long long* d_stage = nullptr;  // stage timestamps when profiling is on
     bool profile = false;
+    // the emit's levels: per level, the scenes' offsets into its blocks
+    uint32_t* d_emit_off = nullptr;
+    int emit_levels = 0;
+    uint32_t emit_jobs[rt::kMaxEmitLevels] = {};
 };
 
 namespace {
@@ -68,6 +74,7 @@ void free_tables(rt_batch* b) {
     dfree(b->d_accum);
     dfree(b->d_lights);
     dfree(b->d_stage);
+    dfree(b->d_emit_off);
     if (b->exec) cudaGraphExecDestroy(b->exec);
     if (b->graph) cudaGraphDestroy(b->graph);
     b->exec = nullptr;
@@ -110,6 +117,7 @@ std::vector<rt::BatchScene> scene_table(rt_batch* b) {
         B.bounds = base;
         B.hist = base + 8;
         B.lookback = base + 8 + 1024;
+        B.emit = reinterpret_cast<uint8_t*>(s->d_scratch) + rt::lbvh_emit_offset(s->N);
     }
     return t;
 }
@@ -153,6 +161,9 @@ rt::BatchBuildArgs build_args(rt_ctx* c, rt_batch* b) {
     a.tile_ctr = b->d_ctr;
     a.status = c->d_status;
     a.stage_ns = b->profile ? b->d_stage : nullptr;
+    a.emit_off = b->d_emit_off;
+    a.emit_levels = b->emit_levels;
+    for (int L = 0; L < rt::kMaxEmitLevels; ++L) a.emit_jobs[L] = b->emit_jobs[L];
     return a;
 }
 
@@ -252,6 +263,33 @@ int32_t rt_batch_set(rt_ctx* c, rt_batch* b, const rt_batch_view* views, int32_t
     b->total_tiles = (uint32_t)tiles;
     b->total_pixels = (uint32_t)pixels;
     b->scratch_words = words;
+    // the emit's blocks per scene and level, as the one-scene build runs them
+    const size_t ns_ = b->scenes.size();
+    std::vector<uint32_t> eoff;
+    std::vector<uint32_t> below(ns_, 0);   // blocks of the level below (0: done)
+    b->emit_levels = 0;
+    for (int L = 0; L < rt::kMaxEmitLevels; ++L) {
+        uint32_t acc = 0;
+        bool any = false;
+        for (size_t k = 0; k < ns_; ++k) {
+            eoff.push_back(acc);
+            uint32_t nb;
+            if (L == 0)
+                nb = rt::emit_blocks0(b->scenes[k]->N);
+            else
+                nb = below[k] > 1 ? rt::emit_next_level(below[k]) : 0u;
+            below[k] = nb;
+            acc += nb;
+            any = any || nb > 0;
+        }
+        eoff.push_back(acc);
+        if (!any) {
+            eoff.resize(eoff.size() - (ns_ + 1));
+            break;
+        }
+        b->emit_jobs[L] = acc;
+        b->emit_levels = L + 1;
+    }
     std::vector<uint32_t> poff(1, 0);
     for (const rt_batch_view& bv : b->views) poff.push_back(poff.back() + bv.width * bv.height);
     std::vector<rt_lights> lights;
@@ -264,7 +302,8 @@ int32_t rt_batch_set(rt_ctx* c, rt_batch* b, const rt_batch_view* views, int32_t
         cudaMalloc(&b->d_pix_off, 4 * (count + 1)) ||
         cudaMalloc(&b->d_accum, 3 * sizeof(uint32_t) * std::max<size_t>(1, poff.back())) ||
         cudaMalloc(&b->d_lights, sizeof(rt_lights) * ns) ||
-        cudaMalloc(&b->d_stage, sizeof(unsigned long long) * 8)) {
+        cudaMalloc(&b->d_stage, sizeof(unsigned long long) * 8) ||
+        cudaMalloc(&b->d_emit_off, 4 * std::max<size_t>(1, eoff.size()))) {
         cudaGetLastError();
         free_tables(b);
         return fail(RT_ERR_OOM, "rt_batch_set: device allocation failed");
@@ -273,6 +312,7 @@ int32_t rt_batch_set(rt_ctx* c, rt_batch* b, const rt_batch_view* views, int32_t
     CU(cudaMemcpyAsync(b->d_tri_off, toff.data(), 4 * toff.size(), cudaMemcpyHostToDevice, cs));
     CU(cudaMemcpyAsync(b->d_tile_off, tloff.data(), 4 * tloff.size(), cudaMemcpyHostToDevice, cs));
     CU(cudaMemcpyAsync(b->d_pix_off, poff.data(), 4 * poff.size(), cudaMemcpyHostToDevice, cs));
+    CU(cudaMemcpyAsync(b->d_emit_off, eoff.data(), 4 * eoff.size(), cudaMemcpyHostToDevice, cs));
     CU(cudaMemcpyAsync(b->d_lights, lights.data(), sizeof(rt_lights) * ns, cudaMemcpyHostToDevice,
                        cs));
     int32_t r = upload_tables(c, b, cs);

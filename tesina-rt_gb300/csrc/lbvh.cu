@@ -153,21 +153,6 @@ __global__ void __launch_bounds__(256) k_refit_leaves(uint32_t n, const uint32_t
     }
 }
 
-#ifndef RT_EMIT_C0
-#define RT_EMIT_C0 512
-#endif
-#ifndef RT_EMIT_MINB0
-#define RT_EMIT_MINB0 2
-#endif
-#ifndef RT_EMIT_LEAVE0
-#define RT_EMIT_LEAVE0 128u   // runs a level-0 block may leave unjoined
-#endif
-#ifndef RT_EMIT_LEAVE1
-#define RT_EMIT_LEAVE1 64u    // the same above level 0
-#endif
-constexpr int EMIT_C0 = RT_EMIT_C0;                // triangles per level-0 block
-constexpr int EMIT_C1 = EMIT_GROUP * EMIT_FMAX;    // items per block above level 0
-
 // One level of the emit (emit_level), one block per run of items; level-0
 // blocks are kept to a register budget that lets RT_EMIT_MINB0 of them
 // share an SM.
@@ -183,19 +168,13 @@ __global__ void __launch_bounds__(C, C == EMIT_C0 ? RT_EMIT_MINB0 : 1) k_emit_le
                   min_leaf, leave, hdr, status);
 }
 
-// Blocks of level 0 and of level 1 (the two item buffers are sized for them).
-static uint32_t emit_blocks0(uint32_t n) { return (n + EMIT_C0 - 1) / EMIT_C0; }
-static uint32_t emit_blocks1(uint32_t n) { return (emit_blocks0(n) + EMIT_GROUP - 1) / EMIT_GROUP; }
 
 static size_t sort_scratch_bytes(uint32_t n, int passes) {
     const size_t tiles = ((size_t)n + SORT_TILE - 1) / SORT_TILE;
     return (sizeof(uint32_t) * (8 + 4 * 256 + 4 + (size_t)passes * tiles * 256) + 255) & ~(size_t)255;
 }
 
-static size_t emit_scratch_bytes(uint32_t n) {
-    const size_t blocks = (size_t)emit_blocks0(n) + emit_blocks1(n);
-    return blocks * EMIT_FMAX * sizeof(EmitItem) + ((blocks * sizeof(uint32_t) + 255) & ~(size_t)255);
-}
+static size_t emit_scratch_bytes(uint32_t n) { return emit_buffers_bytes(n); }
 
 // The emit's levels: level 0 over triangles, then levels over the items left
 // by EMIT_GROUP blocks each until a single block reaches the root.  Item
@@ -210,25 +189,18 @@ static cudaError_t launch_emit(const LbvhArgs& a, uint8_t* emit_scratch, cudaStr
         (int)sizeof(EmitSmem<EMIT_C1>));
     if (attr0 != cudaSuccess) return attr0;
     if (attr1 != cudaSuccess) return attr1;
-    const uint32_t nb0 = emit_blocks0(n), nb1 = emit_blocks1(n);
-    EmitItem* items[2];
-    uint32_t* counts[2];
-    items[0] = reinterpret_cast<EmitItem*>(emit_scratch);
-    items[1] = items[0] + (size_t)nb0 * EMIT_FMAX;
-    counts[0] = reinterpret_cast<uint32_t*>(items[1] + (size_t)nb1 * EMIT_FMAX);
-    counts[1] = counts[0] + nb0;
-    // level-0 blocks leave up to EMIT_FMAX runs to level 1 unless they are
-    // the only block
+    const uint32_t nb0 = emit_blocks0(n);
+    const EmitBuffers B = emit_buffers(n, emit_scratch);
     k_emit_level<EMIT_C0><<<nb0, EMIT_C0, sizeof(EmitSmem<EMIT_C0>), s>>>(
-        n, a.keys_sorted, a.leafbox, nullptr, nullptr, 0, items[0], counts[0], a.nodes,
-        a.min_leaf, nb0 > 1 ? RT_EMIT_LEAVE0 : 32u, a.hdr, a.status);
+        n, a.keys_sorted, a.leafbox, nullptr, nullptr, 0, B.items[0], B.counts[0], a.nodes,
+        a.min_leaf, emit_leave(0, nb0), a.hdr, a.status);
     uint32_t n_in = nb0;
     int src = 0;
     while (n_in > 1) {
-        const uint32_t g = (n_in + EMIT_GROUP - 1) / EMIT_GROUP;
+        const uint32_t g = emit_next_level(n_in);
         k_emit_level<EMIT_C1><<<g, EMIT_C1, sizeof(EmitSmem<EMIT_C1>), s>>>(
-            n, a.keys_sorted, a.leafbox, items[src], counts[src], n_in, items[src ^ 1],
-            counts[src ^ 1], a.nodes, a.min_leaf, g > 1 ? RT_EMIT_LEAVE1 : 32u, a.hdr, a.status);
+            n, a.keys_sorted, a.leafbox, B.items[src], B.counts[src], n_in, B.items[src ^ 1],
+            B.counts[src ^ 1], a.nodes, a.min_leaf, emit_leave(1, g), a.hdr, a.status);
         n_in = g;
         src ^= 1;
     }
@@ -249,6 +221,8 @@ static int grid_for(uint32_t n, int threads, int max_blocks) {
 size_t lbvh_scratch_bytes(uint32_t n, int passes) {
     return sort_scratch_bytes(n, passes) + emit_scratch_bytes(n);
 }
+
+size_t lbvh_emit_offset(uint32_t n) { return sort_scratch_bytes(n, 4); }
 
 cudaError_t lbvh_build(const LbvhArgs& a, cudaStream_t s) {
     const uint32_t n = a.n;
@@ -285,7 +259,7 @@ cudaError_t lbvh_build(const LbvhArgs& a, cudaStream_t s) {
     k_permute<<<grid_for(n, 256, sms * 16), 256, 0, s>>>(n, a.vals_sorted, a.idx_in, a.map_in,
                                                          a.orig_in, a.pos, a.idx_out, a.map_out,
                                                          a.orig_out, a.tris, a.leafbox);
-    return launch_emit(a, reinterpret_cast<uint8_t*>(a.scratch) + sort_scratch_bytes(n, passes), s);
+    return launch_emit(a, reinterpret_cast<uint8_t*>(a.scratch) + lbvh_emit_offset(n), s);
 }
 
 size_t radix_scratch_words(uint32_t n, int passes) {
@@ -327,10 +301,9 @@ cudaError_t lbvh_refit(const LbvhArgs& a, cudaStream_t s) {
     const uint32_t n = a.n;
     k_refit_leaves<<<grid_for(n, 256, a.num_sms * 16), 256, 0, s>>>(n, a.idx_out, a.pos, a.tris,
                                                                     a.leafbox);
-    // the climb is deterministic in the sorted keys, so rerunning it on the
-    // same keys reproduces the same topology with the new boxes; the emit's
-    // item buffers follow the sort scratch of the build (4 passes)
-    return launch_emit(a, reinterpret_cast<uint8_t*>(a.scratch) + sort_scratch_bytes(n, 4), s);
+    // the emit is deterministic in the sorted keys, so rerunning it on the
+    // same keys reproduces the same topology with the new boxes
+    return launch_emit(a, reinterpret_cast<uint8_t*>(a.scratch) + lbvh_emit_offset(n), s);
 }
 
 }  // namespace rt

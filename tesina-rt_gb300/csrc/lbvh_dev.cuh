@@ -460,6 +460,34 @@ __device__ __forceinline__ void emit_climb(uint32_t i, uint32_t n,
 constexpr int EMIT_FMAX = 128;   // items a block may leave
 constexpr int EMIT_GROUP = 8;    // blocks of one level gathered by a block of the next
 
+#ifndef RT_EMIT_C0
+#define RT_EMIT_C0 512
+#endif
+#ifndef RT_EMIT_MINB0
+#define RT_EMIT_MINB0 2
+#endif
+#ifndef RT_EMIT_LEAVE0
+#define RT_EMIT_LEAVE0 128u   // runs a level-0 block may leave unjoined
+#endif
+#ifndef RT_EMIT_LEAVE1
+#define RT_EMIT_LEAVE1 64u    // the same above level 0
+#endif
+constexpr int EMIT_C0 = RT_EMIT_C0;                // triangles per level-0 block
+constexpr int EMIT_C1 = EMIT_GROUP * EMIT_FMAX;    // items per block above level 0
+
+// Blocks of level 0 of an n-triangle scene, and of the level above nb blocks.
+__host__ __device__ __forceinline__ uint32_t emit_blocks0(uint32_t n) {
+    return (n + EMIT_C0 - 1) / EMIT_C0;
+}
+__host__ __device__ __forceinline__ uint32_t emit_next_level(uint32_t nb) {
+    return (nb + EMIT_GROUP - 1) / EMIT_GROUP;
+}
+// Runs a block of a level with `blocks` blocks may leave unjoined (a level of
+// one block is the root's and joins everything).
+__host__ __device__ __forceinline__ uint32_t emit_leave(int level, uint32_t blocks) {
+    return blocks > 1 ? (level == 0 ? RT_EMIT_LEAVE0 : RT_EMIT_LEAVE1) : 32u;
+}
+
 // An item: leaf range, keys at its ends, box, ref / count, and the augmented
 // delta of the boundary before it.
 struct __align__(16) EmitItem {
@@ -469,6 +497,27 @@ struct __align__(16) EmitItem {
     uint64_t db;
     uint32_t pad[2];
 };
+
+// A scene's emit items in its emit scratch `base`: level 0 writes buffer A,
+// level 1 B, level 2 A, ...; A holds up to EMIT_FMAX items per level-0 block,
+// B per level-1 block, then the item counts of A and of B.
+struct EmitBuffers {
+    EmitItem* items[2];
+    uint32_t* counts[2];
+};
+__host__ __device__ __forceinline__ EmitBuffers emit_buffers(uint32_t n, uint8_t* base) {
+    const uint32_t nb0 = emit_blocks0(n), nb1 = emit_next_level(nb0);
+    EmitBuffers b;
+    b.items[0] = reinterpret_cast<EmitItem*>(base);
+    b.items[1] = b.items[0] + (size_t)nb0 * EMIT_FMAX;
+    b.counts[0] = reinterpret_cast<uint32_t*>(b.items[1] + (size_t)nb1 * EMIT_FMAX);
+    b.counts[1] = b.counts[0] + nb0;
+    return b;
+}
+__host__ __device__ __forceinline__ size_t emit_buffers_bytes(uint32_t n) {
+    const size_t blocks = (size_t)emit_blocks0(n) + emit_next_level(emit_blocks0(n));
+    return blocks * EMIT_FMAX * sizeof(EmitItem) + ((blocks * sizeof(uint32_t) + 255) & ~(size_t)255);
+}
 
 struct WarpItem {
     uint32_t l, r, kl, kr;
