@@ -100,7 +100,6 @@ __global__ void __launch_bounds__(SORT_THREADS, 4) k_batch_build(BatchBuildArgs 
         const BatchScene& B = A.scenes[sc];
         const size_t words = (size_t)B.passes * (s_tileoff[sc + 1] - s_tileoff[sc]) * 256;
         for (size_t i = gtid; i < words; i += gthreads) B.lookback[i] = 0;
-        for (uint32_t i = gtid; i + 1 < B.n; i += gthreads) B.flags[i] = 0;
     }
     if (gtid < 4) A.tile_ctr[gtid] = 0;
     grid.sync();

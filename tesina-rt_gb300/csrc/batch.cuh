@@ -30,9 +30,6 @@ struct BatchScene {
     float4* tris;
     float4* leafbox;
     float4* nodes;
-    uint32_t* flags;
-    uint32_t* rangeL;
-    uint32_t* rangeR;
     BvhHeader* hdr;
     uint32_t* bounds;     // 8 words
     uint32_t* hist;       // 4 * 256 words

@@ -109,9 +109,6 @@ std::vector<rt::BatchScene> scene_table(rt_batch* b) {
         B.tris = s->d_tris;
         B.leafbox = s->d_leafbox;
         B.nodes = s->d_nodes;
-        B.flags = s->d_flags;
-        B.rangeL = s->d_rangeL;
-        B.rangeR = s->d_rangeR;
         B.hdr = s->d_hdr;
         uint32_t* base = b->d_scratch + b->scratch_at[k];
         B.bounds = base;

@@ -99,9 +99,6 @@ void free_build(rt_scene* s) {
     sfree(s, s->d_tris);
     sfree(s, s->d_leafbox);
     sfree(s, s->d_nodes);
-    sfree(s, s->d_flags);
-    sfree(s, s->d_rangeL);
-    sfree(s, s->d_rangeR);
     sfree(s, s->d_hdr);
     sfree(s, s->d_scratch);
     s->buildN = 0;
@@ -221,9 +218,7 @@ int32_t scene_ensure_build(rt_scene* s) {
         salloc_n(s, &s->d_keys1, n) || salloc_n(s, &s->d_vals1, n) ||
         salloc_n(s, &s->d_keys_sorted, n) || salloc_n(s, &s->d_vals_sorted, n) ||
         salloc_n(s, &s->d_tris, 3 * (size_t)n) || salloc_n(s, &s->d_leafbox, 2 * (size_t)n) ||
-        salloc_n(s, &s->d_nodes, 4 * nn) || salloc_n(s, &s->d_flags, nn) ||
-        salloc_n(s, &s->d_rangeL, nn) || salloc_n(s, &s->d_rangeR, nn) ||
-        salloc_n(s, &s->d_hdr, 1) || salloc(s, &s->d_scratch, need_scratch)) {
+        salloc_n(s, &s->d_nodes, 4 * nn) || salloc_n(s, &s->d_hdr, 1) || salloc(s, &s->d_scratch, need_scratch)) {
         cudaGetLastError();
         free_build(s);
         return fail(RT_ERR_OOM, "device allocation of LBVH buffers for %u triangles failed", n);
@@ -673,9 +668,6 @@ static rt::LbvhArgs lbvh_args(rt_ctx* c, rt_scene* s) {
     a.tris = s->d_tris;
     a.leafbox = s->d_leafbox;
     a.nodes = s->d_nodes;
-    a.flags = s->d_flags;
-    a.rangeL = s->d_rangeL;
-    a.rangeR = s->d_rangeR;
     a.hdr = s->d_hdr;
     a.scratch = s->d_scratch;
     a.status = c->d_status;

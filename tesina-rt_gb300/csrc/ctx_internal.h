@@ -63,9 +63,6 @@ struct rt_scene {
     float4* d_tris = nullptr;
     float4* d_leafbox = nullptr;
     float4* d_nodes = nullptr;
-    uint32_t* d_flags = nullptr;
-    uint32_t* d_rangeL = nullptr;
-    uint32_t* d_rangeR = nullptr;
     rt::BvhHeader* d_hdr = nullptr;
     uint32_t* d_scratch = nullptr;
     size_t scratch_bytes = 0;

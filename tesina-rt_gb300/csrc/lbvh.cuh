@@ -31,9 +31,6 @@ struct LbvhArgs {
     float4* tris;             // 3 float4 per sorted triangle
     float4* leafbox;          // 2 float4 per sorted triangle
     float4* nodes;            // 4 float4 per radix-tree node (n - 1)
-    uint32_t* flags;          // n - 1 arrival counters
-    uint32_t* rangeL;         // n - 1
-    uint32_t* rangeR;         // n - 1
     BvhHeader* hdr;
     uint32_t* scratch;        // lbvh_scratch_bytes(n, passes)
     uint32_t* status;         // device status word (RT_DEV_* bits)

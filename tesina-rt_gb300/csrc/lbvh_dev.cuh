@@ -347,88 +347,6 @@ __device__ __forceinline__ uint64_t delta(const uint32_t* __restrict__ k, uint32
     return ((uint64_t)x << 32) | (uint64_t)(i ^ (i + 1));
 }
 
-// Bottom-up emit + refit from sorted triangle i of an n-triangle scene: the
-// thread climbs while it is the second child to arrive.  A radix-tree node
-// [L, R] is an interior node of the reference's tree iff R - L + 1 >=
-// min_leaf + 3 (find_middle's unsigned test last - first - 1 <= min_leaf,
-// bvh-builder.cl:501) and its keys are not all equal (the bit loop of
-// :515-525); otherwise it is a leaf, or part of one.  The reference's split
-// (highest differing bit, first index with the bit set) is the radix tree's
-// split, so both trees have the same ranges.
-__device__ __forceinline__ void emit_climb(uint32_t i, uint32_t n,
-                                           const uint32_t* __restrict__ skeys,
-                                           const float4* __restrict__ leafbox,
-                                           float4* __restrict__ nodes, uint32_t* __restrict__ flags,
-                                           uint32_t* __restrict__ rangeL,
-                                           uint32_t* __restrict__ rangeR, int min_leaf,
-                                           BvhHeader* __restrict__ hdr) {
-    float4 lo = leafbox[2 * (size_t)i], hi = leafbox[2 * (size_t)i + 1];
-    if (n == 1) {
-        hdr->root_ref = 0;
-        hdr->root_cnt = 1;
-        hdr->n_tris = 1;
-        hdr->root_lo = lo;
-        hdr->root_hi = hi;
-        return;
-    }
-    uint32_t l = i, r = i;
-    int32_t ref = (int32_t)i, cnt = 1;
-    for (;;) {
-        bool is_left;
-        uint32_t p;
-        if (l == 0 || (r != n - 1 && delta(skeys, r) < delta(skeys, l - 1))) {
-            p = r;
-            is_left = true;
-        } else {
-            p = l - 1;
-            is_left = false;
-        }
-        float* rec = reinterpret_cast<float*>(nodes + 4 * (size_t)p);
-        int* rec_i = reinterpret_cast<int*>(nodes + 4 * (size_t)p + 3);
-        if (is_left) {
-            nodes[4 * (size_t)p] = make_float4(lo.x, lo.y, lo.z, hi.x);
-            *reinterpret_cast<float2*>(rec + 4) = make_float2(hi.y, hi.z);
-            rec_i[0] = ref;
-            rec_i[2] = cnt;
-            rangeL[p] = l;
-        } else {
-            *reinterpret_cast<float2*>(rec + 6) = make_float2(lo.x, lo.y);
-            nodes[4 * (size_t)p + 2] = make_float4(lo.z, hi.x, hi.y, hi.z);
-            rec_i[1] = ref;
-            rec_i[3] = cnt;
-            rangeR[p] = r;
-        }
-        if (atomic_add_acq_rel(&flags[p], 1u) == 0) return;   // the sibling finishes p
-        const float4 n0 = __ldcg(&nodes[4 * (size_t)p]);
-        const float4 n1 = __ldcg(&nodes[4 * (size_t)p + 1]);
-        const float4 n2 = __ldcg(&nodes[4 * (size_t)p + 2]);
-        const uint32_t L = is_left ? l : __ldcg(&rangeL[p]);
-        const uint32_t R = is_left ? __ldcg(&rangeR[p]) : r;
-        // merge_bbox(left, right): lo = fmin(left.lo, right.lo), hi = fmax(...)
-        lo = make_float4(fminf(n0.x, n1.z), fminf(n0.y, n1.w), fminf(n0.z, n2.x), 0.f);
-        hi = make_float4(fmaxf(n0.w, n2.y), fmaxf(n1.x, n2.z), fmaxf(n1.y, n2.w), 0.f);
-        const uint32_t count = R - L + 1;
-        const bool interior =
-            count >= (uint32_t)min_leaf + 3u && __ldg(&skeys[L]) != __ldg(&skeys[R]);
-        if (interior) {
-            ref = (int32_t)p;
-            cnt = 0;
-        } else {
-            ref = (int32_t)L;
-            cnt = (int32_t)count;
-        }
-        l = L;
-        r = R;
-        if (L == 0 && R == n - 1) {
-            hdr->root_ref = ref;
-            hdr->root_cnt = cnt;
-            hdr->n_tris = n;
-            hdr->root_lo = lo;
-            hdr->root_hi = hi;
-            return;
-        }
-    }
-}
 
 // ---------------------------------------------------------------------------
 // Multi-level emit + refit, warp-synchronous.  The tree is built bottom-up
@@ -447,9 +365,16 @@ __device__ __forceinline__ void emit_climb(uint32_t i, uint32_t n,
 // they hang off the chains of nodes crossing its two ends, each at most 64
 // deep (32 key bits + 32 index bits).
 //
-// The tree is the one of emit_climb.  With d[j] the augmented delta of the
-// boundary before item j of a chunk and d[c] the boundary after its last
-// item (D(-1) = D(n-1) = max), a run j..b is a left child iff d[b+1] < d[j];
+// The tree is the binary radix tree of the sorted keys (Karras), collapsed
+// to the reference's leaf rule: a node [L, R] is an interior node of the
+// reference's tree iff R - L + 1 >= min_leaf + 3 (find_middle's unsigned test
+// last - first - 1 <= min_leaf, bvh-builder.cl:501) and its keys are not all
+// equal (the bit loop of :515-525); otherwise it is a leaf, or part of one.
+// The reference's split (highest differing bit, first index with the bit
+// set) is the radix tree's split, so both trees have the same ranges.  With
+// d[j] the augmented delta of the boundary before item j of a chunk and d[c]
+// the boundary after its last item (D(-1) = D(n-1) = max), a run j..b is a
+// left child iff d[b+1] < d[j];
 // its parent stays in the chunk iff max d[b+2..c] > d[b+1] (the parent's
 // range ends at the first boundary above d[b+1]); a right child's parent
 // stays iff max d[0..j-1] > d[j].  Above the leftovers of a chunk, the
@@ -955,104 +880,5 @@ __device__ __forceinline__ void emit_level(EmitSmem<C>& S, uint32_t blk, uint32_
     }
 }
 
-// K climbs of emit_climb advanced in lockstep by one thread: one release
-// fence before the K arrival counters are bumped and one acquire fence before
-// the winners read their siblings, instead of one ordering point per climber
-// and level.  Used where few threads must cover many triangles (the
-// persistent many-scene build).  Climbers are the triangles first..first+K-1
-// of one scene (those >= n are idle).
-template <int K>
-__device__ __forceinline__ void emit_climb_multi(uint32_t first, uint32_t n,
-                                                 const uint32_t* __restrict__ skeys,
-                                                 const float4* __restrict__ leafbox,
-                                                 float4* __restrict__ nodes,
-                                                 uint32_t* __restrict__ flags,
-                                                 uint32_t* __restrict__ rangeL,
-                                                 uint32_t* __restrict__ rangeR, int min_leaf,
-                                                 BvhHeader* __restrict__ hdr) {
-    if (n == 1) {
-        if (first == 0) emit_climb(0, 1, skeys, leafbox, nodes, flags, rangeL, rangeR, min_leaf, hdr);
-        return;
-    }
-    uint32_t l[K], r[K], p[K];
-    int32_t ref[K], cnt[K];
-    float4 lo[K], hi[K];
-    bool alive[K], left[K];
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-        const uint32_t i = first + k;
-        alive[k] = i < n;
-        l[k] = r[k] = i;
-        ref[k] = (int32_t)i;
-        cnt[k] = 1;
-        if (alive[k]) {
-            lo[k] = leafbox[2 * (size_t)i];
-            hi[k] = leafbox[2 * (size_t)i + 1];
-        }
-    }
-    for (;;) {
-        bool any = false;
-#pragma unroll
-        for (int k = 0; k < K; ++k) {
-            if (!alive[k]) continue;
-            any = true;
-            if (l[k] == 0 || (r[k] != n - 1 && delta(skeys, r[k]) < delta(skeys, l[k] - 1))) {
-                p[k] = r[k];
-                left[k] = true;
-            } else {
-                p[k] = l[k] - 1;
-                left[k] = false;
-            }
-            float* rec = reinterpret_cast<float*>(nodes + 4 * (size_t)p[k]);
-            int* rec_i = reinterpret_cast<int*>(nodes + 4 * (size_t)p[k] + 3);
-            if (left[k]) {
-                nodes[4 * (size_t)p[k]] = make_float4(lo[k].x, lo[k].y, lo[k].z, hi[k].x);
-                *reinterpret_cast<float2*>(rec + 4) = make_float2(hi[k].y, hi[k].z);
-                rec_i[0] = ref[k];
-                rec_i[2] = cnt[k];
-                rangeL[p[k]] = l[k];
-            } else {
-                *reinterpret_cast<float2*>(rec + 6) = make_float2(lo[k].x, lo[k].y);
-                nodes[4 * (size_t)p[k] + 2] = make_float4(lo[k].z, hi[k].x, hi[k].y, hi[k].z);
-                rec_i[1] = ref[k];
-                rec_i[3] = cnt[k];
-                rangeR[p[k]] = r[k];
-            }
-        }
-        if (!any) return;
-        __threadfence();   // release every record written above
-#pragma unroll
-        for (int k = 0; k < K; ++k)
-            if (alive[k] && atomicAdd(&flags[p[k]], 1u) == 0) alive[k] = false;
-        __threadfence();   // acquire the siblings' records
-#pragma unroll
-        for (int k = 0; k < K; ++k) {
-            if (!alive[k]) continue;
-            const size_t q = p[k];
-            const float4 n0 = __ldcg(&nodes[4 * q]);
-            const float4 n1 = __ldcg(&nodes[4 * q + 1]);
-            const float4 n2 = __ldcg(&nodes[4 * q + 2]);
-            const uint32_t L = left[k] ? l[k] : __ldcg(&rangeL[q]);
-            const uint32_t R = left[k] ? __ldcg(&rangeR[q]) : r[k];
-            lo[k] = make_float4(fminf(n0.x, n1.z), fminf(n0.y, n1.w), fminf(n0.z, n2.x), 0.f);
-            hi[k] = make_float4(fmaxf(n0.w, n2.y), fmaxf(n1.x, n2.z), fmaxf(n1.y, n2.w), 0.f);
-            const uint32_t count = R - L + 1;
-            const bool interior =
-                count >= (uint32_t)min_leaf + 3u && __ldg(&skeys[L]) != __ldg(&skeys[R]);
-            ref[k] = interior ? (int32_t)q : (int32_t)L;
-            cnt[k] = interior ? 0 : (int32_t)count;
-            l[k] = L;
-            r[k] = R;
-            if (L == 0 && R == n - 1) {
-                hdr->root_ref = ref[k];
-                hdr->root_cnt = cnt[k];
-                hdr->n_tris = n;
-                hdr->root_lo = lo[k];
-                hdr->root_hi = hi[k];
-                alive[k] = false;
-            }
-        }
-    }
-}
 
 }  // namespace rt

@@ -39,6 +39,7 @@
 #include "../../include/rt_cuda.h"
 #include "batch.cuh"
 #include "ctx_internal.h"
+#include "lbvh.cuh"
 #include "trace.cuh"
 
 #define fail rt::set_error
@@ -185,10 +186,10 @@ namespace {
 
 uint64_t scene_bytes(const rt_scene_desc* d) {
     const uint64_t V = d->vertex_count, N = d->triangle_count, M = d->material_count;
-    const uint64_t tiles = (N + 4095) / 4096;
     return 32 * V + 40 * N + 32 * M                     // geometry, both orders
-           + N * (24 + 48 + 32 + 64 + 12)                // sort, triangles, leaves, nodes, flags
-           + 4 * (8 + 1024 + 4 + 4 * tiles * 256) + 4096;
+           + N * (24 + 48 + 32 + 64)                     // sort, triangles, leaves, nodes
+           + rt::lbvh_scratch_bytes((uint32_t)N, 4)      // radix and emit scratch
+           + 4096;
 }
 
 // Scene memory: a device pool that keeps what is freed for later uploads.
