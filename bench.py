@@ -273,6 +273,53 @@ SERVED_KEYS = ("p50_ms", "p99_ms", "mean_ms", "max_ms", "mrays_s", "req_s", "ray
                "evicted", "resident_scenes")
 
 
+def measure_refit(ctx, torch, frames=20, warmup=3):
+    """Refit-only frames (the reference's bvh_refit_only mode,
+    renderer.cpp:53-70) with device-side animation (mangle, mangler.cl:12-32,
+    run before each frame as rt-wave.cpp:141-167 runs it, wave height 0.2):
+    the mid-scale terrain built once, then per frame mangle + refit + the
+    1920x1080 depth-4 render, L2 flushed between frames.  Per-phase CUDA
+    events on the frame's stream; Mrays/s counts primary + secondary rays."""
+    from rtgb import capi, scenes
+    wl = scenes.workload_mid()
+    sc = wl["terrain"].scene(0)
+    stream = torch.cuda.Stream()
+    sh = C.c_void_p(stream.cuda_stream)
+    g = capi.Scene(ctx, sc)
+    g.build(30, 1, stream=sh)
+    w, h, nb = wl["width"], wl["height"], wl["max_bounces"]
+    rgba = ctx.alloc(4 * w * h)
+    stats = ctx.alloc(32)
+    flush = ctx.alloc(256 << 20)
+    t_m, t_r, t_d = [], [], []
+    stats.zero(sh)
+    for f in range(warmup + frames):
+        arg = 1.0 + f
+        flush.zero(sh)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        ev[0].record(stream)
+        g.mangle(arg, arg - 1.0, 0.2, stream=sh)
+        ev[1].record(stream)
+        g.refit(stream=sh)
+        ev[2].record(stream)
+        g.render(wl["camera"], w, h, nb, rgba, None, stats if f >= warmup else None, stream=sh)
+        ev[3].record(stream)
+        stream.synchronize()
+        if f >= warmup:
+            t_m.append(ev[0].elapsed_time(ev[1]))
+            t_r.append(ev[1].elapsed_time(ev[2]))
+            t_d.append(ev[2].elapsed_time(ev[3]))
+    st = stats.read(np.uint64)
+    rays = int(st[0] + st[1])
+    total = sum(t_m) + sum(t_r) + sum(t_d)
+    mr = statistics.median(t_r)
+    return {"workload": wl["name"] + "_mangle_refit", "triangles": sc.n_tris,
+            "vertices": sc.n_verts, "frames": frames, "mangle_ms": statistics.median(t_m),
+            "refit_ms": mr, "refit_mtri_s": sc.n_tris / (mr * 1e-3) / 1e6,
+            "render_ms": statistics.median(t_d), "frame_ms": total / frames,
+            "mrays_s": rays / (total * 1e-3) / 1e6, "device_status": ctx.device_status()}
+
+
 def measure_served(ctx, rates=(2000, 1000, 300, 50), n_req=400, seed=5):
     """Served workload: 32 resident scenes (soups and fBm fields alternating,
     10k-2M triangles log-uniform), a 120 GB admission budget and a scene cap
@@ -544,6 +591,12 @@ def run_gpu(args):
             stress = measure_stress(ctx, torch)
         except Exception as e:
             stress = {"error": str(e)}
+    refit_leg = None
+    if world == 1 and not args.no_refit:
+        try:
+            refit_leg = measure_refit(ctx, torch)
+        except Exception as e:
+            refit_leg = {"error": str(e)}
     served_leg = None
     if world == 1 and not args.no_served:
         try:
@@ -573,6 +626,7 @@ def run_gpu(args):
            "batched": batched,
            "served": served_leg,
            "stress": stress,
+           "refit": refit_leg,
            "e2e": {"value": e2e_value, "unit": UNIT,
                    "h2d_bytes_per_step": 2 * 16 * V,
                    "d2h_bytes_per_step": 4 * w * h + 32,
@@ -600,6 +654,7 @@ def main():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--no-stress", action="store_true")
+    ap.add_argument("--no-refit", action="store_true")
     ap.add_argument("--render-variant", type=int, default=None,
                     help="render kernel variant instead of the autotuner's pick")
     ap.add_argument("--render-blocks", type=int, default=0, help="resident blocks per SM (0: all)")

@@ -223,6 +223,14 @@ RT_API int32_t rt_scene_update_vertices(rt_ctx* ctx, rt_scene* scene, const floa
 /* Same, from device memory. */
 RT_API int32_t rt_scene_update_vertices_device(rt_ctx* ctx, rt_scene* scene, const float* d_pos4,
                                         const float* d_nrm4, uint32_t vertex_count, rt_stream s);
+/* Device-side animation: the mangle kernel (src/kernel/mangler.cl:12-32) on the
+ * scene's vertices, as the reference's wave demo runs it before each frame
+ * (src/rt/rt-wave.cpp:141-167; height 0.2 at :408-413): position.y = height *
+ * sin(0.33 arg + x) * cos(0.57 arg + z), normal.x / normal.z from per-vertex
+ * phases.  last_arg is accepted and unused, as in the kernel.  Follow with
+ * rt_bvh_refit_lbvh (the refit-only mode, renderer.cpp:53-70) or a rebuild. */
+RT_API int32_t rt_scene_mangle(rt_ctx* ctx, rt_scene* scene, float arg, float last_arg,
+                               float height, rt_stream s);
 RT_API int32_t rt_scene_set_lights(rt_ctx* ctx, rt_scene* scene, const rt_lights* lights);
 /* Device buffers of the scene (reference: Scene::index_mem(), material_map_mem()).
  * After a build, indices and material map are permuted into sorted order, as

@@ -23,7 +23,9 @@ CXX = os.environ.get("CXX", "g++")
 FLAGS = ["-std=c++17", "-O3", "-fPIC", "-ffp-contract=off", "-fno-strict-aliasing", "-pthread"]
 
 REF_UNITS = ["ref_bvh", "ref_sort", "ref_trace", "ref_shadow", "ref_shade",
-             "ref_secondary", "ref_primary", "ref_driver"]
+             "ref_secondary", "ref_primary", "ref_driver", "ref_mangle"]
+# per-unit flags: mangler.cl has no fp64 pragma, so its constants are floats
+REF_UNIT_FLAGS = {"ref_mangle": ["-fsingle-precision-constant"]}
 
 
 def _run(cmd):
@@ -69,8 +71,8 @@ def build_ref(force=False):
     def one(unit):
         src = os.path.join(shim, unit + ".cpp")
         obj = os.path.join(outdir, unit + ".o")
-        _run([CXX] + FLAGS + ["-fno-semantic-interposition", "-w", "-I", kdir, "-c", src,
-                              "-o", obj])
+        _run([CXX] + FLAGS + REF_UNIT_FLAGS.get(unit, []) +
+             ["-fno-semantic-interposition", "-w", "-I", kdir, "-c", src, "-o", obj])
         return obj
 
     with ThreadPoolExecutor(max_workers=len(REF_UNITS)) as ex:

@@ -58,6 +58,13 @@ class Oracle(_Lib):
         self.fp64_t_of = b(L, "orc_fp64_t_of", C.c_int, [P, P, I32, P, P])
         self.emit_keys_raw = b(L, "orc_emit_keys", C.c_int, [P, U32, C.c_int, C.c_int, P, U32,
                                                               C.POINTER(U32)])
+        self.mangle_raw = b(L, "orc_mangle", C.c_int, [P, P, U32, F, F, F])
+
+    def mangle(self, pos4, nrm4, arg, last_arg=-1000.0, height=0.2):
+        """mangle on copies of float32 [V, 4] positions / normals."""
+        p, n = np.array(pos4, np.float32, copy=True), np.array(nrm4, np.float32, copy=True)
+        self.mangle_raw(_p(p), _p(n), p.shape[0], arg, last_arg, height)
+        return p, n
 
     def emit_keys(self, sorted_keys, depth=30, min_leaf=1):
         k = np.ascontiguousarray(sorted_keys, np.uint32)
@@ -201,6 +208,12 @@ class RefKernels(_Lib):
                                [P, P, I32, P, P, I32, C.POINTER(I32)])
         self.render = b(L, "refd_render", C.c_int,
                         [P, P, I32, I32, I32, SZ, SZ, SZ, P, P, C.c_int])
+        self.mangle_raw = b(L, "refk_mangle", None, [P, P, U32, F, F, F])
+
+    def mangle(self, pos4, nrm4, arg, last_arg=-1000.0, height=0.2):
+        p, n = np.array(pos4, np.float32, copy=True), np.array(nrm4, np.float32, copy=True)
+        self.mangle_raw(_p(p), _p(n), p.shape[0], arg, last_arg, height)
+        return p, n
 
     def new_scene(self, sc):
         h = self.scene_new(_p(sc.pos4), _p(sc.nrm4), sc.n_verts, _p(sc.idx), sc.n_tris,

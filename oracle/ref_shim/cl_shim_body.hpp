@@ -121,6 +121,9 @@ inline float min(float x, float y) { return (y < x) ? y : x; }
 inline int max(int x, int y) { return (x < y) ? y : x; }
 inline int min(int x, int y) { return (y < x) ? y : x; }
 inline float clamp(float x, float lo, float hi) { return fmin(fmax(x, lo), hi); }
+inline float sin(float a) { return std::sin(a); }
+inline float cos(float a) { return std::cos(a); }
+inline float fmod(float a, float b) { return std::fmod(a, b); }
 
 /* ---- vector built-ins ---------------------------------------------------- */
 inline float3 fmax(float3 a, float3 b) { return float3(fmax(a.x, b.x), fmax(a.y, b.y), fmax(a.z, b.z)); }

@@ -21,6 +21,7 @@
  *   Primary      src/kernel/primary-ray-generator.cl:27-103.
  *   Framebuffer  src/kernel/framebuffer.cl:30-54 + RGBA8 UNORM conversion.
  *   Renderer     src/rt/renderer.cpp:113-214 (tile loop, bounce loop).
+ *   Animation    src/kernel/mangler.cl:12-32 (mangle).
  *
  * Documented restatement choices (identical in the CUDA path):
  *   normalize(v) = v * (1 / sqrt(dot(v, v)))  (zero vector stays zero);
@@ -647,6 +648,25 @@ orc_scene* orc_scene_new(const float* pos4, const float* nrm4, uint32_t V, const
 }
 
 void orc_scene_free(orc_scene* s) { delete s; }
+
+/* mangle (src/kernel/mangler.cl:12-32), the per-frame vertex animation of
+ * src/rt/rt-wave.cpp:141-167, on float4 positions / normals (xyz).  The
+ * kernel has no fp64 pragma, so its constants are single precision; index
+ * is the vertex number as an int, converted to float by the products. */
+int orc_mangle(float* pos4, float* nrm4, uint32_t V, float arg, float last_arg, float height) {
+    (void)last_arg;   /* an argument of the kernel that its body does not read */
+    for (uint32_t i = 0; i < V; ++i) {
+        float* p = pos4 + 4 * (size_t)i;
+        float* q = nrm4 + 4 * (size_t)i;
+        const int index = (int)i;
+        p[1] = height * std::sin(0.33f * arg + p[0]) * std::cos(0.57f * arg + p[2]);
+        const float xfactor = (0.33f + std::fmod(0.01238431f * (float)index, 0.23467f)) * arg;
+        const float zfactor = (0.57f + std::fmod(0.02173f * (float)index, 0.3237247f)) * arg;
+        q[0] = std::cos(xfactor + p[0]);
+        q[2] = -std::sin(zfactor + p[2]);
+    }
+    return 0;
+}
 
 int orc_set_positions(orc_scene* s, const float* pos4, const float* nrm4) {
     std::memcpy(s->pos.data(), pos4, sizeof(float) * 4 * (size_t)s->V);

@@ -603,6 +603,18 @@ int32_t rt_scene_update_vertices_device(rt_ctx* c, rt_scene* s, const float* pos
     return RT_OK;
 }
 
+int32_t rt_scene_mangle(rt_ctx* c, rt_scene* s, float arg, float last_arg, float height,
+                        rt_stream stream) {
+    (void)last_arg;
+    if (!c || !s) return fail(RT_ERR_INVALID, "rt_scene_mangle: null argument");
+    if (s->V == 0) return fail(RT_ERR_INVALID, "rt_scene_mangle: scene has no vertices");
+    cudaStream_t cs = st(c, stream);
+    CU(scene_write_begin(s, cs));
+    CU(rt::launch_mangle(s->d_pos, s->d_nrm, s->V, arg, height, cs));
+    CU(scene_write_end(s, cs));
+    return RT_OK;
+}
+
 int32_t rt_scene_set_lights(rt_ctx* c, rt_scene* s, const rt_lights* L) {
     if (!c || !s || !L) return fail(RT_ERR_INVALID, "rt_scene_set_lights: null argument");
     int32_t r = check_lights(L);

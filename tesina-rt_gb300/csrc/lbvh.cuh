@@ -40,6 +40,9 @@ size_t lbvh_scratch_bytes(uint32_t n, int passes);
 // Byte offset of the emit's item buffers in a scene's build scratch (of
 // lbvh_scratch_bytes(n, 4) bytes); the many-scene build uses them too.
 size_t lbvh_emit_offset(uint32_t n);
+// mangle (src/kernel/mangler.cl:12-32) over V vertices, in place (animate.cu).
+cudaError_t launch_mangle(float4* pos, float4* nrm, uint32_t V, float arg, float height,
+                          cudaStream_t s);
 cudaError_t lbvh_build(const LbvhArgs& a, cudaStream_t s);
 cudaError_t lbvh_refit(const LbvhArgs& a, cudaStream_t s);
 

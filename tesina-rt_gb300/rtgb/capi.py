@@ -44,6 +44,7 @@ SIGNATURES = {
     "rt_scene_read_orig": (I32, [P, P, P]),
     "rt_bvh_build_lbvh": (I32, [P, P, P, P]),
     "rt_bvh_refit_lbvh": (I32, [P, P, P]),
+    "rt_scene_mangle": (I32, [P, P, F, F, F, P]),
     "rt_bvh_export": (I32, [P, P, P, U32, C.POINTER(U32)]),
     "rt_bvh_last_time_ms": (I32, [P, P, C.POINTER(F)]),
     "rt_gen_primary": (I32, [P, P, I32, I32, I32, I32, P, SZ, SZ, P, P]),
@@ -284,6 +285,11 @@ class Scene:
     def refit(self, stream=None):
         check(self.lib, self.lib.rt_bvh_refit_lbvh(self.ctx.h, self.h, stream))
 
+    def mangle(self, arg, last_arg=-1000.0, height=0.2, stream=None):
+        """Device-side vertex animation (mangler.cl); follow with refit() or build()."""
+        check(self.lib, self.lib.rt_scene_mangle(self.ctx.h, self.h, arg, last_arg, height,
+                                                 stream))
+
     def last_build_ms(self):
         ms = F(0)
         check(self.lib, self.lib.rt_bvh_last_time_ms(self.ctx.h, self.h, C.byref(ms)))
@@ -317,6 +323,15 @@ class Scene:
         check(self.lib, self.lib.rt_buf_read(self.ctx.h, _p(a), idx, a.nbytes, None))
         check(self.lib, self.lib.rt_buf_read(self.ctx.h, _p(m), mp, m.nbytes, None))
         return a, m
+
+    def read_vertices(self, n_verts):
+        """Device positions and normals (float32 [V, 4] each)."""
+        _, _, pos, nrm, _ = self.buffers()
+        p = np.zeros((n_verts, 4), np.float32)
+        q = np.zeros((n_verts, 4), np.float32)
+        check(self.lib, self.lib.rt_buf_read(self.ctx.h, _p(p), pos, p.nbytes, None))
+        check(self.lib, self.lib.rt_buf_read(self.ctx.h, _p(q), nrm, q.nbytes, None))
+        return p, q
 
     # stage-wise --------------------------------------------------------------
     def trace(self, smp_buf, n, hit_buf, stream=None):

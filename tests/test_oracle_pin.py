@@ -136,3 +136,17 @@ def test_pin_bitonic_aborts_like_reference(orc, ref, n):
     p = np.zeros(n, np.uint32)
     assert ref.bitonic(_p(keys), n, _p(p)) == -1
     assert orc.sort_bitonic(_p(keys), n, _p(p)) == -1
+
+
+@pytest.mark.parametrize("arg", [1.0, 17.0, 250.0])
+def test_pin_mangle(orc, ref, arg):
+    """mangle (mangler.cl:12-32): the oracle's restatement equals the
+    reference kernel compiled for the CPU, bit for bit, on a terrain's
+    vertices (positions, and the normals' x and z it rewrites)."""
+    ter = tiny_terrain(64, 32, 4)
+    sc = ter.scene(0)
+    po, no = orc.mangle(sc.pos4, sc.nrm4, arg, arg - 1.0, 0.2)
+    pr, nr = ref.mangle(sc.pos4, sc.nrm4, arg, arg - 1.0, 0.2)
+    assert np.array_equal(po.view(np.uint32), pr.view(np.uint32))
+    assert np.array_equal(no.view(np.uint32), nr.view(np.uint32))
+    assert not np.array_equal(po, sc.pos4)
