@@ -320,6 +320,52 @@ def measure_refit(ctx, torch, frames=20, warmup=3):
             "mrays_s": rays / (total * 1e-3) / 1e6, "device_status": ctx.device_status()}
 
 
+def measure_obj(ctx, torch, frames=5):
+    """OBJ input: the mid-scale terrain written as an OBJ file (v, vn and
+    v//vn faces; the reference's own models are not on every machine), read
+    through rt_obj_load (the reader's host time), then uploaded, built and
+    rendered at 1920x1080 depth 4 as one aggregate mesh with one material,
+    as the reference's OBJ scenes are."""
+    import tempfile
+    from rtgb import capi, obj, scenes
+    wl = scenes.workload_mid()
+    ter = wl["terrain"].scene(0)
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "terrain1M.obj")
+        obj.write(path, ter.pos4, ter.nrm4, ter.idx)
+        size = os.path.getsize(path)
+        t0 = time.perf_counter()
+        sc = obj.load(path, lights=ter.lights)
+        t_read = time.perf_counter() - t0
+    stream = torch.cuda.Stream()
+    sh = C.c_void_p(stream.cuda_stream)
+    t0 = time.perf_counter()
+    g = capi.Scene(ctx, sc)
+    g.build(30, 1, stream=sh)
+    stream.synchronize()
+    t_up = time.perf_counter() - t0
+    w, h, nb = wl["width"], wl["height"], wl["max_bounces"]
+    rgba = ctx.alloc(4 * w * h)
+    stats = ctx.alloc(32)
+    g.render(wl["camera"], w, h, nb, rgba, None, None, stream=sh)
+    stats.zero(sh)
+    ts = []
+    for _ in range(frames):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        g.render(wl["camera"], w, h, nb, rgba, None, stats, stream=sh)
+        e1.record(stream)
+        stream.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    st = stats.read(np.uint64)
+    return {"workload": "terrain1M_as_obj_1920x1080_d4", "triangles": sc.n_tris,
+            "vertices": sc.n_verts, "file_mb": size / 1e6, "read_s": t_read,
+            "read_mtri_s": sc.n_tris / t_read / 1e6, "read_mb_s": size / t_read / 1e6,
+            "upload_build_s": t_up, "render_ms": statistics.median(ts),
+            "mrays_s": int(st[0] + st[1]) / (sum(ts) * 1e-3) / 1e6,
+            "device_status": ctx.device_status()}
+
+
 def measure_served(ctx, rates=(2000, 1000, 300, 50), n_req=400, seed=5):
     """Served workload: 32 resident scenes (soups and fBm fields alternating,
     10k-2M triangles log-uniform), a 120 GB admission budget and a scene cap
@@ -597,6 +643,12 @@ def run_gpu(args):
             refit_leg = measure_refit(ctx, torch)
         except Exception as e:
             refit_leg = {"error": str(e)}
+    obj_leg = None
+    if world == 1 and not args.no_obj:
+        try:
+            obj_leg = measure_obj(ctx, torch)
+        except Exception as e:
+            obj_leg = {"error": str(e)}
     served_leg = None
     if world == 1 and not args.no_served:
         try:
@@ -627,6 +679,7 @@ def run_gpu(args):
            "served": served_leg,
            "stress": stress,
            "refit": refit_leg,
+           "obj": obj_leg,
            "e2e": {"value": e2e_value, "unit": UNIT,
                    "h2d_bytes_per_step": 2 * 16 * V,
                    "d2h_bytes_per_step": 4 * w * h + 32,
@@ -655,6 +708,7 @@ def main():
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--no-stress", action="store_true")
     ap.add_argument("--no-refit", action="store_true")
+    ap.add_argument("--no-obj", action="store_true")
     ap.add_argument("--render-variant", type=int, default=None,
                     help="render kernel variant instead of the autotuner's pick")
     ap.add_argument("--render-blocks", type=int, default=0, help="resident blocks per SM (0: all)")

@@ -231,6 +231,25 @@ RT_API int32_t rt_scene_update_vertices_device(rt_ctx* ctx, rt_scene* scene, con
  * rt_bvh_refit_lbvh (the refit-only mode, renderer.cpp:53-70) or a rebuild. */
 RT_API int32_t rt_scene_mangle(rt_ctx* ctx, rt_scene* scene, float arg, float last_arg,
                                float height, rt_stream s);
+/* Wavefront OBJ input, host side: the role of Scene::load_obj_file_as_aggregate
+ * (src/rt/scene.cpp:441-453) with the import rules of the loader the
+ * reference vendors (src/rt/obj-loader.cpp:163-1123): polygons split as fans,
+ * corners shared by bytewise-equal vertex records, material groups, normals
+ * generated when the file has none.  Group materials come from an mtllib file
+ * beside the model (newmtl, Kd, Ns / 1000, d, Tr) or the loader's default. */
+typedef struct rt_obj rt_obj;
+typedef struct {
+    uint32_t first_triangle, triangle_count;
+    float diffuse[3];
+    float shininess, alpha;
+} rt_obj_group;
+RT_API int32_t rt_obj_load(const char* path, rt_obj** out);
+RT_API int32_t rt_obj_info(const rt_obj* obj, uint32_t* vertex_count, uint32_t* triangle_count,
+                           uint32_t* group_count);
+/* Positions / normals as float4 (w = 0), uint3 indices, groups (highest alpha first). */
+RT_API int32_t rt_obj_copy(const rt_obj* obj, float* pos4, float* nrm4, uint32_t* indices,
+                           rt_obj_group* groups);
+RT_API int32_t rt_obj_free(rt_obj* obj);
 RT_API int32_t rt_scene_set_lights(rt_ctx* ctx, rt_scene* scene, const rt_lights* lights);
 /* Device buffers of the scene (reference: Scene::index_mem(), material_map_mem()).
  * After a build, indices and material map are permuted into sorted order, as

@@ -23,7 +23,9 @@ CXX = os.environ.get("CXX", "g++")
 FLAGS = ["-std=c++17", "-O3", "-fPIC", "-ffp-contract=off", "-fno-strict-aliasing", "-pthread"]
 
 REF_UNITS = ["ref_bvh", "ref_sort", "ref_trace", "ref_shadow", "ref_shade",
-             "ref_secondary", "ref_primary", "ref_driver", "ref_mangle"]
+             "ref_secondary", "ref_primary", "ref_driver", "ref_mangle", "ref_obj"]
+# the reference's host sources its OBJ import needs, compiled where they lie
+REF_HOST_SOURCES = ["obj-loader", "cl_aux", "mesh", "vector", "material"]
 # per-unit flags: mangler.cl has no fp64 pragma, so its constants are floats
 REF_UNIT_FLAGS = {"ref_mangle": ["-fsingle-precision-constant"]}
 
@@ -71,12 +73,24 @@ def build_ref(force=False):
     def one(unit):
         src = os.path.join(shim, unit + ".cpp")
         obj = os.path.join(outdir, unit + ".o")
-        _run([CXX] + FLAGS + REF_UNIT_FLAGS.get(unit, []) +
+        extra = host_inc if unit == "ref_obj" else []
+        _run([CXX] + FLAGS + REF_UNIT_FLAGS.get(unit, []) + extra +
              ["-fno-semantic-interposition", "-w", "-I", kdir, "-c", src, "-o", obj])
         return obj
 
-    with ThreadPoolExecutor(max_workers=len(REF_UNITS)) as ex:
-        objs = list(ex.map(one, REF_UNITS))
+    host_inc = ["-I", os.path.join(shim, "include"), "-I", os.path.join(REFERENCE_ROOT, "include")]
+
+    def host(unit):
+        obj = os.path.join(outdir, "host_" + unit + ".o")
+        _run([CXX] + FLAGS + ["-w"] + host_inc +
+             ["-c", os.path.join(REFERENCE_ROOT, "src", "rt", unit + ".cpp"), "-o", obj])
+        return obj
+
+    def any_unit(u):
+        return one(u) if u in REF_UNITS else host(u)
+
+    with ThreadPoolExecutor(max_workers=len(REF_UNITS) + len(REF_HOST_SOURCES)) as ex:
+        objs = list(ex.map(any_unit, REF_UNITS + REF_HOST_SOURCES))
     _run([CXX] + FLAGS + ["-shared"] + objs + ["-o", so])
     return so
 

@@ -209,6 +209,32 @@ class RefKernels(_Lib):
         self.render = b(L, "refd_render", C.c_int,
                         [P, P, I32, I32, I32, SZ, SZ, SZ, P, P, C.c_int])
         self.mangle_raw = b(L, "refk_mangle", None, [P, P, U32, F, F, F])
+        self.obj_load_raw = b(L, "refo_load", P, [C.c_char_p])
+        self.obj_sizes = b(L, "refo_sizes", None, [P, C.POINTER(U32), C.POINTER(U32),
+                                                    C.POINTER(U32)])
+        self.obj_copy = b(L, "refo_copy", None, [P, P, P, P, P, P, P, P])
+        self.obj_free = b(L, "refo_free", None, [P])
+
+    def obj_load(self, path):
+        """The reference's OBJ import: (pos4, nrm4, idx, group starts / ends
+        in index-buffer units, diffuse [G, 3], shininess [G])."""
+        h = self.obj_load_raw(str(path).encode())
+        if not h:
+            raise RuntimeError("reference OBJ import failed: %s" % path)
+        try:
+            V, N, G = U32(), U32(), U32()
+            self.obj_sizes(h, C.byref(V), C.byref(N), C.byref(G))
+            pos = np.zeros((V.value, 4), np.float32)
+            nrm = np.zeros((V.value, 4), np.float32)
+            idx = np.zeros((N.value, 3), np.uint32)
+            gs = np.zeros(G.value, np.uint32)
+            ge = np.zeros(G.value, np.uint32)
+            gd = np.zeros((G.value, 3), np.float32)
+            gsh = np.zeros(G.value, np.float32)
+            self.obj_copy(h, _p(pos), _p(nrm), _p(idx), _p(gs), _p(ge), _p(gd), _p(gsh))
+        finally:
+            self.obj_free(h)
+        return pos, nrm, idx, gs, ge, gd, gsh
 
     def mangle(self, pos4, nrm4, arg, last_arg=-1000.0, height=0.2):
         p, n = np.array(pos4, np.float32, copy=True), np.array(nrm4, np.float32, copy=True)

@@ -45,6 +45,10 @@ SIGNATURES = {
     "rt_bvh_build_lbvh": (I32, [P, P, P, P]),
     "rt_bvh_refit_lbvh": (I32, [P, P, P]),
     "rt_scene_mangle": (I32, [P, P, F, F, F, P]),
+    "rt_obj_load": (I32, [C.c_char_p, C.POINTER(P)]),
+    "rt_obj_info": (I32, [P, C.POINTER(U32), C.POINTER(U32), C.POINTER(U32)]),
+    "rt_obj_copy": (I32, [P, P, P, P, P]),
+    "rt_obj_free": (I32, [P]),
     "rt_bvh_export": (I32, [P, P, P, U32, C.POINTER(U32)]),
     "rt_bvh_last_time_ms": (I32, [P, P, C.POINTER(F)]),
     "rt_gen_primary": (I32, [P, P, I32, I32, I32, I32, P, SZ, SZ, P, P]),

@@ -217,3 +217,42 @@ def test_render_variants_identical(ctx, orc):
     rimg, _ = o.render(cam, w, h, 4)
     assert np.array_equal(images[0].reshape(-1, 3), rimg)
     ctx.set_render_config(saved.variant, saved.blocks_per_sm, saved.chunk)
+
+
+def test_render_obj_model_bit_exact(ctx, orc, tmp_path):
+    """A model through the OBJ path (rt_obj_load -> one aggregate mesh, the
+    first group's material): a 100x100-cell grid written as v/vt/vn faces
+    with one shared normal, and a terrain written as v//vn faces; each
+    rendered on the GPU equals the oracle's render of the same scene."""
+    from rtgb import obj
+    k = 100
+    lines = ["g grid"]
+    for j in range(k + 1):
+        for i in range(k + 1):
+            lines.append("v %.1f %.4f %.1f" % (-5.0 + 0.1 * i, 0.05 * np.sin(0.3 * i + 0.2 * j),
+                                                -5.0 + 0.1 * j))
+    for j in range(k + 1):
+        for i in range(k + 1):
+            lines.append("vt %.2f %.2f" % (i / k, j / k))
+    lines.append("vn 0 1 0")
+    for j in range(k):
+        for i in range(k):
+            a = j * (k + 1) + i + 1
+            b, c, d = a + 1, a + k + 1, a + k + 2
+            lines.append("f %d/%d/1 %d/%d/1 %d/%d/1" % (b, b, a, a, c, c))
+            lines.append("f %d/%d/1 %d/%d/1 %d/%d/1" % (b, b, c, c, d, d))
+    p = tmp_path / "grid.obj"
+    p.write_text("\n".join(lines) + "\n")
+    sc = obj.load(p)
+    assert sc.n_tris == 2 * k * k and sc.n_verts == (k + 1) ** 2
+    cam = scenes.camera((0.0, 4.0, -8.0), (0.0, 0.0, 0.0), aspect=1.0)
+    img, rgba, st, rimg, rst, _, _ = _render_both(ctx, orc, sc, cam, 128, 128, 2)
+    assert np.array_equal(img, rimg) and st[3] == rst.hits and rst.hits > 0
+    ter = tiny_terrain(64, 32, 6).scene(2)
+    q = tmp_path / "terrain.obj"
+    obj.write(q, ter.pos4, ter.nrm4, ter.idx)
+    sc2 = obj.load(q, lights=ter.lights, reflectiveness=0.5)
+    cam2 = scenes.camera((0.0, 4.0, -10.0), (0.0, 0.0, 0.0), aspect=160 / 90)
+    img, rgba, st, rimg, rst, _, _ = _render_both(ctx, orc, sc2, cam2, 160, 90, 3)
+    assert np.array_equal(img, rimg) and st[1] == rst.secondary_rays
+    assert ctx.device_status() == 0

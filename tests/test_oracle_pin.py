@@ -150,3 +150,31 @@ def test_pin_mangle(orc, ref, arg):
     assert np.array_equal(po.view(np.uint32), pr.view(np.uint32))
     assert np.array_equal(no.view(np.uint32), nr.view(np.uint32))
     assert not np.array_equal(po, sc.pos4)
+
+
+OBJ_MODELS = ["floor", "teapot-low_res", "teapot2", "teapot", "grid100", "frame_boat1",
+              "frame_water1"]
+
+
+@pytest.mark.parametrize("name", OBJ_MODELS)
+def test_pin_obj_models(ref, name):
+    """The library's OBJ reader against the reference's own import compiled
+    for the CPU, on every model the reference ships: vertices, normals
+    (read or generated), triangles and material groups, bit for bit."""
+    import os
+    import build as ob
+    from rtgb import obj
+    path = os.path.join(ob.REFERENCE_ROOT, "models", "obj", name + ".obj")
+    if not os.path.exists(path):
+        pytest.skip("model not present")
+    rp, rn, ri, gs, ge, gd, gsh = ref.obj_load(path)
+    op, on, oi, groups = obj.read(path)
+    assert np.array_equal(op.view(np.uint32), rp.view(np.uint32))
+    assert np.array_equal(on.view(np.uint32), rn.view(np.uint32))
+    assert np.array_equal(oi, ri)
+    assert np.array_equal(groups["first_triangle"] * 3, gs)
+    # the reference's end_index is its start (in index-buffer units) plus a
+    # triangle count (obj-loader.cpp:1380-1381)
+    assert np.array_equal(groups["first_triangle"] * 3 + groups["triangle_count"], ge)
+    assert np.array_equal(groups["diffuse"], gd)
+    assert np.array_equal(groups["shininess"], gsh)
