@@ -140,6 +140,15 @@ def cpu_baseline(wl, frame_pos, frame_nrm, sample_rays=65536):
             "lbvh_mtri_s": sc.n_tris / t_build / 1e6}
 
 
+def emit_levels_of(n):
+    """Launches of the LBVH emit for n triangles (512 per level-0 block,
+    then groups of 8 blocks up to the root)."""
+    levels, nb = 1, (n + 511) // 512
+    while nb > 1:
+        nb, levels = (nb + 7) // 8, levels + 1
+    return levels
+
+
 def measure_batched(ctx, lib, torch, reps=5):
     """Batched workload: 64 scenes built in one launch and rendered in one
     launch (CUDA-graph replay) against the same 64 requests through the plain
@@ -207,7 +216,10 @@ def measure_batched(ctx, lib, torch, reps=5):
             "rays_per_batch": rays_b, "plain_ms": statistics.median(t_plain),
             "batched_ms": statistics.median(t_b), "plain_mrays_s": mp, "batched_mrays_s": mb,
             "speedup": mb / mp, "identical_pixels": bool(same and rays_b == rays_plain),
-            "launches_per_batch": 3, "launches_plain": 10 * len(items)}
+            # build: the cooperative launch + one emit launch per level of the
+            # largest scene; render: the pooled kernel + the RGBA8 conversion
+            "launches_per_batch": 1 + max(emit_levels_of(it["scene"].n_tris) for it in items) + 2,
+            "launches_plain": sum(7 + emit_levels_of(it["scene"].n_tris) + 2 for it in items)}
 
 
 def measure_stress(ctx, torch, builds=5):
@@ -615,9 +627,7 @@ def run_gpu(args):
                 "note": "traversal is latency/L2-bound; algorithmic bytes = 88 B per traced "
                         "ray + 25 B per shadow ray"}
     # the emit's levels: 512 triangles per level-0 block, then 8 blocks per block
-    emit_levels, nb = 1, (n_tris + 511) // 512
-    while nb > 1:
-        nb, emit_levels = (nb + 7) // 8, emit_levels + 1
+    emit_levels = emit_levels_of(n_tris)
     launches_per_frame = 7 + emit_levels + (2 if pooled else 1)
     build_roofline = {"kernels": "k_bounds + k_morton_hist + 4x k_onesweep + k_permute + "
                                  "%dx k_emit_level" % emit_levels, "bound": "hbm",
