@@ -113,7 +113,16 @@ inline float fmin(float a, float b) { return std::fmin(a, b); }
 inline float fabs(float a) { return std::fabs(a); }
 inline float fdim(float a, float b) { return std::fdim(a, b); }
 inline float sqrt(float a) { return std::sqrt(a); }
-inline float pow(float a, float b) { return std::pow(a, b); }
+/* pow(x, 5) (the Schlick term of refraction) as the product in double
+ * precision rounded once, as the oracle and the CUDA path evaluate it (within
+ * the 16 ulp OpenCL allows pow); other exponents through the C library. */
+inline float pow(float a, float b) {
+    if (b == 5.0f) {
+        const double p = (double)a;
+        return (float)((((p * p) * p) * p) * p);
+    }
+    return std::pow(a, b);
+}
 inline float ceil(float a) { return std::ceil(a); }
 inline float floor(float a) { return std::floor(a); }
 inline float max(float x, float y) { return (x < y) ? y : x; }

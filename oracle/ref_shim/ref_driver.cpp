@@ -291,8 +291,11 @@ int refd_shade(refd_scene* s, const rt_sample* samples, rt_hit* hits, int32_t n,
     pad.push_back(sentinel);
     std::vector<rt_hit> hpad(hits, hits + n);
     hpad.push_back(rt_hit{});
+    /* one thread: the kernel adds to pixels without atomics, and with
+     * refraction one pixel has two samples in a wavefront */
+    (void)threads;
     refk_shade(primary, image, hpad.data(), pad.data(), s->mats.data(), s->map.data(),
-               s->lights.data(), n, threads);
+               s->lights.data(), n, 1);
     return 0;
 }
 

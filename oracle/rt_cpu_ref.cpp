@@ -597,14 +597,68 @@ static void shade_one(const orc_scene* s, const rt_sample& smp, const rt_hit& in
     v3 f = muls(valrgb, smp.contribution);
     f = mk(clamp01(f.x), clamp01(f.y), clamp01(f.z));
     uint32_t* px = image + 3 * (size_t)smp.pixel;
-    px[0] += (uint32_t)std::floor(f.x * 1e6f);
-    px[1] += (uint32_t)std::floor(f.y * 1e6f);
-    px[2] += (uint32_t)std::floor(f.z * 1e6f);
+    /* atomic: with refraction a pixel has two rays in one wavefront, shaded
+     * by different threads (integer sums, so any order gives the same bits) */
+    __atomic_fetch_add(&px[0], (uint32_t)std::floor(f.x * 1e6f), __ATOMIC_RELAXED);
+    __atomic_fetch_add(&px[1], (uint32_t)std::floor(f.y * 1e6f), __ATOMIC_RELAXED);
+    __atomic_fetch_add(&px[2], (uint32_t)std::floor(f.z * 1e6f), __ATOMIC_RELAXED);
+}
+
+/* pow(x, 5) of the Schlick term: the product in double precision, rounded
+ * to float once (identical in the CUDA path and the reference shim; within
+ * the 16 ulp OpenCL allows pow). */
+static float pow5(float x) {
+    const double p = (double)x;
+    return (float)((((p * p) * p) * p) * p);
+}
+
+/* Refraction branch of generate_secondary_rays_disc
+ * (secondary-ray-generator.cl:220-256): the Schlick factor R, and the
+ * refracted ray when k > 0.  Returns whether a ray was made. */
+static bool refract_ray(const rt_sample& in, const rt_hit& info, const rt_material& mat, float* R,
+                        rt_sample* out) {
+    const v3 d = neg(normalize(ld3(in.ray.dir)));
+    const v3 n = normalize(ld3(info.n));
+    float etai, etat;
+    if (info.inverse_n) {
+        etat = 1.0f;
+        etai = mat.refractive_index;
+    } else {
+        etai = 1.0f;
+        etat = mat.refractive_index;
+    }
+    const float cosi = dot(d, n);
+    const float rel_eta = etai / etat;
+    const float w = rel_eta * cosi;
+    float k = 1.0f + (w - rel_eta) * (w + rel_eta);
+    if (!(k > 0.0f)) return false;
+    float R0 = (etat - 1.0f) / (etat + 1.0f);
+    R0 *= R0;
+    const float cos5 = pow5(1.0f - cosi);
+    *R = R0 + (1.0f - R0) * cos5;
+    k = std::sqrt(k);
+    const v3 dir = normalize(sub(muls(n, w - k), muls(d, etai)));
+    rt_sample o;
+    std::memset(&o, 0, sizeof(o));
+    o.ray.ori[0] = info.hit_point[0];
+    o.ray.ori[1] = info.hit_point[1];
+    o.ray.ori[2] = info.hit_point[2];
+    o.ray.dir[0] = dir.x; o.ray.dir[1] = dir.y; o.ray.dir[2] = dir.z;
+    o.ray.inv_dir[0] = 1.0f / dir.x;
+    o.ray.inv_dir[1] = 1.0f / dir.y;
+    o.ray.inv_dir[2] = 1.0f / dir.z;
+    o.ray.tmin = 0.0001f;
+    o.ray.tmax = 1e37f;
+    o.pixel = in.pixel;
+    o.contribution = in.contribution * mat.reflectiveness * (1.0f - *R);
+    *out = o;
+    return true;
 }
 
 /* Reflection branch of generate_secondary_rays_disc
- * (secondary-ray-generator.cl:258-270). */
-static void reflect_ray(const rt_sample& in, const rt_hit& info, float refl, rt_sample* out) {
+ * (secondary-ray-generator.cl:258-270): contribution * reflectiveness * R. */
+static void reflect_ray(const rt_sample& in, const rt_hit& info, float refl, float R,
+                        rt_sample* out) {
     v3 d = neg(normalize(ld3(in.ray.dir)));
     v3 n = normalize(ld3(info.n));
     d = neg(d);
@@ -621,7 +675,7 @@ static void reflect_ray(const rt_sample& in, const rt_hit& info, float refl, rt_
     o.ray.tmin = 0.0001f;
     o.ray.tmax = 1e37f;
     o.pixel = in.pixel;
-    o.contribution = in.contribution * refl * 1.0f;
+    o.contribution = in.contribution * refl * R;
     *out = o;
 }
 
@@ -887,23 +941,45 @@ int orc_shadow(const orc_scene* s, const rt_sample* smp, int32_t n, rt_hit* hits
 
 int orc_shade(const orc_scene* s, const rt_sample* smp, const rt_hit* hits, int32_t n,
               uint32_t* image, int threads) {
-    /* one sample per pixel per launch, so pixel writes never collide */
     parallel_for(n, threads, [&](int64_t i) { shade_one(s, smp[i], hits[i], image); });
     return 0;
 }
 
-/* mark + exclusive scan + emit (reflection rays only), stable order. */
+/* mark + exclusive scan + emit of generate_secondary_rays_disc: reflection
+ * rays first (in input order), then refraction rays (in input order); a ray
+ * whose slot is at or beyond max_out is dropped, and a hit whose refraction
+ * slot is beyond it keeps R = 1 for its reflection ray, as in the kernel. */
 int orc_gen_secondary(const orc_scene* s, const rt_sample* in, int32_t n, const rt_hit* hits,
                       rt_sample* out, int32_t max_out, int32_t* count) {
-    int32_t k = 0;
+    std::vector<uint8_t> refl_flag(n, 0), refr_flag(n, 0);
+    int32_t n_refl = 0, n_refr = 0;
     for (int32_t i = 0; i < n; ++i) {
         if (!hits[i].hit) continue;
-        float refl = s->mats[s->map[hits[i].id]].reflectiveness;
-        if (!(refl > 0.0f)) continue;
-        if (k < max_out) reflect_ray(in[i], hits[i], refl, &out[k]);
-        ++k;
+        const rt_material& mat = s->mats[s->map[hits[i].id]];
+        if (mat.refractive_index > 0.0f) {
+            float R;
+            rt_sample tmp;
+            if (refract_ray(in[i], hits[i], mat, &R, &tmp)) refr_flag[i] = 1;
+        }
+        if (mat.reflectiveness > 0.0f) refl_flag[i] = 1;
+        n_refl += refl_flag[i];
+        n_refr += refr_flag[i];
     }
-    *count = std::min(k, max_out);
+    int32_t refl_id = 0, refr_id = n_refl;
+    for (int32_t i = 0; i < n; ++i) {
+        if (!hits[i].hit) continue;
+        const rt_material& mat = s->mats[s->map[hits[i].id]];
+        float R = 1.0f;
+        if (mat.refractive_index > 0.0f && refr_id < max_out) {
+            rt_sample r;
+            if (refract_ray(in[i], hits[i], mat, &R, &r)) out[refr_id] = r;
+        }
+        if (mat.reflectiveness > 0.0f && refl_id < max_out)
+            reflect_ray(in[i], hits[i], mat.reflectiveness, R, &out[refl_id]);
+        refl_id += refl_flag[i];
+        refr_id += refr_flag[i];
+    }
+    *count = std::min(n_refl + n_refr, max_out);
     return 0;
 }
 

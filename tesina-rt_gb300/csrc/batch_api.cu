@@ -220,6 +220,9 @@ int32_t rt_batch_set(rt_ctx* c, rt_batch* b, const rt_batch_view* views, int32_t
         const rt_batch_view& bv = views[v];
         if (!bv.scene || bv.scene->N == 0)
             return fail(RT_ERR_INVALID, "rt_batch_set: view %d has no uploaded scene", v);
+        if (bv.scene->refracts)
+            return fail(RT_ERR_INVALID, "rt_batch_set: view %d's scene refracts (rt_render and "
+                        "the stage-wise calls render refraction)", v);
         if (bv.width <= 0 || bv.height <= 0 || bv.max_bounces < 0 || bv.max_bounces > 64)
             return fail(RT_ERR_INVALID, "rt_batch_set: view %d has a bad size or depth", v);
         if (bv.rgba_offset != pixels)

@@ -518,8 +518,6 @@ int32_t rt_scene_upload(rt_ctx* c, rt_scene* s, const rt_scene_desc* d, rt_strea
     for (uint32_t i = 0; i < M; ++i) {
         if (d->h_materials[i].texture >= 0)
             return fail(RT_ERR_INVALID, "rt_scene_upload: material %u is textured (unsupported)", i);
-        if (d->h_materials[i].refractive_index > 0.f)
-            return fail(RT_ERR_INVALID, "rt_scene_upload: material %u refracts (unsupported)", i);
     }
     CU(cudaSetDevice(c->device));
     cudaStream_t cs = st(c, stream);
@@ -575,6 +573,8 @@ int32_t rt_scene_upload(rt_ctx* c, rt_scene* s, const rt_scene_desc* d, rt_strea
     }
     s->lights = d->lights;
     s->built = false;
+    s->refracts = false;
+    for (uint32_t i = 0; i < M; ++i) s->refracts = s->refracts || d->h_materials[i].refractive_index > 0.f;
     CU(scene_write_end(s, cs));
     return RT_OK;
 }
@@ -1009,8 +1009,14 @@ int32_t rt_render(rt_ctx* c, rt_scene* s, const rt_camera* cam, int32_t w, int32
     a.stats = stats;
     a.work_counter = work;
     a.status = c->d_status;
+    rt_render_config cfg = c->render_cfg;
+    if (s->refracts && !rt::render_variant_refracts(cfg.variant)) {
+        // refracting materials branch each hit: the variant that walks ray trees
+        cfg.variant = rt::render_refract_variant();
+        cfg.blocks_per_sm = 0;
+    }
     CU(scene_read_begin(s, cs));
-    CU(launch_render_cfg(c, a, c->render_cfg, cs));
+    CU(launch_render_cfg(c, a, cfg, cs));
     CU(scene_read_end(s, cs));
     return RT_OK;
 }
@@ -1067,6 +1073,7 @@ int32_t rt_autotune_render(rt_ctx* c, rt_scene* s, const rt_camera* cam, int32_t
     float bestt = 1e30f;
     const int chunks[] = {32, 64, 128};
     for (int v = 0; v < rt::render_variant_count(); ++v) {
+        if (rt::render_variant_refracts(v) != s->refracts) continue;   // the variants that fit the scene
         // full residency, one and two blocks fewer (more L1 per block:
         // the carveout follows the launched blocks), and half residency
         const int occ = c->variant_occupancy[v];

@@ -68,6 +68,7 @@ struct rt_scene {
     size_t scratch_bytes = 0;
     uint32_t buildN = 0;             // capacity of the build buffers
     bool built = false;
+    bool refracts = false;           // some material has refractive_index > 0
     int depth = 30, min_leaf = 1;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     // Order of the rt_* calls on this scene across streams: the completion

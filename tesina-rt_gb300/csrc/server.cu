@@ -271,6 +271,9 @@ int32_t create_scene(rt_server* S, const rt_scene_desc* d, cudaStream_t stream, 
     if (r) return r;
     rt::scene_use_pool(sc, S->pool, stream);
     r = rt_scene_upload(S->ctx, sc, d, stream);
+    if (!r && sc->refracts)
+        r = fail(RT_ERR_INVALID, "rt_server: a scene with refracting materials (rt_render and "
+                 "the stage-wise calls render refraction)");
     if (r) {
         rt_scene_destroy(S->ctx, sc);
         return r;

@@ -13,7 +13,7 @@ namespace rt {
 // fused per-pixel Whitted path (Renderer::render_to_framebuffer, one pixel
 // per lane, persistent warps fetching 32 pixels at a time)
 // ---------------------------------------------------------------------------
-template <int THREADS, int MINB>
+template <int THREADS, int MINB, bool REFR = false>
 __global__ void __launch_bounds__(THREADS, MINB) k_render(RenderArgs a) {
     const SceneView S = a.scene;
     __shared__ BvhHeader sH;
@@ -37,8 +37,8 @@ __global__ void __launch_bounds__(THREADS, MINB) k_render(RenderArgs a) {
         if (gid < pixels) {
             int x, y;
             pixel_of(warp_tile_order(gid, a.width, a.height), a.width, a.height, 32, x, y);
-            const PixelResult pr = render_pixel(S, H, sL, a.cam, x, y, a.width, a.height,
-                                                a.max_bounces, a.status);
+            const PixelResult pr = render_pixel<false, REFR>(S, H, sL, a.cam, x, y, a.width,
+                                                             a.height, a.max_bounces, a.status);
             const uint32_t acc_r = pr.r, acc_g = pr.g, acc_b = pr.b;
             ++n_prim;
             n_sec += pr.secondary;
@@ -355,21 +355,41 @@ __global__ void k_shade(SceneView S, rt_lights Ls, const rt_sample* __restrict__
     atomicAdd(px + 2, c.z);
 }
 
-// Secondary generation: flags -> per-block counts -> block offsets -> emit,
-// which keeps the input order (the reference's mark / scan / generate).
-__device__ __forceinline__ bool wants_reflection(const SceneView& S, const rt_hit& h, float& refl) {
-    if (!h.hit) return false;
-    refl = S.mats[__ldg(&S.map[h.id])].reflectiveness;
-    return refl > 0.0f;
+// Secondary generation (the reference's mark / scan / generate of
+// generate_secondary_rays_disc): flags -> per-block counts -> block offsets
+// -> emit, in input order.  Reflected rays take the first slots, refracted
+// rays the slots after all of them; a ray whose slot is at or beyond max_out
+// is dropped, and a hit whose refracted slot is beyond it keeps R = 1 for its
+// reflected ray, as in the kernel.
+__device__ __forceinline__ void sec_flags(const SceneView& S, const rt_sample& smp, const rt_hit& h,
+                                          bool& refl, bool& refr, rt_material& mat) {
+    refl = refr = false;
+    if (!h.hit) return;
+    mat = S.mats[__ldg(&S.map[h.id])];
+    refl = mat.reflectiveness > 0.0f;
+    if (mat.refractive_index > 0.0f) {
+        float R;
+        f3 td;
+        refr = refract_ray(f3_of(smp.ray.dir), f3_of(h.n), h.inverse_n != 0, mat.refractive_index,
+                           R, td);
+    }
 }
 
-__global__ void k_sec_count(SceneView S, const rt_hit* __restrict__ hits, int n,
+// block_counts[b] = reflected rays of block b, block_counts[nb + b] =
+// refracted ones; the scan over the 2 nb entries gives both slot bases.
+__global__ void k_sec_count(SceneView S, const rt_sample* __restrict__ in,
+                            const rt_hit* __restrict__ hits, int n,
                             uint32_t* __restrict__ block_counts) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    float refl;
-    const bool f = i < n && wants_reflection(S, hits[i], refl);
-    const int c = __syncthreads_count(f);
-    if (threadIdx.x == 0) block_counts[blockIdx.x] = (uint32_t)c;
+    bool refl = false, refr = false;
+    rt_material mat;
+    if (i < n) sec_flags(S, in[i], hits[i], refl, refr, mat);
+    const int cr = __syncthreads_count(refl);
+    const int ct = __syncthreads_count(refr);
+    if (threadIdx.x == 0) {
+        block_counts[blockIdx.x] = (uint32_t)cr;
+        block_counts[gridDim.x + blockIdx.x] = (uint32_t)ct;
+    }
 }
 
 __global__ void k_sec_scan(uint32_t* __restrict__ block_counts, int nblocks, int max_out,
@@ -398,27 +418,8 @@ __global__ void k_sec_scan(uint32_t* __restrict__ block_counts, int nblocks, int
     if (threadIdx.x == 0) *d_count = (int32_t)min(carry, (uint32_t)max_out);
 }
 
-__global__ void k_sec_emit(SceneView S, const rt_sample* __restrict__ in,
-                           const rt_hit* __restrict__ hits, int n,
-                           const uint32_t* __restrict__ block_offsets, rt_sample* __restrict__ out,
-                           int max_out) {
-    __shared__ uint32_t warp_tot[32];
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    float refl = 0.f;
-    const bool f = i < n && wants_reflection(S, hits[i], refl);
-    const unsigned bal = __ballot_sync(0xffffffffu, f);
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    if (lane == 0) warp_tot[w] = __popc(bal);
-    __syncthreads();
-    uint32_t wbase = 0;
-    for (int k = 0; k < w; ++k) wbase += warp_tot[k];
-    if (!f) return;
-    const uint32_t slot = block_offsets[blockIdx.x] + wbase + __popc(bal & ((1u << lane) - 1u));
-    if (slot >= (uint32_t)max_out) return;
-    const rt_hit& h = hits[i];
-    const rt_sample& s = in[i];
-    f3 dir;
-    reflect_ray(f3_of(s.ray.dir), f3_of(h.n), dir);
+__device__ __forceinline__ rt_sample sec_sample(const rt_hit& h, f3 dir, int pixel,
+                                                float contribution) {
     rt_sample o;
     o.ray.ori[0] = h.hit_point[0];
     o.ray.ori[1] = h.hit_point[1];
@@ -435,10 +436,51 @@ __global__ void k_sec_emit(SceneView S, const rt_sample* __restrict__ in,
     o.ray.tmin = 0.0001f;
     o.ray.tmax = 1e37f;
     o.ray._pad[0] = o.ray._pad[1] = 0.f;
-    o.pixel = s.pixel;
-    o.contribution = s.contribution * refl * 1.0f;
+    o.pixel = pixel;
+    o.contribution = contribution;
     o._pad[0] = o._pad[1] = 0;
-    out[slot] = o;
+    return o;
+}
+
+__global__ void k_sec_emit(SceneView S, const rt_sample* __restrict__ in,
+                           const rt_hit* __restrict__ hits, int n,
+                           const uint32_t* __restrict__ block_offsets, rt_sample* __restrict__ out,
+                           int max_out) {
+    __shared__ uint32_t warp_tot[2][32];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    bool refl = false, refr = false;
+    rt_material mat;
+    if (i < n) sec_flags(S, in[i], hits[i], refl, refr, mat);
+    const unsigned bal_l = __ballot_sync(0xffffffffu, refl);
+    const unsigned bal_t = __ballot_sync(0xffffffffu, refr);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) {
+        warp_tot[0][w] = __popc(bal_l);
+        warp_tot[1][w] = __popc(bal_t);
+    }
+    __syncthreads();
+    if (!refl && !refr) return;
+    uint32_t wl = 0, wt = 0;
+    for (int k = 0; k < w; ++k) {
+        wl += warp_tot[0][k];
+        wt += warp_tot[1][k];
+    }
+    const uint32_t below = (1u << lane) - 1u;
+    const uint32_t slot_l = block_offsets[blockIdx.x] + wl + __popc(bal_l & below);
+    const uint32_t slot_t = block_offsets[gridDim.x + blockIdx.x] + wt + __popc(bal_t & below);
+    const rt_hit& h = hits[i];
+    const rt_sample& smp = in[i];
+    float R = 1.0f;
+    if (refr && slot_t < (uint32_t)max_out) {
+        f3 td;
+        refract_ray(f3_of(smp.ray.dir), f3_of(h.n), h.inverse_n != 0, mat.refractive_index, R, td);
+        out[slot_t] = sec_sample(h, td, smp.pixel, smp.contribution * mat.reflectiveness * (1.0f - R));
+    }
+    if (refl && slot_l < (uint32_t)max_out) {
+        f3 dir;
+        reflect_ray(f3_of(smp.ray.dir), f3_of(h.n), dir);
+        out[slot_l] = sec_sample(h, dir, smp.pixel, smp.contribution * mat.reflectiveness * R);
+    }
 }
 
 __global__ void k_fb_copy(const uint32_t* __restrict__ img, uchar4* __restrict__ rgba, size_t px,
@@ -464,6 +506,7 @@ struct RenderVariant {
     int threads, min_blocks;
     void (*fn)(RenderArgs);
     bool pooled;
+    bool refract;   // walks the ray tree of refracting materials
 };
 static const RenderVariant kVariants[] = {
     {64, 8, k_render<64, 8>, false},    {64, 12, k_render<64, 12>, false},
@@ -472,6 +515,7 @@ static const RenderVariant kVariants[] = {
     {256, 3, k_render<256, 3>, false},  {256, 4, k_render<256, 4>, false},
     {128, 6, k_render_pool<128, 6>, true}, {128, 8, k_render_pool<128, 8>, true},
     {256, 3, k_render_pool<256, 3>, true}, {256, 4, k_render_pool<256, 4>, true},
+    {128, 6, k_render<128, 6, true>, false, true},
 };
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
@@ -486,6 +530,14 @@ int render_variant_info(int v, int* threads, int* min_blocks, const void** fn) {
 }
 
 bool render_variant_pooled(int v) { return v >= 0 && v < kNumVariants && kVariants[v].pooled; }
+
+bool render_variant_refracts(int v) { return v >= 0 && v < kNumVariants && kVariants[v].refract; }
+
+int render_refract_variant() {
+    for (int v = 0; v < kNumVariants; ++v)
+        if (kVariants[v].refract) return v;
+    return -1;
+}
 
 cudaError_t launch_render(const RenderArgs& a, int variant, int grid, cudaStream_t s) {
     if (variant < 0 || variant >= kNumVariants) return cudaErrorInvalidValue;
@@ -535,8 +587,8 @@ cudaError_t launch_gen_secondary(const SceneView& S, const rt_sample* in, int n,
                                  uint32_t* block_scratch, cudaStream_t s) {
     if (n <= 0) return cudaMemsetAsync(d_count, 0, sizeof(int32_t), s);
     const int nb = (int)blocks(n, 256);
-    k_sec_count<<<nb, 256, 0, s>>>(S, hits, n, block_scratch);
-    k_sec_scan<<<1, 1024, 0, s>>>(block_scratch, nb, max_out, d_count);
+    k_sec_count<<<nb, 256, 0, s>>>(S, in, hits, n, block_scratch);
+    k_sec_scan<<<1, 1024, 0, s>>>(block_scratch, 2 * nb, max_out, d_count);
     k_sec_emit<<<nb, 256, 0, s>>>(S, in, hits, n, block_scratch, out, max_out);
     return cudaGetLastError();
 }
@@ -548,6 +600,6 @@ cudaError_t launch_fb_copy(const uint32_t* img, uint8_t* rgba, size_t px, float 
     return cudaGetLastError();
 }
 
-size_t gen_secondary_scratch_bytes(int n) { return sizeof(uint32_t) * (blocks(n, 256) + 1); }
+size_t gen_secondary_scratch_bytes(int n) { return sizeof(uint32_t) * (2 * blocks(n, 256) + 1); }
 
 }  // namespace rt

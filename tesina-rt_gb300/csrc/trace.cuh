@@ -28,6 +28,10 @@ int render_variant_count();
 int render_variant_info(int v, int* threads, int* min_blocks, const void** fn);
 // True for variants that accumulate into RenderArgs::accum (k_render_pool).
 bool render_variant_pooled(int v);
+// True for the variant that walks refraction trees; the scenes with
+// refracting materials render with it.
+bool render_variant_refracts(int v);
+int render_refract_variant();
 cudaError_t launch_render(const RenderArgs& a, int variant, int grid, cudaStream_t s);
 cudaError_t launch_gen_primary(const rt_camera& cam, int w, int h, int q, const rt_pixel_sample* ps,
                                size_t count, size_t offset, rt_sample* out, cudaStream_t s);

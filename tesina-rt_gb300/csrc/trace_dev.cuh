@@ -423,6 +423,34 @@ __device__ __forceinline__ void reflect_ray(f3 d_in, f3 n_in, f3& dir) {
     dir = normalize(sub(d, muls(muls(n, 2.0f), dot(d, n))));
 }
 
+// pow(x, 5) of the Schlick term: the product in double precision, rounded to
+// float once (the oracle evaluates it the same way; OpenCL allows pow 16 ulp).
+__device__ __forceinline__ float pow5(float x) {
+    const double p = (double)x;
+    return (float)((((p * p) * p) * p) * p);
+}
+
+// Refraction branch of generate_secondary_rays_disc
+// (secondary-ray-generator.cl:220-256): whether the refracted ray exists
+// (k > 0), Schlick's factor R and the refracted direction.
+__device__ __forceinline__ bool refract_ray(f3 d_in, f3 n_in, bool inverse_n, float ior, float& R,
+                                            f3& dir) {
+    const f3 d = neg(normalize(d_in));
+    const f3 n = normalize(n_in);
+    const float etai = inverse_n ? ior : 1.0f, etat = inverse_n ? 1.0f : ior;
+    const float cosi = dot(d, n);
+    const float rel_eta = etai / etat;
+    const float w = rel_eta * cosi;
+    float k = 1.0f + (w - rel_eta) * (w + rel_eta);
+    if (!(k > 0.0f)) return false;
+    float R0 = (etat - 1.0f) / (etat + 1.0f);
+    R0 *= R0;
+    R = R0 + (1.0f - R0) * pow5(1.0f - cosi);
+    k = sqrtf(k);
+    dir = normalize(sub(muls(n, w - k), muls(d, etai)));
+    return true;
+}
+
 // Pixel of global id gid in the quad_size block order of generate_primary_rays.
 __device__ __forceinline__ void pixel_of(int gid, int w, int h, int q, int& x, int& y) {
     const int pixels = w * h;
@@ -487,7 +515,22 @@ struct PixelResult {
 // shadow ray per light, local shading, reflection ray while the material
 // reflects and the bounce budget lasts.  Integer accumulation of the
 // fixed-point contributions makes the sum independent of evaluation order.
-template <bool WW = false>
+// Pending secondary ray of a pixel's ray tree (refraction branches it).
+struct PendingRay {
+    f3 o, d;
+    float contribution;
+    int bounce;
+};
+constexpr int REFR_STACK = 16;   // pending rays per lane: one per level of the tree
+
+// One pixel's Whitted rays: the primary ray and, up to max_bounces, the
+// secondary rays of generate_secondary_rays_disc (a reflected ray with
+// contribution * reflectiveness * R, and with REFR a refracted one with
+// contribution * reflectiveness * (1 - R), R = Schlick's factor, 1 without
+// refraction), each traced, shadowed and shaded as the reference's wavefront
+// does.  The sums are integers, so the depth-first order of this tree walk
+// gives the wavefront's image.  WW: the two-phase traversal.
+template <bool WW = false, bool REFR = false>
 __device__ __forceinline__ PixelResult render_pixel(const SceneView& S, const BvhHeader& H,
                                                     const rt_lights& L, const rt_camera& cam,
                                                     int x, int y, int w, int h, int max_bounces,
@@ -496,29 +539,62 @@ __device__ __forceinline__ PixelResult render_pixel(const SceneView& S, const Bv
     f3 o = mk3(cam.pos[0], cam.pos[1], cam.pos[2]);
     f3 d = primary_dir(cam, x, y, w, h, 0.0f, 0.0f);
     float tmin = 0.0f, tmax = 1e36f, contribution = 1.0f;
-    for (int bounce = 0;; ++bounce) {
+    PendingRay stack[REFR ? REFR_STACK : 1];
+    int sp = 0;
+    for (int bounce = 0;;) {
+        bool next = false;
         const f3 inv = mk3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
         const TRay r = make_tray(o, d, inv, tmin);
         const Hit hit = WW ? closest_hit_ww(S, H, r, tmax, status) : closest_hit(S, H, r, tmax, status);
-        if (hit.id < 0) break;
-        ++res.hits;
-        const HitInfo hi = complete_hit(S, o, d, hit);
-        const rt_material mat = S.mats[__ldg(&S.map[hit.id])];
-        uint32_t mask = 0;
-        for (int l = 0; l < L.count; ++l)
-            if (occluded<WW>(S, H, L.light[l], hi.hp, status)) mask |= 1u << l;
-        res.shadow += (uint32_t)L.count;
-        const uint3 c = shade_hit(L, mat, hi.hp, hi.n, d, contribution, mask);
-        res.r += c.x;
-        res.g += c.y;
-        res.b += c.z;
-        if (bounce == max_bounces) break;
-        if (!(mat.reflectiveness > 0.0f)) break;
-        f3 nd;
-        reflect_ray(d, hi.n, nd);
-        contribution = contribution * mat.reflectiveness * 1.0f;
-        o = hi.hp;
-        d = nd;
+        if (hit.id >= 0) {
+            ++res.hits;
+            const HitInfo hi = complete_hit(S, o, d, hit);
+            const rt_material mat = S.mats[__ldg(&S.map[hit.id])];
+            uint32_t mask = 0;
+            for (int l = 0; l < L.count; ++l)
+                if (occluded<WW>(S, H, L.light[l], hi.hp, status)) mask |= 1u << l;
+            res.shadow += (uint32_t)L.count;
+            const uint3 c = shade_hit(L, mat, hi.hp, hi.n, d, contribution, mask);
+            res.r += c.x;
+            res.g += c.y;
+            res.b += c.z;
+            if (bounce < max_bounces) {
+                float R = 1.0f;
+                if (REFR && mat.refractive_index > 0.0f) {
+                    f3 td;
+                    if (refract_ray(d, hi.n, hi.inverse_n != 0, mat.refractive_index, R, td)) {
+                        if (sp < REFR_STACK) {
+                            stack[sp].o = hi.hp;
+                            stack[sp].d = td;
+                            stack[sp].contribution = contribution * mat.reflectiveness * (1.0f - R);
+                            stack[sp].bounce = bounce + 1;
+                            ++sp;
+                        } else {
+                            atomicOr(status, RT_DEV_OVERFLOW);
+                        }
+                    }
+                }
+                if (mat.reflectiveness > 0.0f) {
+                    f3 nd;
+                    reflect_ray(d, hi.n, nd);
+                    contribution = contribution * mat.reflectiveness * R;
+                    o = hi.hp;
+                    d = nd;
+                    tmin = 0.0001f;
+                    tmax = 1e37f;
+                    ++bounce;
+                    ++res.secondary;
+                    next = true;
+                }
+            }
+        }
+        if (next) continue;
+        if (!REFR || sp == 0) break;
+        --sp;   // the next refracted ray set aside
+        o = stack[sp].o;
+        d = stack[sp].d;
+        contribution = stack[sp].contribution;
+        bounce = stack[sp].bounce;
         tmin = 0.0001f;
         tmax = 1e37f;
         ++res.secondary;

@@ -89,6 +89,22 @@ def soup(n_tris=10000, seed=0, mirror_frac=0.2, offset_sigma=0.03,
     return Scene(pos, nrm, idx, mats, mat_map, lights)
 
 
+def with_glass(sc, frac=0.3, index=1.333, reflectiveness=0.9, seed=0):
+    """A copy of sc in which a fraction of the triangles take a refracting
+    material (the reference's scenes use refractive_index 1.333): one extra
+    material, diffuse 0.1, reflectiveness splitting the light between the
+    reflected and the refracted ray by Schlick's factor."""
+    rng = np.random.default_rng(seed)
+    mats = np.concatenate([sc.mats, _materials(1)])
+    g = mats.shape[0] - 1
+    mats["diffuse"][g, :3] = 0.1
+    mats["reflectiveness"][g] = reflectiveness
+    mats["refractive_index"][g] = index
+    mat_map = sc.mat_map.copy()
+    mat_map[rng.random(sc.n_tris) < frac] = g
+    return Scene(sc.pos4, sc.nrm4, sc.idx, mats, mat_map, sc.lights)
+
+
 # ---------------------------------------------------------------------------
 # value-noise fBm
 # ---------------------------------------------------------------------------

@@ -192,8 +192,8 @@ def test_invalid_inputs_rejected(ctx):
         capi.Scene(ctx, bad)
     assert e.value.code == -2
     mats = sc.mats.copy()
-    mats["refractive_index"][0] = 1.33
-    with pytest.raises(capi.RtError):
+    mats["texture"][0] = 2
+    with pytest.raises(capi.RtError):   # textured materials are not rendered
         capi.Scene(ctx, scenes.Scene(sc.pos4, sc.nrm4, sc.idx, mats, sc.mat_map, sc.lights))
     g = capi.Scene(ctx, sc)
     with pytest.raises(capi.RtError) as e:

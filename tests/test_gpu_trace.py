@@ -256,3 +256,68 @@ def test_render_obj_model_bit_exact(ctx, orc, tmp_path):
     img, rgba, st, rimg, rst, _, _ = _render_both(ctx, orc, sc2, cam2, 160, 90, 3)
     assert np.array_equal(img, rimg) and st[1] == rst.secondary_rays
     assert ctx.device_status() == 0
+
+
+@pytest.mark.parametrize("fill", [1.0, 0.7])
+def test_refraction_secondary_rays_match_oracle(ctx, orc, fill):
+    """generate_secondary_rays_disc with glass (refractive index 1.333): the
+    stage-wise GPU call makes the oracle's rays, slot for slot, both with
+    room for all of them and with a buffer that cuts into the refracted
+    rays (those past it are dropped, and their hits' reflected rays keep
+    R = 1, as in the kernel)."""
+    sc = scenes.with_glass(scenes.soup(10000, seed=2), frac=0.4, seed=3)
+    g, o = _pair(ctx, orc, sc)
+    cam = camera_small()
+    w = h = 256
+    n = w * h
+    smp_d, smp = _primary(ctx, orc, cam, w, h)
+    hit_d = ctx.alloc(64 * n)
+    hit_d.zero()
+    g.trace(smp_d, n, hit_d)
+    g.shadow(smp_d, n, hit_d)
+    ctx.sync()
+    ref = o.trace(smp)
+    o.shadow(smp, ref)
+    total = o.gen_secondary(smp, ref, 2 * n).shape[0]
+    max_out = max(1, int(total * fill))
+    out_d = ctx.alloc(80 * max_out)
+    cnt_d = ctx.alloc(4)
+    k = g.gen_secondary(smp_d, n, hit_d, out_d, max_out, cnt_d)
+    ref_sec = o.gen_secondary(smp, ref, max_out)
+    assert k == ref_sec.shape[0] == min(total, max_out) and k > 1000
+    assert out_d.read(abi.SAMPLE_DTYPE, k).tobytes() == ref_sec.tobytes()
+
+
+@pytest.mark.parametrize("bounces", [1, 4])
+def test_render_refraction_bit_exact(ctx, orc, bounces):
+    """rt_render of a soup with glass: each hit on glass spawns a refracted
+    and a reflected ray, walked as a tree per pixel; the fixed-point image and
+    the ray counts equal the oracle's wavefront render (a tile large enough
+    that no wavefront is cut)."""
+    sc = scenes.with_glass(scenes.soup(8000, seed=5), frac=0.4, seed=1)
+    g, o = _pair(ctx, orc, sc)
+    cam = scenes.camera((0.0, 0.0, -4.0), (0.0, 0.0, 0.0), aspect=1.0)
+    w = h = 256
+    n = w * h
+    rgba_d, img_d, st_d = ctx.alloc(4 * n), ctx.alloc(12 * n), ctx.alloc(32)
+    st_d.zero()
+    g.render(cam, w, h, bounces, rgba_d, img_d, st_d)
+    ctx.sync()
+    img = img_d.read(np.uint32).reshape(-1, 3)
+    st = st_d.read(np.uint64)
+    rimg, rst = o.render(cam, w, h, bounces, tile=1 << 20)
+    assert np.array_equal(img, rimg)
+    assert st[1] == rst.secondary_rays and st[2] == rst.shadow_rays and st[3] == rst.hits
+    assert rst.secondary_rays > 5000
+    assert ctx.device_status() == 0
+
+
+def test_refraction_outside_plain_path_rejected(ctx):
+    """The batched and served forms take no refracting scenes (yet)."""
+    sc = scenes.with_glass(scenes.soup(500, seed=1), frac=0.5)
+    g = capi.Scene(ctx, sc)
+    g.build(30, 1)
+    b = capi.Batch(ctx)
+    with pytest.raises(capi.RtError) as e:
+        b.set([(g, scenes.camera((0.0, 0.0, -4.0), (0.0, 0.0, 0.0)), 32, 32, 1)])
+    assert e.value.code == -2

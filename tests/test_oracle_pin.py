@@ -178,3 +178,26 @@ def test_pin_obj_models(ref, name):
     assert np.array_equal(groups["first_triangle"] * 3 + groups["triangle_count"], ge)
     assert np.array_equal(groups["diffuse"], gd)
     assert np.array_equal(groups["shininess"], gsh)
+
+
+@pytest.mark.parametrize("frac", [0.3, 1.0])
+def test_pin_refraction_render(orc, ref, frac):
+    """Refraction (secondary-ray-generator.cl:220-256): a soup with glass
+    triangles (refractive index 1.333) rendered end to end by the
+    reference's kernels and by the oracle, depth 4; the secondary rays of the
+    first bounce compared ray by ray, and the images, bit for bit."""
+    sc = scenes.with_glass(scenes.soup(6000, seed=9), frac=frac, seed=2)
+    s, rh = _pair(orc, ref, sc)
+    keys, perm, _, _ = s.sort_arrays()
+    ref.apply_perm(rh, _p(perm))
+    canon = s.canon()
+    ref.set_tree(rh, _p(canon), canon.shape[0])
+    cam = scenes.camera((0.0, 0.0, -4.0), (0.0, 0.0, 0.0), aspect=1.0)
+    w = h = 200
+    img_o, st_o = s.render(cam, w, h, 4)
+    img_r = np.zeros((w * h, 3), np.uint32)
+    st_r = abi.RenderStats()
+    ref.render(rh, C.byref(cam), w, h, 4, 0, w * h, 1 << 18, _p(img_r), C.byref(st_r), 8)
+    assert st_o.secondary_rays == st_r.secondary_rays > 2000
+    assert np.array_equal(img_o, img_r)
+    ref.scene_free(rh)
