@@ -332,6 +332,44 @@ def measure_refit(ctx, torch, frames=20, warmup=3):
             "mrays_s": rays / (total * 1e-3) / 1e6, "device_status": ctx.device_status()}
 
 
+def measure_refraction(ctx, torch, frames=5):
+    """Refraction: the mid-scale terrain with its 200 spheres made of glass
+    (refractive index 1.333, reflectiveness 0.9: every hit on a sphere sends
+    a refracted and a reflected ray, weighted by Schlick's factor), built
+    once and rendered at 1920x1080 depth 4 through rt_render (the ray-tree
+    variant).  Mrays/s counts primary + secondary rays."""
+    from rtgb import capi, scenes
+    wl = scenes.workload_mid()
+    sc = wl["terrain"].scene(0)
+    mats = sc.mats.copy()
+    mats["refractive_index"][1] = 1.333      # the spheres' material
+    mats["reflectiveness"][1] = 0.9
+    sc = scenes.Scene(sc.pos4, sc.nrm4, sc.idx, mats, sc.mat_map, sc.lights)
+    stream = torch.cuda.Stream()
+    sh = C.c_void_p(stream.cuda_stream)
+    g = capi.Scene(ctx, sc)
+    g.build(30, 1, stream=sh)
+    w, h, nb = wl["width"], wl["height"], wl["max_bounces"]
+    rgba = ctx.alloc(4 * w * h)
+    stats = ctx.alloc(32)
+    g.render(wl["camera"], w, h, nb, rgba, None, None, stream=sh)
+    stats.zero(sh)
+    ts = []
+    for _ in range(frames):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        g.render(wl["camera"], w, h, nb, rgba, None, stats, stream=sh)
+        e1.record(stream)
+        stream.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    st = stats.read(np.uint64)
+    rays = int(st[0] + st[1])
+    return {"workload": "terrain1M_glass_spheres_1920x1080_d4", "triangles": sc.n_tris,
+            "render_ms": statistics.median(ts), "rays_per_frame": rays // frames,
+            "secondary_per_frame": int(st[1]) // frames,
+            "mrays_s": rays / (sum(ts) * 1e-3) / 1e6, "device_status": ctx.device_status()}
+
+
 def measure_obj(ctx, torch, frames=5):
     """OBJ input: the mid-scale terrain written as an OBJ file (v, vn and
     v//vn faces; the reference's own models are not on every machine), read
@@ -653,6 +691,12 @@ def run_gpu(args):
             refit_leg = measure_refit(ctx, torch)
         except Exception as e:
             refit_leg = {"error": str(e)}
+    refraction_leg = None
+    if world == 1 and not args.no_refraction:
+        try:
+            refraction_leg = measure_refraction(ctx, torch)
+        except Exception as e:
+            refraction_leg = {"error": str(e)}
     obj_leg = None
     if world == 1 and not args.no_obj:
         try:
@@ -690,6 +734,7 @@ def run_gpu(args):
            "stress": stress,
            "refit": refit_leg,
            "obj": obj_leg,
+           "refraction": refraction_leg,
            "e2e": {"value": e2e_value, "unit": UNIT,
                    "h2d_bytes_per_step": 2 * 16 * V,
                    "d2h_bytes_per_step": 4 * w * h + 32,
@@ -719,6 +764,7 @@ def main():
     ap.add_argument("--no-stress", action="store_true")
     ap.add_argument("--no-refit", action="store_true")
     ap.add_argument("--no-obj", action="store_true")
+    ap.add_argument("--no-refraction", action="store_true")
     ap.add_argument("--render-variant", type=int, default=None,
                     help="render kernel variant instead of the autotuner's pick")
     ap.add_argument("--render-blocks", type=int, default=0, help="resident blocks per SM (0: all)")
