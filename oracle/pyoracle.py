@@ -59,6 +59,39 @@ class Oracle(_Lib):
         self.emit_keys_raw = b(L, "orc_emit_keys", C.c_int, [P, U32, C.c_int, C.c_int, P, U32,
                                                               C.POINTER(U32)])
         self.mangle_raw = b(L, "orc_mangle", C.c_int, [P, P, U32, F, F, F])
+        self.multi_new_raw = b(L, "orc_multi_new", P, [P, I32, P, P, P, I32, P])
+        self.multi_free = b(L, "orc_multi_free", None, [P])
+        self.multi_trace_raw = b(L, "orc_multi_trace", C.c_int, [P, P, I32, P, C.c_int])
+        self.multi_shadow_raw = b(L, "orc_multi_shadow", C.c_int, [P, P, I32, P, C.c_int])
+        self.multi_render_raw = b(L, "orc_multi_render", C.c_int,
+                                  [P, P, I32, I32, I32, SZ, P, P, C.c_int])
+
+    def multi(self, scene_handles, inst_scene, tr, trinv, lights):
+        """Multi-root scene over built oracle scenes; tr / trinv: float32 [n, 4, 4]."""
+        arr = (P * len(scene_handles))(*scene_handles)
+        ins = np.ascontiguousarray(inst_scene, np.int32)
+        t = np.ascontiguousarray(tr, np.float32)
+        ti = np.ascontiguousarray(trinv, np.float32)
+        h = self.multi_new_raw(C.cast(arr, P), len(scene_handles), _p(ins), _p(t), _p(ti),
+                               ins.shape[0], C.byref(lights))
+        if not h:
+            raise RuntimeError("oracle multi-root scene rejected")
+        return h
+
+    def multi_trace(self, h, samples, threads=0):
+        hits = np.zeros(samples.shape[0], abi.HIT_DTYPE)
+        self.multi_trace_raw(h, _p(samples), samples.shape[0], _p(hits), threads or os.cpu_count())
+        return hits
+
+    def multi_shadow(self, h, samples, hits, threads=0):
+        self.multi_shadow_raw(h, _p(samples), samples.shape[0], _p(hits), threads or os.cpu_count())
+
+    def multi_render(self, h, cam, w, hh, max_bounces, tile=1 << 20, threads=0):
+        image = np.zeros((hh * w, 3), np.uint32)
+        st = abi.RenderStats()
+        self.multi_render_raw(h, C.byref(cam), w, hh, max_bounces, tile, _p(image), C.byref(st),
+                              threads or os.cpu_count())
+        return image, st
 
     def mangle(self, pos4, nrm4, arg, last_arg=-1000.0, height=0.2):
         """mangle on copies of float32 [V, 4] positions / normals."""
@@ -209,11 +242,22 @@ class RefKernels(_Lib):
         self.render = b(L, "refd_render", C.c_int,
                         [P, P, I32, I32, I32, SZ, SZ, SZ, P, P, C.c_int])
         self.mangle_raw = b(L, "refk_mangle", None, [P, P, U32, F, F, F])
+        self.multi_new_raw = b(L, "refd_multi_new", P, [P, I32, P, P, P, I32, P])
+        self.multi_free = b(L, "refd_multi_free", None, [P])
+        self.multi_trace_raw = b(L, "refd_multi_trace", C.c_int, [P, P, I32, P, C.c_int])
+        self.multi_shadow_raw = b(L, "refd_multi_shadow", C.c_int, [P, P, I32, P, C.c_int])
+        self.multi_render_raw = b(L, "refd_multi_render", C.c_int,
+                                  [P, P, I32, I32, I32, SZ, P, P, C.c_int])
         self.obj_load_raw = b(L, "refo_load", P, [C.c_char_p])
         self.obj_sizes = b(L, "refo_sizes", None, [P, C.POINTER(U32), C.POINTER(U32),
                                                     C.POINTER(U32)])
         self.obj_copy = b(L, "refo_copy", None, [P, P, P, P, P, P, P, P])
         self.obj_free = b(L, "refo_free", None, [P])
+
+    multi = Oracle.multi
+    multi_trace = Oracle.multi_trace
+    multi_shadow = Oracle.multi_shadow
+    multi_render = Oracle.multi_render
 
     def obj_load(self, path):
         """The reference's OBJ import: (pos4, nrm4, idx, group starts / ends

@@ -104,6 +104,17 @@ CLSHIM_V2_BIN(*)
 CLSHIM_V2_BIN(/)
 #undef CLSHIM_V2_BIN
 
+/* OpenCL's vector literal (float4)(v, s) with v a float3: in C++ the
+ * parenthesised pair is a comma expression, so the comma of (float3, float)
+ * builds the pair and the cast turns it into the float4 OpenCL means
+ * (multiply_vector / multiply_point, trace-bvh.cl:84-113). */
+struct V3S {
+    float3 v;
+    float s;
+    operator float4() const { return float4(v.x, v.y, v.z, s); }
+};
+inline V3S operator,(float3 a, float b) { return V3S{a, b}; }
+
 inline float3 operator-(float3 a) { return float3(-a.x, -a.y, -a.z); }
 inline float4 operator-(float4 a) { return float4(-a.x, -a.y, -a.z, -a.w); }
 

@@ -114,3 +114,18 @@ void refk_build_node_bbox(void* nodes, size_t start, size_t count) {
     }
 }
 }
+
+extern "C" {
+/* Offsets node references for a node array placed at node_off among others
+ * whose triangles start at tri_off (leaf ranges) -- the layout the
+ * reference's Scene::create_bvhs gives several meshes' trees. */
+void refk_offset_nodes(void* nodes, size_t n, unsigned node_off, unsigned tri_off) {
+    rk::BVHNode* nd = (rk::BVHNode*)nodes;
+    for (size_t i = 0; i < n; ++i) {
+        const unsigned o = nd[i].leaf ? tri_off : node_off;
+        nd[i].l_child += o;
+        nd[i].r_child += o;
+        nd[i].parent += node_off;
+    }
+}
+}

@@ -49,6 +49,13 @@ void refk_morton_sort(int g, void* codes, unsigned* tris, int inc, int dir, int 
 void refk_trace_single(rt_hit* info, rt_sample* samples, void* vtx, int* idx, void* nodes, size_t n,
                        int threads);
 int refk_make_lights(const rt_lights* in, void* out);
+void refk_offset_nodes(void* nodes, size_t n, unsigned node_off, unsigned tri_off);
+size_t refk_sizeof_root(void);
+void refk_make_root(void* roots, size_t i, int node, const float* tr, const float* trinv);
+void refk_trace_multi(rt_hit* info, rt_sample* samples, void* vtx, int* idx, void* nodes, void* roots,
+                      int root_count, size_t n, int threads);
+void refk_shadow_trace_multi(rt_hit* info, rt_sample* samples, void* vtx, int* idx, void* nodes,
+                             void* lights, void* roots, int root_count, size_t n, int threads);
 void refk_shadow_trace_single(rt_hit* info, rt_sample* samples, void* vtx, int* idx, void* nodes,
                               void* lights, size_t n, int threads);
 void refk_shade(int primary, uint32_t* image, rt_hit* info, rt_sample* samples, rt_material* mats,
@@ -346,6 +353,95 @@ int refd_render(refd_scene* s, const rt_camera* cam, int32_t w, int32_t h, int32
             refd_shadow(s, rin, sec, hits.data(), threads);
             refd_shade(s, rin, hits.data(), sec, image, 0, threads);
             if (stats) stats->secondary_rays += (uint64_t)sec;
+        }
+    }
+    return 0;
+}
+
+/* Scene::create_bvhs (src/rt/scene.cpp:636-703) over built scenes: the
+ * meshes' vertices, indices, materials and trees concatenated (node and
+ * triangle references offset), one BVHRoot per instance. */
+struct refd_multi {
+    refd_scene all;
+    std::vector<uint8_t> roots;
+    int nroots = 0;
+};
+
+refd_multi* refd_multi_new(refd_scene** scenes, int32_t nscenes, const int32_t* inst_scene,
+                           const float* tr, const float* trinv, int32_t ninst,
+                           const rt_lights* lights) {
+    refd_multi* m = new refd_multi();
+    std::vector<uint32_t> node_off;
+    uint32_t vo = 0, to = 0, no = 0, mo = 0;
+    for (int k = 0; k < nscenes; ++k) {
+        refd_scene* s = scenes[k];
+        node_off.push_back(no);
+        m->all.vtx.insert(m->all.vtx.end(), s->vtx.begin(), s->vtx.end());
+        for (int x : s->idx) m->all.idx.push_back(x + (int)vo);
+        for (unsigned x : s->map) m->all.map.push_back(x + mo);
+        m->all.mats.insert(m->all.mats.end(), s->mats.begin(), s->mats.end());
+        const size_t at = m->all.nodes.size();
+        m->all.nodes.insert(m->all.nodes.end(), s->nodes.begin(), s->nodes.end());
+        refk_offset_nodes(m->all.nodes.data() + at, s->nnodes, no, to);
+        vo += s->V;
+        to += s->N;
+        no += s->nnodes;
+        mo += (uint32_t)s->mats.size();
+    }
+    m->all.V = vo;
+    m->all.N = to;
+    m->all.nnodes = no;
+    m->all.lights.resize(refk_sizeof_lights());
+    if (refk_make_lights(lights, m->all.lights.data())) {
+        delete m;
+        return nullptr;
+    }
+    m->nroots = ninst;
+    m->roots.assign(refk_sizeof_root() * (size_t)ninst, 0);
+    for (int i = 0; i < ninst; ++i)
+        refk_make_root(m->roots.data(), i, (int)node_off[inst_scene[i]], tr + 16 * i, trinv + 16 * i);
+    return m;
+}
+
+void refd_multi_free(refd_multi* m) { delete m; }
+
+int refd_multi_trace(refd_multi* m, rt_sample* smp, int32_t n, rt_hit* hits, int threads) {
+    refk_trace_multi(hits, smp, m->all.vtx.data(), m->all.idx.data(), m->all.nodes.data(),
+                     m->roots.data(), m->nroots, n, threads);
+    return 0;
+}
+
+int refd_multi_shadow(refd_multi* m, rt_sample* smp, int32_t n, rt_hit* hits, int threads) {
+    refk_shadow_trace_multi(hits, smp, m->all.vtx.data(), m->all.idx.data(), m->all.nodes.data(),
+                            m->all.lights.data(), m->roots.data(), m->nroots, n, threads);
+    return 0;
+}
+
+int refd_multi_render(refd_multi* m, const rt_camera* cam, int32_t w, int32_t h,
+                      int32_t max_bounces, size_t tile, uint32_t* image, rt_render_stats* stats,
+                      int threads) {
+    if (tile == 0) tile = 1u << 18;
+    const size_t count = (size_t)w * h;
+    std::vector<rt_sample> a(tile), b(tile);
+    std::vector<rt_hit> hits(tile);
+    for (size_t off = 0; off < count; off += tile) {
+        size_t cur = std::min(tile, count - off);
+        rt_sample* rin = a.data();
+        rt_sample* rout = b.data();
+        refd_gen_primary(cam, w, h, 32, 1, nullptr, cur, off, rin);
+        int32_t sec = (int32_t)cur;
+        for (int bounce = 0;; ++bounce) {
+            std::memset(hits.data(), 0, sizeof(rt_hit) * (size_t)sec);
+            refd_multi_trace(m, rin, sec, hits.data(), threads);
+            refd_multi_shadow(m, rin, sec, hits.data(), threads);
+            refd_shade(&m->all, rin, hits.data(), sec, image, bounce == 0, threads);
+            if (stats && bounce > 0) stats->secondary_rays += (uint64_t)sec;
+            if (bounce == max_bounces) break;
+            int32_t nout = 0;
+            refd_gen_secondary(&m->all, rin, sec, hits.data(), rout, (int32_t)tile, &nout);
+            std::swap(rin, rout);
+            sec = nout;
+            if (!sec) break;
         }
     }
     return 0;

@@ -52,3 +52,17 @@ void refk_shadow_trace_single(rt_hit* info, rt_sample* samples, void* vtx, int* 
     });
 }
 }
+
+extern "C" {
+void refk_shadow_trace_multi(rt_hit* info, rt_sample* samples, void* vtx, int* idx, void* nodes,
+                             void* lights, void* roots, int root_count, size_t n, int threads) {
+    refk_run(0, n, threads, [&](size_t g) {
+        rk::g_wi.gid = g;
+        rk::g_wi.goff = 0;
+        rk::shadow_trace_multi((rk::SampleTraceInfo*)info, (rk::Sample*)samples, (rk::Vertex*)vtx,
+                               idx, (rk::BVHNode*)nodes, (rk::Lights*)lights,
+                               (rk::BVHRoot*)roots, root_count);
+    });
+}
+}
+

@@ -1126,3 +1126,230 @@ int orc_fp64_t_of(const orc_scene* s, const rt_sample* smp, int32_t n, const int
 }
 
 }  /* extern "C" */
+
+/* ----------------------------------------------------------------------- */
+/* Multi-root traversal: trace_multi (trace-bvh.cl:420-463), its helpers     */
+/* multiply_vector / multiply_point / transform_ray / transform_hit_info /   */
+/* complete_transformed_hit_info (:84-181), and shadow_trace_multi           */
+/* (shadow-trace-bvh.cl:317-373).  Instances reference built scenes and      */
+/* carry a row-major 4x4 transform and its inverse (sqmat4); hit ids are     */
+/* global over the distinct scenes in first-use order (instances of one      */
+/* scene share its triangles, as the reference's roots of one mesh share its */
+/* node range).                                                               */
+/* ----------------------------------------------------------------------- */
+struct orc_multi {
+    std::vector<const orc_scene*> scenes;   /* distinct */
+    std::vector<uint32_t> tri_off;          /* per distinct scene */
+    std::vector<int> inst_scene;            /* per instance */
+    std::vector<float> tr, trinv;           /* 16 per instance */
+    orc_scene all;                          /* concatenated geometry and materials */
+};
+
+/* M x (v, w), then the homogeneous divide when |w'| > 1e-26 (the
+ * kernels' dot of float4 is a left-to-right sum of the four products). */
+static v3 mat_apply(const float* M, v3 v, float w) {
+    float r[4];
+    for (int k = 0; k < 4; ++k)
+        r[k] = M[4 * k] * v.x + M[4 * k + 1] * v.y + M[4 * k + 2] * v.z + M[4 * k + 3] * w;
+    if (std::fabs(r[3]) > 1e-26f) {
+        const float d = r[3];
+        r[0] = r[0] / d;
+        r[1] = r[1] / d;
+        r[2] = r[2] / d;
+    }
+    return mk(r[0], r[1], r[2]);
+}
+
+static Ray transform_ray(const Ray& ray, const float* M) {
+    Ray t = ray;
+    t.dir = mat_apply(M, ray.dir, 0.0f);
+    t.ori = mat_apply(M, ray.ori, 1.0f);
+    t.inv = mk(1.0f / t.dir.x, 1.0f / t.dir.y, 1.0f / t.dir.z);
+    return t;
+}
+
+static Best trace_multi_ray(const orc_multi* m, const Ray& ray, int* root) {
+    Best best{-1, 0.f, 0.f, 0.f};
+    *root = -1;
+    for (size_t i = 0; i < m->inst_scene.size(); ++i) {
+        const int k = m->inst_scene[i];
+        const Ray tr = transform_ray(ray, &m->trinv[16 * i]);
+        Best h = trace_ray(m->scenes[k], tr);
+        if (h.id >= 0) {
+            v3 hp = add(tr.ori, muls(tr.dir, h.t));
+            hp = mat_apply(&m->tr[16 * i], hp, 1.0f);
+            const v3 dv = sub(hp, ray.ori);
+            h.t = std::sqrt(dot(dv, dv));
+            h.id += (int32_t)m->tri_off[k];
+        }
+        if (h.id >= 0 && (best.id < 0 || h.t < best.t)) {
+            best = h;
+            *root = (int)i;
+        }
+    }
+    return best;
+}
+
+static void complete_multi(const orc_multi* m, const Ray& ray, const Best& b, int root, rt_hit* out) {
+    if (b.id < 0) {
+        out->hit = 0;
+        return;
+    }
+    const orc_scene* s = &m->all;
+    rt_hit h;
+    std::memset(&h, 0, sizeof(h));
+    h.hit = 1;
+    h.shadow_hit = out->shadow_hit;
+    h.t = b.t;
+    h.id = b.id;
+    const v3 hp = add(ray.ori, muls(ray.dir, b.t));
+    const uint32_t* ix = &s->idx[3 * (size_t)b.id];
+    const v3 n0 = normalize(ld3(&s->nrm[4 * (size_t)ix[0]]));
+    const v3 n1 = normalize(ld3(&s->nrm[4 * (size_t)ix[1]]));
+    const v3 n2 = normalize(ld3(&s->nrm[4 * (size_t)ix[2]]));
+    const float u = b.u, v = b.v;
+    const float w = 1.0f - (u + v);
+    v3 n = normalize(add(add(muls(n0, w), muls(n2, v)), muls(n1, u)));
+    n = mat_apply(&m->tr[16 * (size_t)root], n, 0.0f);   /* not renormalised */
+    if (dot(n, ray.dir) > 0.0f) {
+        h.inverse_n = 1;
+        n = muls(n, -1.0f);
+    } else {
+        h.inverse_n = 0;
+    }
+    h.n[0] = n.x; h.n[1] = n.y; h.n[2] = n.z;
+    h.hit_point[0] = hp.x; h.hit_point[1] = hp.y; h.hit_point[2] = hp.z;
+    *out = h;
+}
+
+/* shadow_trace_multi per light: the spot cone test leaves the point lit
+ * (shadow-trace-bvh.cl:343-347, unlike the single-root kernel), unknown
+ * light types light it; point lights (an extension) are spots without a
+ * cone.  The shadow ray is traced against every root in object space. */
+static bool light_occluded_multi(const orc_multi* m, const rt_light& L, v3 hp) {
+    Ray r;
+    r.ori = hp;
+    if (L.type == RT_DIR_L) {
+        r.dir = neg(ld3(L.dir));
+    } else if (L.type == RT_SPOT_L) {
+        r.dir = normalize(sub(ld3(L.pos), hp));
+        if (dot(r.dir, ld3(L.dir)) < L.angle) return false;
+    } else if (L.type == RT_POINT_L) {
+        r.dir = normalize(sub(ld3(L.pos), hp));
+    } else {
+        return false;
+    }
+    r.inv = mk(1.0f / r.dir.x, 1.0f / r.dir.y, 1.0f / r.dir.z);
+    r.tmin = 0.01f;
+    r.tmax = 1e37f;
+    for (size_t i = 0; i < m->inst_scene.size(); ++i) {
+        const Ray tr = transform_ray(r, &m->trinv[16 * i]);
+        if (trace_shadow(m->scenes[m->inst_scene[i]], tr)) return true;
+    }
+    return false;
+}
+
+extern "C" {
+
+orc_multi* orc_multi_new(orc_scene** scenes, int32_t nscenes, const int32_t* inst_scene,
+                         const float* tr, const float* trinv, int32_t ninst,
+                         const rt_lights* lights) {
+    orc_multi* m = new orc_multi();
+    uint32_t vo = 0, to = 0, mo = 0;
+    for (int k = 0; k < nscenes; ++k) {
+        const orc_scene* s = scenes[k];
+        if (!s->built) {
+            delete m;
+            return nullptr;
+        }
+        m->scenes.push_back(s);
+        m->tri_off.push_back(to);
+        m->all.pos.insert(m->all.pos.end(), s->pos.begin(), s->pos.end());
+        m->all.nrm.insert(m->all.nrm.end(), s->nrm.begin(), s->nrm.end());
+        for (uint32_t x : s->idx) m->all.idx.push_back(x + vo);
+        for (uint32_t x : s->map) m->all.map.push_back(x + mo);
+        m->all.mats.insert(m->all.mats.end(), s->mats.begin(), s->mats.end());
+        vo += s->V;
+        to += s->N;
+        mo += (uint32_t)s->mats.size();
+    }
+    m->all.V = vo;
+    m->all.N = to;
+    m->all.lights = *lights;
+    m->all.built = true;
+    m->inst_scene.assign(inst_scene, inst_scene + ninst);
+    m->tr.assign(tr, tr + 16 * (size_t)ninst);
+    m->trinv.assign(trinv, trinv + 16 * (size_t)ninst);
+    return m;
+}
+
+void orc_multi_free(orc_multi* m) { delete m; }
+
+int orc_multi_trace(const orc_multi* m, const rt_sample* smp, int32_t n, rt_hit* hits, int threads) {
+    parallel_for(n, threads, [&](int64_t i) {
+        const Ray r = ray_of(smp[i]);
+        int root;
+        const Best b = trace_multi_ray(m, r, &root);
+        complete_multi(m, r, b, root, &hits[i]);
+    });
+    return 0;
+}
+
+int orc_multi_shadow(const orc_multi* m, const rt_sample* smp, int32_t n, rt_hit* hits, int threads) {
+    (void)smp;
+    parallel_for(n, threads, [&](int64_t i) {
+        if (!hits[i].hit) return;
+        uint32_t mask = 0;
+        const v3 hp = ld3(hits[i].hit_point);
+        for (int l = 0; l < m->all.lights.count; ++l)
+            if (light_occluded_multi(m, m->all.lights.light[l], hp)) mask |= 1u << l;
+        hits[i].shadow_hit = (uint8_t)mask;
+    });
+    return 0;
+}
+
+/* The renderer's tile and bounce loop (renderer.cpp:113-214) with the
+ * multi-root tracer. */
+int orc_multi_render(const orc_multi* m, const rt_camera* cam, int32_t width, int32_t height,
+                     int32_t max_bounces, size_t tile_size, uint32_t* image, rt_render_stats* stats,
+                     int threads) {
+    if (threads <= 0) threads = (int)hw_threads();
+    if (tile_size == 0) tile_size = 1u << 18;
+    const orc_scene* s = &m->all;
+    const size_t count = (size_t)width * height;
+    std::vector<rt_sample> a(tile_size), b(tile_size);
+    std::vector<rt_hit> h(tile_size);
+    for (size_t off = 0; off < count; off += tile_size) {
+        size_t cur = std::min(tile_size, count - off);
+        rt_sample* rin = a.data();
+        rt_sample* rout = b.data();
+        orc_gen_primary(cam, width, height, 32, 1, nullptr, cur, off, rin);
+        int32_t sec = (int32_t)cur;
+        for (int bounce = 0;; ++bounce) {
+            std::memset(h.data(), 0, sizeof(rt_hit) * (size_t)sec);
+            orc_multi_trace(m, rin, sec, h.data(), threads);
+            orc_multi_shadow(m, rin, sec, h.data(), threads);
+            orc_shade(s, rin, h.data(), sec, image, threads);
+            if (stats) {
+                if (bounce == 0)
+                    stats->primary_rays += (uint64_t)sec;
+                else
+                    stats->secondary_rays += (uint64_t)sec;
+                for (int32_t i = 0; i < sec; ++i)
+                    if (h[i].hit) {
+                        stats->hits++;
+                        stats->shadow_rays += (uint64_t)s->lights.count;
+                    }
+            }
+            if (bounce == max_bounces) break;
+            int32_t nout = 0;
+            orc_gen_secondary(s, rin, sec, h.data(), rout, (int32_t)tile_size, &nout);
+            std::swap(rin, rout);
+            sec = nout;
+            if (!sec) break;
+        }
+    }
+    return 0;
+}
+
+}  /* extern "C" */

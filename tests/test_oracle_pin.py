@@ -201,3 +201,63 @@ def test_pin_refraction_render(orc, ref, frac):
     assert st_o.secondary_rays == st_r.secondary_rays > 2000
     assert np.array_equal(img_o, img_r)
     ref.scene_free(rh)
+
+
+def _instances():
+    """Two meshes, four instances: identity, a translation, a rotation with
+    uniform scale, a non-uniform scale (row-major 4x4, inverse in float64)."""
+    def tr(rot_deg=0.0, scale=(1, 1, 1), t=(0, 0, 0)):
+        a = np.radians(rot_deg)
+        r = np.array([[np.cos(a), 0, np.sin(a)], [0, 1, 0], [-np.sin(a), 0, np.cos(a)]])
+        m = np.eye(4)
+        m[:3, :3] = r @ np.diag(scale)
+        m[:3, 3] = t
+        return m
+    ms = [tr(), tr(t=(2.0, 0.0, 0.0)), tr(30.0, (0.7, 0.7, 0.7), (-1.5, 0.3, 1.0)),
+          tr(0.0, (1.0, 0.5, 1.2), (0.0, -1.0, 2.0))]
+    T = np.array(ms, np.float32)
+    Ti = np.array([np.linalg.inv(m) for m in ms], np.float32)
+    return [0, 1, 1, 0], T, Ti
+
+
+def test_pin_multi_root(orc, ref):
+    """trace_multi / shadow_trace_multi (trace-bvh.cl:420-463,
+    shadow-trace-bvh.cl:317-373) and the render over several roots: the
+    oracle against the reference's kernels on the same trees, bit for bit."""
+    meshes = [scenes.soup(3000, seed=4), tiny_terrain(32, 16, 2).scene(0)]
+    o_h, r_h = [], []
+    for sc in meshes:
+        s, rh = _pair(orc, ref, sc)
+        keys, perm, _, _ = s.sort_arrays()
+        ref.apply_perm(rh, _p(perm))
+        canon = s.canon()
+        ref.set_tree(rh, _p(canon), canon.shape[0])
+        o_h.append(s)
+        r_h.append(rh)
+    inst, T, Ti = _instances()
+    lights = abi.make_lights((0.1, 0.1, 0.1), [dict(type=abi.RT_POINT_L, pos=(0.0, 4.0, -3.0),
+                                                   color=(1.0, 1.0, 1.0))])
+    om = orc.multi([s.h for s in o_h], inst, T, Ti, lights)
+    rm = ref.multi(r_h, inst, T, Ti, lights)
+    cam = scenes.camera((0.0, 1.5, -6.0), (0.0, 0.0, 0.5), aspect=1.0)
+    w = h = 160
+    import pyoracle as po
+    smp = po.gen_primary(orc, cam, w, h)
+    ho = orc.multi_trace(om, smp)
+    hr = ref.multi_trace(rm, smp)
+    m = ho["hit"] == 1
+    assert np.array_equal(ho["hit"], hr["hit"]) and m.sum() > 2000
+    for f in ("id", "t", "inverse_n"):
+        assert np.array_equal(ho[f][m], hr[f][m]), f
+    for f in ("n", "hit_point"):
+        assert np.array_equal(ho[f][m][:, :3].view(np.uint32), hr[f][m][:, :3].view(np.uint32)), f
+    orc.multi_shadow(om, smp, ho)
+    ref.multi_shadow(rm, smp, hr)
+    assert np.array_equal(ho["shadow_hit"][m], hr["shadow_hit"][m])
+    img_o, st_o = orc.multi_render(om, cam, w, h, 3)
+    img_r, st_r = ref.multi_render(rm, cam, w, h, 3)
+    assert np.array_equal(img_o, img_r) and st_o.secondary_rays == st_r.secondary_rays > 0
+    orc.multi_free(om)
+    ref.multi_free(rm)
+    for rh in r_h:
+        ref.scene_free(rh)
