@@ -250,6 +250,28 @@ RT_API int32_t rt_obj_info(const rt_obj* obj, uint32_t* vertex_count, uint32_t* 
 RT_API int32_t rt_obj_copy(const rt_obj* obj, float* pos4, float* nrm4, uint32_t* indices,
                            rt_obj_group* groups);
 RT_API int32_t rt_obj_free(rt_obj* obj);
+/* Multi-root (instanced) scenes: the reference's objects with their own BVH
+ * roots and transforms (Scene::create_bvhs / update_bvh_roots,
+ * src/rt/scene.cpp:595-703; trace_multi, src/kernel/trace-bvh.cl:420-463;
+ * shadow_trace_multi, src/kernel/shadow-trace-bvh.cl:317-373).  Instance i
+ * draws built scene inst_scene[i] under the row-major 4x4 transform tr[16 i]
+ * whose inverse is tr_inv[16 i] (both given, as BVHRoot holds both).  Each
+ * scene keeps its materials; lights are the instance set's.  Scenes with
+ * refracting materials are not taken. */
+typedef struct rt_instances rt_instances;
+RT_API int32_t rt_instances_create(rt_ctx* ctx, rt_scene* const* scenes, int32_t scene_count,
+                                   const int32_t* inst_scene, const float* tr, const float* tr_inv,
+                                   int32_t instance_count, const rt_lights* lights,
+                                   rt_instances** out);
+/* New transforms for every instance (Scene::update_bvh_roots). */
+RT_API int32_t rt_instances_set_transforms(rt_ctx* ctx, rt_instances* inst, const float* tr,
+                                           const float* tr_inv);
+/* The Whitted frame over all instances (reflection, shadows, max_bounces). */
+RT_API int32_t rt_instances_render(rt_ctx* ctx, rt_instances* inst, const rt_camera* cam,
+                                   int32_t width, int32_t height, int32_t max_bounces,
+                                   uint8_t* d_rgba, uint32_t* d_image_rgb,
+                                   rt_render_stats* d_stats, rt_stream s);
+RT_API int32_t rt_instances_destroy(rt_ctx* ctx, rt_instances* inst);
 RT_API int32_t rt_scene_set_lights(rt_ctx* ctx, rt_scene* scene, const rt_lights* lights);
 /* Device buffers of the scene (reference: Scene::index_mem(), material_map_mem()).
  * After a build, indices and material map are permuted into sorted order, as

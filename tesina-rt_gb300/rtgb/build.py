@@ -14,7 +14,7 @@ CSRC = os.path.join(PKG, "csrc")
 LIB = os.path.join(PKG, "librt_cuda.so")
 OBJDIR = os.path.join(PKG, "_build")
 NVCC = os.environ.get("NVCC", "nvcc")
-UNITS = ["lbvh", "trace", "capi", "noalloc", "batch", "batch_api", "server", "animate", "obj"]
+UNITS = ["lbvh", "trace", "capi", "noalloc", "batch", "batch_api", "server", "animate", "obj", "instances"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ARCH + ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
                 "-Xcompiler", "-fvisibility=hidden"]

@@ -49,6 +49,10 @@ SIGNATURES = {
     "rt_obj_info": (I32, [P, C.POINTER(U32), C.POINTER(U32), C.POINTER(U32)]),
     "rt_obj_copy": (I32, [P, P, P, P, P]),
     "rt_obj_free": (I32, [P]),
+    "rt_instances_create": (I32, [P, P, I32, P, P, P, I32, P, C.POINTER(P)]),
+    "rt_instances_set_transforms": (I32, [P, P, P, P]),
+    "rt_instances_render": (I32, [P, P, P, I32, I32, I32, P, P, P, P]),
+    "rt_instances_destroy": (I32, [P, P]),
     "rt_bvh_export": (I32, [P, P, P, U32, C.POINTER(U32)]),
     "rt_bvh_last_time_ms": (I32, [P, P, C.POINTER(F)]),
     "rt_gen_primary": (I32, [P, P, I32, I32, I32, I32, P, SZ, SZ, P, P]),
@@ -530,3 +534,45 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+class Instances:
+    """Multi-root scene: instances of built Scenes under 4x4 transforms."""
+
+    def __init__(self, ctx, scenes_, inst_scene, tr, tr_inv, lights):
+        self.ctx, self.lib = ctx, ctx.lib
+        self._scenes = list(scenes_)   # kept alive with the instance set
+        arr = (P * len(self._scenes))(*[s.h for s in self._scenes])
+        self._ins = np.ascontiguousarray(inst_scene, np.int32)
+        t = np.ascontiguousarray(tr, np.float32)
+        ti = np.ascontiguousarray(tr_inv, np.float32)
+        self._lights = lights
+        h = P()
+        check(self.lib, self.lib.rt_instances_create(ctx.h, C.cast(arr, P), len(self._scenes),
+                                                     _p(self._ins), _p(t), _p(ti),
+                                                     self._ins.shape[0], C.byref(lights),
+                                                     C.byref(h)))
+        self.h = h
+
+    def set_transforms(self, tr, tr_inv):
+        t = np.ascontiguousarray(tr, np.float32)
+        ti = np.ascontiguousarray(tr_inv, np.float32)
+        check(self.lib, self.lib.rt_instances_set_transforms(self.ctx.h, self.h, _p(t), _p(ti)))
+
+    def render(self, cam, w, h, max_bounces, rgba_buf, img_buf=None, stats_buf=None, stream=None):
+        check(self.lib, self.lib.rt_instances_render(self.ctx.h, self.h, C.byref(cam), w, h,
+                                                     max_bounces, rgba_buf.ptr,
+                                                     img_buf.ptr if img_buf else None,
+                                                     stats_buf.ptr if stats_buf else None, stream))
+
+    def close(self):
+        if self.h:
+            self.lib.rt_instances_destroy(self.ctx.h, self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
