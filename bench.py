@@ -416,6 +416,92 @@ def measure_obj(ctx, torch, frames=5):
             "device_status": ctx.device_status()}
 
 
+def measure_instances(ctx, torch, frames=5):
+    """Multi-root: 16 instances of two meshes (rtgb.scenes.workload_instances)
+    rendered at 1920x1080 depth 4 through rt_instances_render, each frame
+    after new transforms for the 12 soups (rt_instances_set_transforms, the
+    per-frame root update of animated objects).  Beside it, the same
+    geometry flattened into one mesh (vertices moved on the host) and
+    rendered through the single-root path, for the cost of instancing.
+    Mrays/s counts primary + secondary rays."""
+    from rtgb import capi, scenes
+    wl = scenes.workload_instances()
+    stream = torch.cuda.Stream()
+    sh = C.c_void_p(stream.cuda_stream)
+    gs = []
+    for sc in wl["meshes"]:
+        g = capi.Scene(ctx, sc)
+        g.build(30, 1, stream=sh)
+        gs.append(g)
+    stream.synchronize()
+    I = capi.Instances(ctx, gs, wl["inst"], wl["tr"], wl["tr_inv"], wl["lights"])
+    w, h, nb = wl["width"], wl["height"], wl["max_bounces"]
+    rgba = ctx.alloc(4 * w * h)
+    stats = ctx.alloc(32)
+    I.render(wl["camera"], w, h, nb, rgba, None, None, stream=sh)
+    stats.zero(sh)
+    trs = []
+    for f in range(frames):          # turn the soups a little each frame
+        T, Ti = wl["tr"].copy(), wl["tr_inv"].copy()
+        for k in range(4, T.shape[0]):
+            m, mi = scenes.transform(5.0 * (f + 1))
+            T[k] = T[k] @ m
+            Ti[k] = mi @ Ti[k]
+        trs.append((T, Ti))
+    ts = []
+    for f in range(frames):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        stream.synchronize()
+        e0.record(stream)
+        I.set_transforms(*trs[f])        # ordered on the context stream before the render
+        I.render(wl["camera"], w, h, nb, rgba, None, stats, stream=sh)
+        e1.record(stream)
+        stream.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    st = stats.read(np.uint64)
+    rays = int(st[0] + st[1])
+    out = {"workload": wl["name"], "instances": int(len(wl["inst"])), "meshes": len(gs),
+           "triangles_instanced": int(sum(wl["meshes"][i].n_tris for i in wl["inst"])),
+           "render_ms": statistics.median(ts), "rays_per_frame": rays // frames,
+           "mrays_s": rays / (sum(ts) * 1e-3) / 1e6}
+    I.close()
+    # the same geometry as one aggregate mesh, at the first frame's transforms
+    T, _ = trs[0]
+    pos, nrm, idx, mats, mmap, base = [], [], [], [], [], 0
+    for k, si in enumerate(wl["inst"]):
+        sc = wl["meshes"][si]
+        p = sc.pos4.copy()
+        p[:, 3] = 1.0
+        p = (p @ T[k].T).astype(np.float32)
+        p[:, 3] = 0.0
+        n = sc.nrm4.copy()
+        n[:, :3] = n[:, :3] @ T[k][:3, :3].T
+        pos.append(p), nrm.append(n.astype(np.float32)), idx.append(sc.idx + base)
+        mmap.append(sc.mat_map + sum(len(m) for m in mats))
+        mats.append(sc.mats)
+        base += sc.pos4.shape[0]
+    flat = scenes.Scene(np.concatenate(pos), np.concatenate(nrm), np.concatenate(idx),
+                        np.concatenate(mats), np.concatenate(mmap).astype(np.uint32),
+                        wl["lights"])
+    g = capi.Scene(ctx, flat)
+    g.build(30, 1, stream=sh)
+    g.render(wl["camera"], w, h, nb, rgba, None, None, stream=sh)
+    stats.zero(sh)
+    ts = []
+    for _ in range(frames):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        g.render(wl["camera"], w, h, nb, rgba, None, stats, stream=sh)
+        e1.record(stream)
+        stream.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    st = stats.read(np.uint64)
+    out.update({"flattened_render_ms": statistics.median(ts),
+                "flattened_mrays_s": int(st[0] + st[1]) / (sum(ts) * 1e-3) / 1e6,
+                "device_status": ctx.device_status()})
+    return out
+
+
 def measure_served(ctx, rates=(2000, 1000, 300, 50), n_req=400, seed=5):
     """Served workload: 32 resident scenes (soups and fBm fields alternating,
     10k-2M triangles log-uniform), a 120 GB admission budget and a scene cap
@@ -697,6 +783,12 @@ def run_gpu(args):
             refraction_leg = measure_refraction(ctx, torch)
         except Exception as e:
             refraction_leg = {"error": str(e)}
+    instances_leg = None
+    if world == 1 and not args.no_instances:
+        try:
+            instances_leg = measure_instances(ctx, torch)
+        except Exception as e:
+            instances_leg = {"error": str(e)}
     obj_leg = None
     if world == 1 and not args.no_obj:
         try:
@@ -735,6 +827,7 @@ def run_gpu(args):
            "refit": refit_leg,
            "obj": obj_leg,
            "refraction": refraction_leg,
+           "instances": instances_leg,
            "e2e": {"value": e2e_value, "unit": UNIT,
                    "h2d_bytes_per_step": 2 * 16 * V,
                    "d2h_bytes_per_step": 4 * w * h + 32,
@@ -765,6 +858,7 @@ def main():
     ap.add_argument("--no-refit", action="store_true")
     ap.add_argument("--no-obj", action="store_true")
     ap.add_argument("--no-refraction", action="store_true")
+    ap.add_argument("--no-instances", action="store_true")
     ap.add_argument("--render-variant", type=int, default=None,
                     help="render kernel variant instead of the autotuner's pick")
     ap.add_argument("--render-blocks", type=int, default=0, help="resident blocks per SM (0: all)")

@@ -130,6 +130,10 @@ int32_t check_lights(const rt_lights* L) {
 
 cudaStream_t st(rt_ctx* c, rt_stream s) { return s ? (cudaStream_t)s : c->stream; }
 
+}  // namespace
+
+namespace rt {
+
 // Calls on one scene behave as on one in-order queue, whatever streams they
 // name (the reference runs every call on one command queue): a call that
 // writes the scene (upload, vertex update, build, refit) waits on the device
@@ -198,6 +202,16 @@ cudaError_t scene_host_wait(rt_scene* s, bool all) {
     }
     return cudaSuccess;
 }
+
+}  // namespace rt
+
+using rt::scene_write_begin;
+using rt::scene_write_end;
+using rt::scene_read_begin;
+using rt::scene_read_end;
+using rt::scene_host_wait;
+
+namespace {
 
 static void destroy_order_events(rt_scene* s) {
     if (s->ev_write) cudaEventDestroy(s->ev_write);

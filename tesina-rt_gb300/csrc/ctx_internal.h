@@ -111,4 +111,13 @@ uint32_t* accum_buffer(rt_ctx* c, cudaStream_t s, size_t pixels);
 // rt_gen_secondary scratch for launches on stream s, at least `bytes` long;
 // grown in stream order.  nullptr if it cannot be allocated.
 uint32_t* sec_scratch(rt_ctx* c, cudaStream_t s, size_t bytes);
+// Per-scene ordering across streams: calls on one scene behave as on one
+// in-order queue.  Writers (upload, build, refit) wait for every earlier call
+// on other streams; readers (trace, render) for the last writer.
+cudaError_t scene_write_begin(rt_scene* s, cudaStream_t cs);
+cudaError_t scene_write_end(rt_scene* s, cudaStream_t cs);
+cudaError_t scene_read_begin(rt_scene* s, cudaStream_t cs);
+cudaError_t scene_read_end(rt_scene* s, cudaStream_t cs);
+// Host wait for the scene's last writer (and its readers too when `all`).
+cudaError_t scene_host_wait(rt_scene* s, bool all);
 }  // namespace rt

@@ -19,6 +19,7 @@
 #include <stdint.h>
 
 #include <new>
+#include <cstring>
 #include <vector>
 
 #include "../../include/rt_cuda.h"
@@ -36,12 +37,12 @@ struct InstanceRoot {
 
 struct InstanceArgs {
     const InstanceRoot* roots;
+    const float4* cull;       // per root: world box lo, hi (padded; infinite = never culled)
     int count;
     rt_lights lights;
     rt_camera cam;
-    int width, height, max_bounces, chunk;
-    uint8_t* rgba;
-    uint32_t* image_rgb;
+    int width, height, max_bounces;
+    uint32_t* accum;          // 3 fixed-point sums per pixel, zeroed before the launch
     rt_render_stats* stats;
     uint32_t* work_counter;
     uint32_t* status;
@@ -64,31 +65,129 @@ __device__ __forceinline__ f3 mat_apply(const float* M, f3 v, float w) {
     return mk3(r[0], r[1], r[2]);
 }
 
+// World-space box of each root, for culling only: the eight corners of the
+// root box moved by the root's transform, padded for rounding.  A projective
+// transform, or one that gives non-finite corners, gets an infinite box.
+// Skipping a root the ray cannot reach changes no result: each root's hit is
+// a function of that root and the ray alone.
+__global__ void k_instance_boxes(const InstanceRoot* roots, int count, float4* cull) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    const InstanceRoot& R = roots[i];
+    const BvhHeader H = *R.scene.hdr;
+    const float* M = R.tr;
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    bool ok = M[12] == 0.0f && M[13] == 0.0f && M[14] == 0.0f && M[15] == 1.0f;
+    float big = 0.0f;
+    for (int c = 0; c < 8 && ok; ++c) {
+        const float x = (c & 1) ? H.root_hi.x : H.root_lo.x;
+        const float y = (c & 2) ? H.root_hi.y : H.root_lo.y;
+        const float z = (c & 4) ? H.root_hi.z : H.root_lo.z;
+        for (int k = 0; k < 3; ++k) {
+            const float v = M[4 * k] * x + M[4 * k + 1] * y + M[4 * k + 2] * z + M[4 * k + 3];
+            if (!isfinite(v)) ok = false;
+            lo[k] = fminf(lo[k], v);
+            hi[k] = fmaxf(hi[k], v);
+            big = fmaxf(big, fabsf(v));
+        }
+    }
+    if (!ok || H.n_tris == 0) {
+        cull[2 * i] = make_float4(-INFINITY, -INFINITY, -INFINITY, 0.0f);
+        cull[2 * i + 1] = make_float4(INFINITY, INFINITY, INFINITY, 0.0f);
+        return;
+    }
+    const float pad = 1e-4f * big + 1e-30f;
+    cull[2 * i] = make_float4(lo[0] - pad, lo[1] - pad, lo[2] - pad, 0.0f);
+    cull[2 * i + 1] = make_float4(hi[0] + pad, hi[1] + pad, hi[2] + pad, 0.0f);
+}
+
+// Entry parameter of the ray o + t d (t >= 0) into the box, or -1 when it
+// misses.  NaN slabs (a zero direction component on a box face) constrain
+// nothing, so the test can only keep roots, never drop one it would reach.
+__device__ __forceinline__ float cull_enter(const float4* cull, int i, f3 o, f3 inv) {
+    const float4 lo = __ldg(&cull[2 * i]), hi = __ldg(&cull[2 * i + 1]);
+    const float ax = (lo.x - o.x) * inv.x, bx = (hi.x - o.x) * inv.x;
+    const float ay = (lo.y - o.y) * inv.y, by = (hi.y - o.y) * inv.y;
+    const float az = (lo.z - o.z) * inv.z, bz = (hi.z - o.z) * inv.z;
+    const float t0 = fmaxf(fmaxf(fmaxf(fminf(ax, bx), fminf(ay, by)), fminf(az, bz)), 0.0f);
+    const float t1 = fminf(fminf(fmaxf(ax, bx), fmaxf(ay, by)), fmaxf(az, bz));
+    return t0 > t1 ? -1.0f : t0;
+}
+
 struct MultiHit {
     Hit h;        // id local to the instance's scene; t in world space
     int root;
 };
 
+__device__ __forceinline__ Hit root_closest(const InstanceRoot& R, f3 o, f3 d, float tmin,
+                                            float tmax, uint32_t* status) {
+    const f3 td = mat_apply(R.trinv, d, 0.0f);
+    const f3 to = mat_apply(R.trinv, o, 1.0f);
+    const TRay tr = make_tray(to, td, mk3(1.0f / td.x, 1.0f / td.y, 1.0f / td.z), tmin);
+    const BvhHeader H = *R.scene.hdr;
+    Hit h = closest_hit(R.scene, H, tr, tmax, status);
+    if (h.id >= 0) {
+        const f3 hp = mat_apply(R.tr, add(to, muls(td, h.t)), 1.0f);
+        const f3 dv = sub(hp, o);
+        h.t = sqrtf(dot(dv, dv));
+    }
+    return h;
+}
+
+// The reference keeps the first root (in index order) of least world t.  Each
+// root's hit depends only on that root and the ray, so the roots are visited
+// in groups of 32, near to far by box entry within a group, and a root is
+// taken when nearer, or as near and of lower index; the visit stops once the
+// next entry lies beyond the best hit.  The result is the reference's as long
+// as no world t is NaN (no order then): a NaN t reruns the reference's own
+// loop, every root in index order.
 __device__ __forceinline__ MultiHit closest_multi(const InstanceArgs& A, f3 o, f3 d, float tmin,
                                                   float tmax) {
-    MultiHit best{{-1, 0.f, 0.f, 0.f}, -1};
-    for (int i = 0; i < A.count; ++i) {
-        const InstanceRoot& R = A.roots[i];
-        const f3 td = mat_apply(R.trinv, d, 0.0f);
-        const f3 to = mat_apply(R.trinv, o, 1.0f);
-        const TRay tr = make_tray(to, td, mk3(1.0f / td.x, 1.0f / td.y, 1.0f / td.z), tmin);
-        const BvhHeader H = *R.scene.hdr;
-        Hit h = closest_hit(R.scene, H, tr, tmax, A.status);
-        if (h.id >= 0) {
-            const f3 hp = mat_apply(R.tr, add(to, muls(td, h.t)), 1.0f);
-            const f3 dv = sub(hp, o);
-            h.t = sqrtf(dot(dv, dv));
+    MultiHit best;
+    const f3 inv = mk3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
+    // world hit t is a distance: a root entered at parameter e is no nearer
+    // than e |d| (slack for rounding)
+    const float dlen = sqrtf(dot(d, d)) * 0.999f;
+    float ent[32];
+    bool seq = false, again;
+    do {
+        again = false;
+        best = MultiHit{{-1, 0.f, 0.f, 0.f}, -1};
+        for (int g = 0; g < A.count && !again; g += 32) {
+            const int m = min(32, A.count - g);
+            uint32_t live = 0;
+            for (int j = 0; j < m; ++j) {
+                const float e = seq ? 0.0f : cull_enter(A.cull, g + j, o, inv);
+                ent[j] = e;
+                if (seq || (e >= 0.0f && !(best.h.id >= 0 && e * dlen > best.h.t)))
+                    live |= 1u << j;
+            }
+            while (live) {
+                int jm = __ffs(live) - 1;
+                float em = ent[jm];
+                for (uint32_t r = live & (live - 1); r && !seq; r &= r - 1) {
+                    const int j = __ffs(r) - 1;
+                    if (ent[j] < em) {
+                        em = ent[j];
+                        jm = j;
+                    }
+                }
+                live &= ~(1u << jm);
+                if (!seq && best.h.id >= 0 && em * dlen > best.h.t) break;
+                const int i = g + jm;
+                const Hit h = root_closest(A.roots[i], o, d, tmin, tmax, A.status);
+                if (!seq && h.id >= 0 && isnan(h.t)) {
+                    seq = again = true;
+                    break;
+                }
+                if (h.id >= 0 &&
+                    (best.h.id < 0 || h.t < best.h.t || (h.t == best.h.t && i < best.root))) {
+                    best.h = h;
+                    best.root = i;
+                }
+            }
         }
-        if (h.id >= 0 && (best.h.id < 0 || h.t < best.h.t)) {
-            best.h = h;
-            best.root = i;
-        }
-    }
+    } while (again);
     return best;
 }
 
@@ -104,7 +203,9 @@ __device__ __forceinline__ bool occluded_multi(const InstanceArgs& A, const rt_l
     } else {
         return false;
     }
+    const f3 inv = mk3(1.0f / dir.x, 1.0f / dir.y, 1.0f / dir.z);
     for (int i = 0; i < A.count; ++i) {
+        if (cull_enter(A.cull, i, hp, inv) < 0.0f) continue;
         const InstanceRoot& R = A.roots[i];
         const f3 td = mat_apply(R.trinv, dir, 0.0f);
         const f3 to = mat_apply(R.trinv, hp, 1.0f);
@@ -115,95 +216,178 @@ __device__ __forceinline__ bool occluded_multi(const InstanceArgs& A, const rt_l
     return false;
 }
 
-// One pixel's Whitted path over the instances (reflection only).
-__device__ __forceinline__ PixelResult render_pixel_multi(const InstanceArgs& A, int x, int y) {
-    PixelResult res = {0, 0, 0, 0, 0, 0};
-    f3 o = mk3(A.cam.pos[0], A.cam.pos[1], A.cam.pos[2]);
-    f3 d = primary_dir(A.cam, x, y, A.width, A.height, 0.0f, 0.0f);
-    float tmin = 0.0f, tmax = 1e36f, contribution = 1.0f;
-    for (int bounce = 0;; ++bounce) {
-        const MultiHit mh = closest_multi(A, o, d, tmin, tmax);
-        if (mh.h.id < 0) break;
-        ++res.hits;
-        const InstanceRoot& R = A.roots[mh.root];
-        const SceneView& S = R.scene;
-        const f3 hp = add(o, muls(d, mh.h.t));
-        const uint32_t* ix = S.idx + 3 * (size_t)mh.h.id;
-        const f3 n0 = normalize(ld3(__ldg(&S.nrm[__ldg(ix)])));
-        const f3 n1 = normalize(ld3(__ldg(&S.nrm[__ldg(ix + 1)])));
-        const f3 n2 = normalize(ld3(__ldg(&S.nrm[__ldg(ix + 2)])));
-        const float w = 1.0f - (mh.h.u + mh.h.v);
-        f3 n = normalize(add(add(muls(n0, w), muls(n2, mh.h.v)), muls(n1, mh.h.u)));
-        n = mat_apply(R.tr, n, 0.0f);
-        if (dot(n, d) > 0.0f) n = muls(n, -1.0f);
-        const rt_material mat = S.mats[__ldg(&S.map[mh.h.id])];
-        uint32_t mask = 0;
-        for (int l = 0; l < A.lights.count; ++l)
-            if (occluded_multi(A, A.lights.light[l], hp)) mask |= 1u << l;
-        res.shadow += (uint32_t)A.lights.count;
-        const uint3 c = shade_hit(A.lights, mat, hp, n, d, contribution, mask);
-        res.r += c.x;
-        res.g += c.y;
-        res.b += c.z;
-        if (bounce == A.max_bounces) break;
-        if (!(mat.reflectiveness > 0.0f)) break;
-        f3 nd;
-        reflect_ray(d, n, nd);
-        contribution = contribution * mat.reflectiveness * 1.0f;
-        o = hp;
-        d = nd;
-        tmin = 0.0001f;
-        tmax = 1e37f;
-        ++res.secondary;
-    }
-    return res;
+// Surface of a multi-root hit: world point o + d t, the interpolated normal of
+// the instance's mesh moved by its transform (not renormalised), turned
+// against the ray.
+__device__ __forceinline__ void multi_surface(const InstanceArgs& A, const MultiHit& mh, f3 o, f3 d,
+                                              f3& hp, f3& n) {
+    const SceneView& S = A.roots[mh.root].scene;
+    hp = add(o, muls(d, mh.h.t));
+    const uint32_t* ix = S.idx + 3 * (size_t)mh.h.id;
+    const f3 n0 = normalize(ld3(__ldg(&S.nrm[__ldg(ix)])));
+    const f3 n1 = normalize(ld3(__ldg(&S.nrm[__ldg(ix + 1)])));
+    const f3 n2 = normalize(ld3(__ldg(&S.nrm[__ldg(ix + 2)])));
+    const float w = 1.0f - (mh.h.u + mh.h.v);
+    n = normalize(add(add(muls(n0, w), muls(n2, mh.h.v)), muls(n1, mh.h.u)));
+    n = mat_apply(A.roots[mh.root].tr, n, 0.0f);
+    if (dot(n, d) > 0.0f) n = muls(n, -1.0f);
 }
 
-__global__ void __launch_bounds__(128, 6) k_render_instances(InstanceArgs A) {
+// k_render_instances: the rays of the reference's multi-root render
+// (primary, then reflections up to max_bounces; one shadow ray per hit and
+// light), scheduled as in the single-root pooled kernel: a warp traces 32
+// primary rays of a pixel tile together, the hits' shadow rays as a dense
+// list of (hit, light) tasks, and the continuing paths' reflection rays from
+// a pool in shared memory, 32 at a time whichever pixels they belong to.
+// Contributions are fixed-point sums per pixel (independent of order), so
+// the image is the one the per-pixel loop gives.
+namespace {
+constexpr int IPOOL = 64;   // reflection rays a warp can hold: < 32 left + 32 new
+
+struct InstPool {
+    float ro[3][IPOOL], rd[3][IPOOL], rc[IPOOL];
+    int rpix[IPOOL], rbounce[IPOOL];
+    float hp[3][32], hn[3][32], hd[3][32], hc[32];
+    int hid[32], hroot[32], hpix[32], hbounce[32];
+    unsigned hmask[32];
+    int pool_n;
+};
+}  // namespace
+
+#ifndef RT_INST_MINB
+#define RT_INST_MINB 5
+#endif
+__global__ void __launch_bounds__(128, RT_INST_MINB) k_render_instances(InstanceArgs A) {
     __shared__ InstanceArgs sA;
+    __shared__ InstPool sQ[4];
     if (threadIdx.x == 0) sA = A;
-    __syncthreads();
     const int lane = threadIdx.x & 31;
+    InstPool& Q = sQ[threadIdx.x >> 5];
+    if (lane == 0) Q.pool_n = 0;
+    __syncthreads();
     const int pixels = sA.width * sA.height;
+    const unsigned lt = (1u << lane) - 1u;
     uint64_t n_sec = 0, n_shadow = 0, n_hits = 0, n_prim = 0;
+    bool tiles = true;
     for (;;) {
-        int base0 = 0;
-        if (lane == 0) base0 = (int)atomicAdd(sA.work_counter, (unsigned)sA.chunk);
-        base0 = __shfl_sync(0xffffffffu, base0, 0);
-        if (base0 >= pixels) break;
-        for (int base = base0; base < base0 + sA.chunk && base < pixels; base += 32) {
-            const int gid = base + lane;
-            if (gid >= pixels) continue;
-            int x, y;
-            pixel_of(warp_tile_order(gid, sA.width, sA.height), sA.width, sA.height, 32, x, y);
-            const PixelResult pr = render_pixel_multi(sA, x, y);
-            ++n_prim;
-            n_sec += pr.secondary;
-            n_shadow += pr.shadow;
-            n_hits += pr.hits;
-            const int pix = sA.width * y + x;
-            if (sA.image_rgb) {
-                sA.image_rgb[3 * (size_t)pix] = pr.r;
-                sA.image_rgb[3 * (size_t)pix + 1] = pr.g;
-                sA.image_rgb[3 * (size_t)pix + 2] = pr.b;
+        const int pn = Q.pool_n;
+        bool have = false;
+        f3 o = mk3(0.f, 0.f, 0.f), d = o;
+        float c = 1.0f, tmin = 0.0f, tmax = 1e36f;
+        int pix = 0, bounce = 0;
+        if (pn >= 32 || (!tiles && pn > 0)) {
+            const int k = min(32, pn);
+            const int j = pn - k + lane;
+            have = lane < k;
+            if (have) {
+                o = mk3(Q.ro[0][j], Q.ro[1][j], Q.ro[2][j]);
+                d = mk3(Q.rd[0][j], Q.rd[1][j], Q.rd[2][j]);
+                c = Q.rc[j];
+                pix = Q.rpix[j];
+                bounce = Q.rbounce[j];
+                tmin = 0.0001f;
+                tmax = 1e37f;
             }
-            uchar4 px;
-            px.x = to_unorm8(pr.r, sA.inv1e6);
-            px.y = to_unorm8(pr.g, sA.inv1e6);
-            px.z = to_unorm8(pr.b, sA.inv1e6);
-            px.w = 255;
-            reinterpret_cast<uchar4*>(sA.rgba)[pix] = px;
+            __syncwarp();
+            if (lane == 0) Q.pool_n = pn - k;
+        } else if (tiles) {
+            int base = 0;
+            if (lane == 0) base = (int)atomicAdd(sA.work_counter, 32u);
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (base >= pixels) {
+                tiles = false;
+                continue;
+            }
+            const int gid = base + lane;
+            have = gid < pixels;
+            if (have) {
+                int x, y;
+                pixel_of(warp_tile_order(gid, sA.width, sA.height), sA.width, sA.height, 32, x, y);
+                pix = sA.width * y + x;
+                o = mk3(sA.cam.pos[0], sA.cam.pos[1], sA.cam.pos[2]);
+                d = primary_dir(sA.cam, x, y, sA.width, sA.height, 0.0f, 0.0f);
+                ++n_prim;
+            }
+        } else {
+            break;
         }
+        MultiHit mh{{-1, 0.f, 0.f, 0.f}, -1};
+        if (have) mh = closest_multi(sA, o, d, tmin, tmax);
+        const bool hit_ok = mh.h.id >= 0;
+        const unsigned hm = __ballot_sync(0xffffffffu, hit_ok);
+        const int nh = __popc(hm);
+        if (hit_ok) {
+            const int k = __popc(hm & lt);
+            f3 hp, n;
+            multi_surface(sA, mh, o, d, hp, n);
+            Q.hp[0][k] = hp.x; Q.hp[1][k] = hp.y; Q.hp[2][k] = hp.z;
+            Q.hn[0][k] = n.x; Q.hn[1][k] = n.y; Q.hn[2][k] = n.z;
+            Q.hd[0][k] = d.x; Q.hd[1][k] = d.y; Q.hd[2][k] = d.z;
+            Q.hc[k] = c;
+            Q.hid[k] = mh.h.id;
+            Q.hroot[k] = mh.root;
+            Q.hpix[k] = pix;
+            Q.hbounce[k] = bounce;
+            Q.hmask[k] = 0u;
+        }
+        __syncwarp();
+        const int nl = sA.lights.count;
+        for (int t = lane; t < nh * nl; t += 32) {
+            const int k = t / nl, l = t - k * nl;
+            const f3 p = mk3(Q.hp[0][k], Q.hp[1][k], Q.hp[2][k]);
+            if (occluded_multi(sA, sA.lights.light[l], p)) atomicOr(&Q.hmask[k], 1u << l);
+        }
+        __syncwarp();
+        bool push = false;
+        f3 np = mk3(0.f, 0.f, 0.f), nd = np;
+        float nc = 0.f;
+        int npix = 0, nbounce = 0;
+        if (lane < nh) {
+            const int k = lane;
+            const f3 p = mk3(Q.hp[0][k], Q.hp[1][k], Q.hp[2][k]);
+            const f3 n = mk3(Q.hn[0][k], Q.hn[1][k], Q.hn[2][k]);
+            const f3 dk = mk3(Q.hd[0][k], Q.hd[1][k], Q.hd[2][k]);
+            const float ck = Q.hc[k];
+            const SceneView& S = sA.roots[Q.hroot[k]].scene;
+            const rt_material mat = S.mats[__ldg(&S.map[Q.hid[k]])];
+            const uint3 col = shade_hit(sA.lights, mat, p, n, dk, ck, Q.hmask[k]);
+            const int pk = Q.hpix[k];
+            atomicAdd(&sA.accum[3 * (size_t)pk], col.x);
+            atomicAdd(&sA.accum[3 * (size_t)pk + 1], col.y);
+            atomicAdd(&sA.accum[3 * (size_t)pk + 2], col.z);
+            ++n_hits;
+            n_shadow += (uint32_t)nl;
+            const int bk = Q.hbounce[k];
+            if (bk != sA.max_bounces && mat.reflectiveness > 0.0f) {
+                reflect_ray(dk, n, nd);
+                np = p;
+                nc = ck * mat.reflectiveness * 1.0f;
+                npix = pk;
+                nbounce = bk + 1;
+                push = true;
+                ++n_sec;
+            }
+        }
+        const unsigned pm = __ballot_sync(0xffffffffu, push);
+        const int pbase = Q.pool_n;
+        if (push) {
+            const int j = pbase + __popc(pm & lt);
+            Q.ro[0][j] = np.x; Q.ro[1][j] = np.y; Q.ro[2][j] = np.z;
+            Q.rd[0][j] = nd.x; Q.rd[1][j] = nd.y; Q.rd[2][j] = nd.z;
+            Q.rc[j] = nc;
+            Q.rpix[j] = npix;
+            Q.rbounce[j] = nbounce;
+        }
+        __syncwarp();
+        if (lane == 0) Q.pool_n = pbase + __popc(pm);
+        __syncwarp();
     }
     if (sA.stats) {
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            n_prim += __shfl_down_sync(0xffffffffu, n_prim, o);
-            n_sec += __shfl_down_sync(0xffffffffu, n_sec, o);
-            n_shadow += __shfl_down_sync(0xffffffffu, n_shadow, o);
-            n_hits += __shfl_down_sync(0xffffffffu, n_hits, o);
-        }
-        if (lane == 0 && n_prim) {
+        n_prim = __reduce_add_sync(0xffffffffu, (unsigned)n_prim);
+        n_sec = __reduce_add_sync(0xffffffffu, (unsigned)n_sec);
+        n_shadow = __reduce_add_sync(0xffffffffu, (unsigned)n_shadow);
+        n_hits = __reduce_add_sync(0xffffffffu, (unsigned)n_hits);
+        if (lane == 0) {
             atomicAdd((unsigned long long*)&sA.stats->primary_rays, (unsigned long long)n_prim);
             atomicAdd((unsigned long long*)&sA.stats->secondary_rays, (unsigned long long)n_sec);
             atomicAdd((unsigned long long*)&sA.stats->shadow_rays, (unsigned long long)n_shadow);
@@ -220,6 +404,11 @@ struct rt_instances {
     std::vector<float> tr, trinv;
     rt_lights lights;
     rt::InstanceRoot* d_roots = nullptr;
+    float4* d_cull = nullptr;          // 2 float4 per root, rewritten before each render
+    std::vector<rt::SceneView> views;  // the scenes' buffers as the roots name them
+    cudaEvent_t ev_render = nullptr;   // after the last render that read d_roots
+    cudaStream_t render_stream = nullptr;
+    bool rendered = false;
 };
 
 namespace {
@@ -234,10 +423,15 @@ namespace {
                         __FILE__, __LINE__);                                                  \
     } while (0)
 
+// Rewrites the device roots on stream s once every earlier render that read
+// them has finished, and returns when the copy is done.
 int32_t upload_roots(rt_instances* I, cudaStream_t s) {
+    if (I->rendered) CU(cudaStreamWaitEvent(s, I->ev_render, 0));
+    I->views.resize(I->scenes.size());
+    for (size_t k = 0; k < I->scenes.size(); ++k) I->views[k] = rt::scene_view(I->scenes[k]);
     std::vector<rt::InstanceRoot> roots(I->inst_scene.size());
     for (size_t i = 0; i < roots.size(); ++i) {
-        roots[i].scene = rt::scene_view(I->scenes[I->inst_scene[i]]);
+        roots[i].scene = I->views[I->inst_scene[i]];
         for (int k = 0; k < 16; ++k) {
             roots[i].tr[k] = I->tr[16 * i + k];
             roots[i].trinv[k] = I->trinv[16 * i + k];
@@ -281,14 +475,17 @@ int32_t rt_instances_create(rt_ctx* c, rt_scene* const* scenes, int32_t scene_co
     I->tr.assign(tr, tr + 16 * (size_t)count);
     I->trinv.assign(tr_inv, tr_inv + 16 * (size_t)count);
     I->lights = *lights;
-    if (cudaMalloc(&I->d_roots, sizeof(rt::InstanceRoot) * (size_t)count) != cudaSuccess) {
+    if (cudaMalloc(&I->d_roots, sizeof(rt::InstanceRoot) * (size_t)count) != cudaSuccess ||
+        cudaMalloc(&I->d_cull, 2 * sizeof(float4) * (size_t)count) != cudaSuccess) {
         cudaGetLastError();
+        cudaFree(I->d_roots);
         delete I;
         return fail(RT_ERR_OOM, "rt_instances_create: device allocation failed");
     }
     const int32_t r = upload_roots(I, c->stream);
     if (r) {
         cudaFree(I->d_roots);
+        cudaFree(I->d_cull);
         delete I;
         return r;
     }
@@ -314,20 +511,22 @@ int32_t rt_instances_render(rt_ctx* c, rt_instances* I, const rt_camera* cam, in
         if (!s->built || s->refracts)
             return fail(RT_ERR_INVALID, "rt_instances_render: a scene is not built or refracts");
     cudaStream_t cs = stream ? (cudaStream_t)stream : c->stream;
+    if (!I->ev_render) CU(cudaEventCreateWithFlags(&I->ev_render, cudaEventDisableTiming));
     uint32_t* work = rt::work_counter(c, cs);
     if (!work) return fail(RT_ERR_OOM, "rt_instances_render: work counter");
     CU(cudaMemsetAsync(work, 0, sizeof(uint32_t), cs));
     rt::InstanceArgs A;
     A.roots = I->d_roots;
+    A.cull = I->d_cull;
     A.count = (int)I->inst_scene.size();
     A.lights = I->lights;
     A.cam = *cam;
     A.width = w;
     A.height = h;
     A.max_bounces = max_bounces;
-    A.chunk = 64;
-    A.rgba = rgba;
-    A.image_rgb = img;
+    const size_t px = (size_t)w * h;
+    A.accum = img ? img : rt::accum_buffer(c, cs, px);
+    if (!A.accum) return fail(RT_ERR_OOM, "rt_instances_render: pixel sums");
     A.stats = stats;
     A.work_counter = work;
     A.status = c->d_status;
@@ -339,17 +538,42 @@ int32_t rt_instances_render(rt_ctx* c, rt_instances* I, const rt_camera* cam, in
         occ = b > 0 ? b : 1;
     }
     int64_t grid = (int64_t)c->num_sms * occ;
-    const int64_t useful = ((int64_t)w * h + 127) / 128;
+    const int64_t useful = ((int64_t)px + 127) / 128;   // one 32-pixel tile per warp
     if (grid > useful) grid = useful;
+    for (size_t k = 0; k < I->scenes.size(); ++k) {
+        // a rebuild may have moved a scene's sorted buffers: name the new ones
+        const rt::SceneView v = rt::scene_view(I->scenes[k]);
+        if (std::memcmp(&v, &I->views[k], sizeof v) != 0) {
+            const int32_t r = upload_roots(I, cs);
+            if (r) return r;
+            break;
+        }
+    }
+    for (rt_scene* s : I->scenes) CU(rt::scene_read_begin(s, cs));
+    // renders of one instance set share its cull boxes: they run in call order
+    if (I->rendered && I->render_stream != cs) CU(cudaStreamWaitEvent(cs, I->ev_render, 0));
+    rt::k_instance_boxes<<<(unsigned)((A.count + 127) / 128), 128, 0, cs>>>(I->d_roots, A.count,
+                                                                            I->d_cull);
+    CU(cudaMemsetAsync(A.accum, 0, 3 * sizeof(uint32_t) * px, cs));
     rt::k_render_instances<<<(unsigned)grid, 128, 0, cs>>>(A);
     CU(cudaGetLastError());
+    CU(rt::launch_fb_copy(A.accum, rgba, px, c->inv1e6, cs));
+    for (rt_scene* s : I->scenes) CU(rt::scene_read_end(s, cs));
+    CU(cudaEventRecord(I->ev_render, cs));
+    I->render_stream = cs;
+    I->rendered = true;
     return RT_OK;
 }
 
 int32_t rt_instances_destroy(rt_ctx* c, rt_instances* I) {
     if (!I) return RT_OK;
     if (c) cudaStreamSynchronize(c->stream);
+    if (I->ev_render) {
+        cudaEventSynchronize(I->ev_render);
+        cudaEventDestroy(I->ev_render);
+    }
     cudaFree(I->d_roots);
+    cudaFree(I->d_cull);
     delete I;
     return RT_OK;
 }

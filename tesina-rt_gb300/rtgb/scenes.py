@@ -337,6 +337,44 @@ def workload_batched(seed=3, count=64):
     return dict(name="soups64_1k-500k_mixed-res", items=items)
 
 
+def transform(rot_y_deg=0.0, scale=(1.0, 1.0, 1.0), t=(0.0, 0.0, 0.0)):
+    """Row-major 4x4 object-to-world matrix (rotation about y, then scale and
+    translation) and its inverse, both float32 (inverse taken in float64)."""
+    a = math.radians(rot_y_deg)
+    r = np.array([[math.cos(a), 0, math.sin(a)], [0, 1, 0], [-math.sin(a), 0, math.cos(a)]])
+    m = np.eye(4)
+    m[:3, :3] = r @ np.diag(scale)
+    m[:3, 3] = t
+    return m.astype(np.float32), np.linalg.inv(m).astype(np.float32)
+
+
+def workload_instances(seed=6):
+    """Multi-root (instanced) scene: one mesh per object, as the reference's
+    per-object BVHs.  A 256x128-cell fBm tile with 20 mirror spheres (≈86k
+    triangles) placed 2x2 as the ground, and a 50k-triangle soup placed 12
+    times above it with random turns and scales: 16 roots, 2 meshes.
+    1920x1080, depth 4, the tile's two point lights."""
+    rng = np.random.default_rng(seed)
+    tile = Terrain(256, 128, n_spheres=20, seed=seed)
+    blob = soup(50000, seed=seed + 1)
+    inst, ms, mis = [], [], []
+    for ix in (-1, 1):
+        for iz in (-1, 1):
+            m, mi = transform(t=(8.0 * ix, 0.0, 4.0 * iz))
+            inst.append(0), ms.append(m), mis.append(mi)
+    for _ in range(12):
+        s = float(rng.uniform(0.4, 1.0))
+        m, mi = transform(float(rng.uniform(0, 360)), (s, s, s),
+                          (float(rng.uniform(-12, 12)), float(rng.uniform(2.0, 4.0)),
+                           float(rng.uniform(-6, 6))))
+        inst.append(1), ms.append(m), mis.append(mi)
+    cam = camera((0.0, 12.0, -16.0), (0.0, 0.0, 0.0), fov_deg=60.0, aspect=1920 / 1080)
+    return dict(name="instances16_tile86k+soup50k_1920x1080_d4",
+                meshes=[tile.scene(0), blob], inst=np.array(inst, np.int32),
+                tr=np.array(ms), tr_inv=np.array(mis), lights=tile.lights, camera=cam,
+                width=1920, height=1080, max_bounces=4)
+
+
 def _served_scene(kind, n, seed):
     """One scene of the served pool: a soup of n triangles, or an fBm field of
     about n triangles (2 per cell, cells 2:1) over [-2,2]x[-1,1] with 16 mirror
