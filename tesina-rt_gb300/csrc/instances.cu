@@ -114,6 +114,10 @@ __device__ __forceinline__ float cull_enter(const float4* cull, int i, f3 o, f3 
     return t0 > t1 ? -1.0f : t0;
 }
 
+#ifndef RT_INST_NEAR
+#define RT_INST_NEAR 1   // visit a group's roots near to far (0: in index order)
+#endif
+
 struct MultiHit {
     Hit h;        // id local to the instance's scene; t in world space
     int root;
@@ -165,7 +169,7 @@ __device__ __forceinline__ MultiHit closest_multi(const InstanceArgs& A, f3 o, f
             while (live) {
                 int jm = __ffs(live) - 1;
                 float em = ent[jm];
-                for (uint32_t r = live & (live - 1); r && !seq; r &= r - 1) {
+                for (uint32_t r = live & (live - 1); RT_INST_NEAR && r && !seq; r &= r - 1) {
                     const int j = __ffs(r) - 1;
                     if (ent[j] < em) {
                         em = ent[j];
@@ -173,7 +177,10 @@ __device__ __forceinline__ MultiHit closest_multi(const InstanceArgs& A, f3 o, f
                     }
                 }
                 live &= ~(1u << jm);
-                if (!seq && best.h.id >= 0 && em * dlen > best.h.t) break;
+                if (!seq && best.h.id >= 0 && em * dlen > best.h.t) {
+                    if (RT_INST_NEAR) break;   // the rest of the group enters later still
+                    continue;
+                }
                 const int i = g + jm;
                 const Hit h = root_closest(A.roots[i], o, d, tmin, tmax, A.status);
                 if (!seq && h.id >= 0 && isnan(h.t)) {
@@ -255,7 +262,7 @@ struct InstPool {
 }  // namespace
 
 #ifndef RT_INST_MINB
-#define RT_INST_MINB 5
+#define RT_INST_MINB 6
 #endif
 __global__ void __launch_bounds__(128, RT_INST_MINB) k_render_instances(InstanceArgs A) {
     __shared__ InstanceArgs sA;
