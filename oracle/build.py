@@ -23,9 +23,10 @@ CXX = os.environ.get("CXX", "g++")
 FLAGS = ["-std=c++17", "-O3", "-fPIC", "-ffp-contract=off", "-fno-strict-aliasing", "-pthread"]
 
 REF_UNITS = ["ref_bvh", "ref_sort", "ref_trace", "ref_shadow", "ref_shade",
-             "ref_secondary", "ref_primary", "ref_driver", "ref_mangle", "ref_obj"]
-# the reference's host sources its OBJ import needs, compiled where they lie
-REF_HOST_SOURCES = ["obj-loader", "cl_aux", "mesh", "vector", "material"]
+             "ref_secondary", "ref_primary", "ref_driver", "ref_mangle", "ref_obj", "ref_sah"]
+# the reference's host sources its OBJ import and CPU SAH BVH need, compiled
+# where they lie
+REF_HOST_SOURCES = ["obj-loader", "cl_aux", "mesh", "vector", "material", "bbox", "bvh"]
 # per-unit flags: mangler.cl has no fp64 pragma, so its constants are floats
 REF_UNIT_FLAGS = {"ref_mangle": ["-fsingle-precision-constant"]}
 
@@ -73,7 +74,7 @@ def build_ref(force=False):
     def one(unit):
         src = os.path.join(shim, unit + ".cpp")
         obj = os.path.join(outdir, unit + ".o")
-        extra = host_inc if unit == "ref_obj" else []
+        extra = host_inc if unit in ("ref_obj", "ref_sah") else []
         _run([CXX] + FLAGS + REF_UNIT_FLAGS.get(unit, []) + extra +
              ["-fno-semantic-interposition", "-w", "-I", kdir, "-c", src, "-o", obj])
         return obj

@@ -65,6 +65,8 @@ class Oracle(_Lib):
         self.multi_shadow_raw = b(L, "orc_multi_shadow", C.c_int, [P, P, I32, P, C.c_int])
         self.multi_render_raw = b(L, "orc_multi_render", C.c_int,
                                   [P, P, I32, I32, I32, SZ, P, P, C.c_int])
+        self.build_sah_raw = b(L, "orc_build_sah", C.c_int, [P])
+        self.sah_nodes_raw = b(L, "orc_sah_nodes", C.c_int, [P, P, P, P, P, P, P, C.POINTER(U32)])
 
     def multi(self, scene_handles, inst_scene, tr, trinv, lights):
         """Multi-root scene over built oracle scenes; tr / trinv: float32 [n, 4, 4]."""
@@ -129,6 +131,27 @@ class OracleScene:
         r = self.o.build(self.h, depth, min_leaf, sort_kind)
         if r:
             raise RuntimeError("oracle build failed")
+
+    def build_sah(self):
+        """The reference's CPU SAH BVH over the current triangle order."""
+        r = self.o.build_sah_raw(self.h)
+        if r == -2:
+            raise ValueError("SAH tree deeper than the traversal's 32-entry stack")
+        if r:
+            raise RuntimeError("oracle SAH build failed")
+
+    def sah_nodes(self):
+        """(lo, hi, a, b, leaf, order) of the SAH tree in the reference's numbering."""
+        cnt = U32(0)
+        self.o.sah_nodes_raw(self.h, None, None, None, None, None, None, C.byref(cnt))
+        m = cnt.value
+        lo, hi = np.zeros((m, 3), np.float32), np.zeros((m, 3), np.float32)
+        a, b, leaf = (np.zeros(m, np.uint32) for _ in range(3))
+        order = np.zeros(self.n, np.uint32)
+        if self.o.sah_nodes_raw(self.h, _p(lo), _p(hi), _p(a), _p(b), _p(leaf), _p(order),
+                                C.byref(cnt)):
+            raise RuntimeError("no SAH tree")
+        return lo, hi, a, b, leaf, order
 
     def sort_arrays(self):
         n = self.n
@@ -253,11 +276,29 @@ class RefKernels(_Lib):
                                                     C.POINTER(U32)])
         self.obj_copy = b(L, "refo_copy", None, [P, P, P, P, P, P, P, P])
         self.obj_free = b(L, "refo_free", None, [P])
+        self.sah_build_raw = b(L, "refs_build", P, [P, U32, P, U32, C.POINTER(U32)])
+        self.sah_copy = b(L, "refs_copy", None, [P, P, P, P, P, P, P])
+        self.sah_free = b(L, "refs_free", None, [P])
 
     multi = Oracle.multi
     multi_trace = Oracle.multi_trace
     multi_shadow = Oracle.multi_shadow
     multi_render = Oracle.multi_render
+
+    def sah_build(self, pos4, idx):
+        """BVH::construct of the reference over (pos4, idx): (lo, hi, a, b,
+        leaf, order) in its numbering."""
+        pos4 = np.ascontiguousarray(pos4, np.float32)
+        idx = np.ascontiguousarray(idx, np.uint32)
+        cnt = U32(0)
+        h = self.sah_build_raw(_p(pos4), pos4.shape[0], _p(idx), idx.shape[0], C.byref(cnt))
+        m = cnt.value
+        lo, hi = np.zeros((m, 3), np.float32), np.zeros((m, 3), np.float32)
+        a, b, leaf = (np.zeros(m, np.uint32) for _ in range(3))
+        order = np.zeros(idx.shape[0], np.uint32)
+        self.sah_copy(h, _p(lo), _p(hi), _p(a), _p(b), _p(leaf), _p(order))
+        self.sah_free(h)
+        return lo, hi, a, b, leaf, order
 
     def obj_load(self, path):
         """The reference's OBJ import: (pos4, nrm4, idx, group starts / ends

@@ -39,6 +39,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <limits>
 #include <thread>
 #include <vector>
 
@@ -123,9 +124,10 @@ struct orc_scene {
     std::vector<uint32_t> perm;        /* sorted slot -> triangle id before the build */
     std::vector<uint32_t> sorted_keys;
     std::vector<uint32_t> orig_id;     /* sorted slot -> triangle id at upload */
-    std::vector<Node> nodes;           /* pre-order, root = 0 */
+    std::vector<Node> nodes;           /* LBVH: pre-order; SAH: the reference's numbering; root = 0 */
     int depth = 30, min_leaf = 1;
     bool built = false;
+    bool sah = false;                  /* built by orc_build_sah (no refit) */
 };
 
 /* ----------------------------------------------------------------------- */
@@ -682,6 +684,175 @@ static void reflect_ray(const rt_sample& in, const rt_hit& info, float refl, flo
 /* ----------------------------------------------------------------------- */
 /* C API                                                                    */
 /* ----------------------------------------------------------------------- */
+
+/* ----------------------------------------------------------------------- */
+/* CPU SAH BVH (BVH::construct / BVHNode::sort, src/rt/bvh.cpp:6-179;       */
+/* BBox, src/rt/bbox.cpp)                                                   */
+/* ----------------------------------------------------------------------- */
+namespace sah {
+
+/* std::max / std::min, which BBox uses: (a < b) ? b : a, (b < a) ? b : a. */
+static inline float smax(float a, float b) { return a < b ? b : a; }
+static inline float smin(float a, float b) { return b < a ? b : a; }
+
+struct Box {
+    float lo[3], hi[3];
+};
+
+/* BBox::reset (bbox.cpp:8-16): hi = FLT_MIN (the least positive normal
+ * float, not -FLT_MAX), lo = FLT_MAX.  A merge with such a box raises every
+ * negative maximum to FLT_MIN. */
+static Box empty_box() {
+    Box b;
+    for (int c = 0; c < 3; ++c) {
+        b.hi[c] = std::numeric_limits<float>::min();
+        b.lo[c] = std::numeric_limits<float>::max();
+    }
+    return b;
+}
+
+static inline void merge(Box& a, const Box& b) {   /* BBox::merge, bbox.cpp:30-35 */
+    for (int c = 0; c < 3; ++c) {
+        a.hi[c] = smax(a.hi[c], b.hi[c]);
+        a.lo[c] = smin(a.lo[c], b.lo[c]);
+    }
+}
+
+static inline float centroid(const Box& b, int ax) { return (b.hi[ax] + b.lo[ax]) * 0.5f; }
+
+static inline float area(const Box& b) {           /* BBox::surfaceArea, bbox.cpp:79-86 */
+    float d[3];
+    for (int c = 0; c < 3; ++c) d[c] = smax(b.hi[c] - b.lo[c], 0.f);
+    return (d[0] * (d[1] + d[2]) + d[1] * d[2]) * 2.f;
+}
+
+static inline int largest_axis(const Box& b) {     /* BBox::largestAxis, bbox.cpp:49-68 */
+    const float dx = b.hi[0] - b.lo[0], dy = b.hi[1] - b.lo[1], dz = b.hi[2] - b.lo[2];
+    if (dx > dy && dx > dz) return 0;
+    if (dy > dz) return 1;
+    return 2;
+}
+
+/* uint32_t(32 * ((c - min) / length)) clamped to 31: the position lies in
+ * [0, 32], or is NaN on a flat axis, which converts to 0. */
+static inline uint32_t bucket_of(float x) {
+    if (!(x > 0.f)) return 0;
+    if (x >= 31.f) return 31;
+    return (uint32_t)x;
+}
+
+constexpr uint32_t BUCKETS = 32;        /* BVH::SAH_BUCKETS */
+constexpr uint32_t MIN_PRIMS = 2;       /* BVH::MIN_PRIMS_PER_NODE */
+constexpr uint32_t MAX_INTERIOR_DEPTH = 31;   /* the traversal's 32-entry stack */
+
+struct Builder {
+    const std::vector<Box>& boxes;
+    std::vector<uint32_t>& ot;
+    std::vector<Node>& nodes;
+    bool too_deep = false;
+
+    /* chooseSplitLocationSAH (bvh.cpp:242-313): buckets over the centroid
+     * range of the node box on `axis`; cost of the split after bucket i,
+     * whose right side starts from the last bucket and then merges buckets
+     * i+1..31 again (the last bucket is counted twice); the first least
+     * cost wins; split at the first triangle whose centroid reaches the
+     * bucket boundary. */
+    uint32_t choose(const Box& bb, int axis, uint32_t start, uint32_t end) const {
+        const float len = bb.hi[axis] - bb.lo[axis];
+        const float mn = bb.lo[axis];
+        const float sa = area(bb);
+        uint32_t prims[BUCKETS];
+        Box bbox[BUCKETS];
+        for (uint32_t k = 0; k < BUCKETS; ++k) {
+            prims[k] = 0;
+            bbox[k] = empty_box();
+        }
+        for (uint32_t i = start; i < end; ++i) {
+            const Box& t = boxes[ot[i]];
+            const float c = centroid(t, axis);
+            const uint32_t slot = bucket_of((float)BUCKETS * ((c - mn) / len));
+            prims[slot]++;
+            merge(bbox[slot], t);
+        }
+        float cost[BUCKETS - 1];
+        for (uint32_t i = 0; i < BUCKETS - 1; ++i) {
+            Box bl = bbox[0], br = bbox[BUCKETS - 1];
+            uint32_t nl = prims[0], nr = prims[BUCKETS - 1];
+            for (uint32_t j = 1; j <= i; ++j) {
+                merge(bl, bbox[j]);
+                nl += prims[j];
+            }
+            for (uint32_t j = i + 1; j < BUCKETS; ++j) {
+                merge(br, bbox[j]);
+                nr += prims[j];
+            }
+            cost[i] = .125f + ((float)nl * area(bl) + (float)nr * area(br)) / sa;
+        }
+        float best = cost[0];
+        uint32_t best_i = 0;
+        for (uint32_t i = 1; i < BUCKETS - 1; ++i)
+            if (cost[i] < best) {
+                best = cost[i];
+                best_i = i;
+            }
+        float split_value = mn;
+        split_value += (float)(best_i + 1) * (len / (float)BUCKETS);
+        uint32_t i = start;
+        for (; i < end; ++i)
+            if (centroid(boxes[ot[i]], axis) >= split_value) break;
+        return i;
+    }
+
+    /* BVHNode::sort (bvh.cpp:6-90): node `me` over ot[start, end). */
+    void sort(uint32_t me, uint32_t start, uint32_t end, uint32_t depth) {
+        Box bb = boxes[ot[start]];
+        for (uint32_t i = start; i < end; ++i) merge(bb, boxes[ot[i]]);
+        Node nd;
+        std::memset(&nd, 0, sizeof nd);
+        for (int c = 0; c < 3; ++c) {
+            nd.lo[c] = bb.lo[c];
+            nd.hi[c] = bb.hi[c];
+        }
+        nd.start = start;
+        nd.end = end;
+        nd.depth = depth;
+        nd.leaf = 1;
+        nd.a = start;
+        nd.b = end;
+        if (end - start <= MIN_PRIMS) {
+            nodes[me] = nd;
+            return;
+        }
+        int axis = largest_axis(bb);
+        uint32_t split = start;
+        for (int tries = 0; tries < 2; ++tries) {
+            std::sort(ot.begin() + start, ot.begin() + end, [&](uint32_t x, uint32_t y) {
+                return centroid(boxes[x], axis) < centroid(boxes[y], axis);
+            });
+            split = choose(bb, axis, start, end);
+            if (split == start || split == end)
+                axis = (axis + 1) % 3;
+            else
+                break;
+        }
+        if (split == start || split == end) {
+            nodes[me] = nd;
+            return;
+        }
+        if (depth > MAX_INTERIOR_DEPTH) too_deep = true;
+        nodes.resize(nodes.size() + 2);
+        const uint32_t l = (uint32_t)nodes.size() - 2, r = l + 1;
+        nd.leaf = 0;
+        nd.a = l;
+        nd.b = r;
+        nodes[me] = nd;
+        sort(l, start, split, depth + 1);
+        sort(r, split, end, depth + 1);
+    }
+};
+
+}  // namespace sah
+
 extern "C" {
 
 orc_scene* orc_scene_new(const float* pos4, const float* nrm4, uint32_t V, const uint32_t* idx,
@@ -792,6 +963,71 @@ int orc_build(orc_scene* s, int depth, int min_leaf, int sort_kind) {
     return 0;
 }
 
+/* BVH::construct (bvh.cpp:92-141) over the scene's triangles in their
+ * current order: boxes by BBox::set (bbox.cpp:24-28), the recursive SAH
+ * split, then the triangles (indices, materials, ids) reordered like
+ * Mesh::reorderTriangles.  -2 when an interior node lies deeper than the
+ * traversal's 32-entry stack reaches. */
+int orc_build_sah(orc_scene* s) {
+    if (s->N == 0) return -1;
+    const uint32_t N = s->N;
+    std::vector<sah::Box> boxes(N);
+    for (uint32_t i = 0; i < N; ++i) {
+        const float* p0 = &s->pos[4 * (size_t)s->idx[3 * (size_t)i + 0]];
+        const float* p1 = &s->pos[4 * (size_t)s->idx[3 * (size_t)i + 1]];
+        const float* p2 = &s->pos[4 * (size_t)s->idx[3 * (size_t)i + 2]];
+        for (int c = 0; c < 3; ++c) {
+            boxes[i].hi[c] = sah::smax(p0[c], sah::smax(p1[c], p2[c]));
+            boxes[i].lo[c] = sah::smin(p0[c], sah::smin(p1[c], p2[c]));
+        }
+    }
+    std::vector<uint32_t> ot(N);
+    for (uint32_t i = 0; i < N; ++i) ot[i] = i;
+    std::vector<Node> nodes(1);
+    sah::Builder b{boxes, ot, nodes};
+    b.sort(0, 0, N, 0);
+    if (b.too_deep) return -2;
+    std::vector<uint32_t> idx2((size_t)N * 3), map2(N), orig2(N);
+    for (uint32_t i = 0; i < N; ++i) {
+        const uint32_t o = ot[i];
+        for (int k = 0; k < 3; ++k) idx2[3 * (size_t)i + k] = s->idx[3 * (size_t)o + k];
+        map2[i] = s->map[o];
+        orig2[i] = s->orig_id[o];
+    }
+    s->idx.swap(idx2);
+    s->map.swap(map2);
+    s->orig_id.swap(orig2);
+    s->perm = ot;
+    s->keys.clear();
+    s->sorted_keys.clear();
+    s->nodes.swap(nodes);
+    s->built = true;
+    s->sah = true;
+    return 0;
+}
+
+/* The SAH tree in the reference's numbering: per node lo[3], hi[3], (a, b)
+ * = children or the leaf's [start, end), leaf flag; order = slot ->
+ * triangle before the build. */
+int orc_sah_nodes(const orc_scene* s, float* lo, float* hi, uint32_t* a, uint32_t* b,
+                  uint32_t* leaf, uint32_t* order, uint32_t* count) {
+    if (!s->built || !s->sah) return -1;
+    *count = (uint32_t)s->nodes.size();
+    if (!lo) return 0;
+    for (size_t k = 0; k < s->nodes.size(); ++k) {
+        const Node& nd = s->nodes[k];
+        for (int c = 0; c < 3; ++c) {
+            lo[3 * k + c] = nd.lo[c];
+            hi[3 * k + c] = nd.hi[c];
+        }
+        a[k] = nd.a;
+        b[k] = nd.b;
+        leaf[k] = nd.leaf;
+    }
+    std::memcpy(order, s->perm.data(), 4 * (size_t)s->N);
+    return 0;
+}
+
 /* The emit rule alone on given sorted keys (ranges only; AABBs zero). */
 int orc_emit_keys(const uint32_t* sorted_keys, uint32_t n, int depth, int min_leaf,
                   rt_canon_node* out, uint32_t cap, uint32_t* count) {
@@ -819,7 +1055,7 @@ int orc_emit_keys(const uint32_t* sorted_keys, uint32_t n, int depth, int min_le
 
 /* refit_lbvh (bvh-builder.cpp:743-850): new AABBs, same topology and order. */
 int orc_refit(orc_scene* s) {
-    if (!s->built) return -1;
+    if (!s->built || s->sah) return -1;
     refit(s);
     return 0;
 }
@@ -846,8 +1082,21 @@ int orc_export(const orc_scene* s, rt_canon_node* out, uint32_t cap, uint32_t* c
     *count = (uint32_t)s->nodes.size();
     if (!out) return 0;
     if (cap < s->nodes.size()) return -1;
-    for (size_t k = 0; k < s->nodes.size(); ++k) {
-        const Node& nd = s->nodes[k];
+    /* pre-order, left child first (the LBVH's array order already is) */
+    std::vector<uint32_t> todo{0}, order;
+    order.reserve(s->nodes.size());
+    while (!todo.empty()) {
+        const uint32_t k = todo.back();
+        todo.pop_back();
+        order.push_back(k);
+        if (!s->nodes[k].leaf) {
+            todo.push_back(s->nodes[k].b);
+            todo.push_back(s->nodes[k].a);
+        }
+    }
+    for (size_t q = 0; q < order.size(); ++q) {
+        const size_t k = q;
+        const Node& nd = s->nodes[order[q]];
         rt_canon_node c;
         std::memset(&c, 0, sizeof(c));
         c.start = nd.start;

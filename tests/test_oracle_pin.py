@@ -261,3 +261,73 @@ def test_pin_multi_root(orc, ref):
     ref.multi_free(rm)
     for rh in r_h:
         ref.scene_free(rh)
+
+
+def _canon_of_numbered(lo, hi, a, b, leaf):
+    """A tree in the reference's numbering (root 0; children or leaf range in
+    a, b) as canonical pre-order nodes, interior ranges from their subtrees."""
+    out = []
+
+    def walk(k, depth):
+        me = len(out)
+        out.append(None)
+        if leaf[k]:
+            s, e = int(a[k]), int(b[k])
+        else:
+            s, _ = walk(int(a[k]), depth + 1)
+            _, e = walk(int(b[k]), depth + 1)
+        out[me] = (s, e, int(leaf[k]), depth, lo[k], hi[k])
+        return s, e
+
+    walk(0, 0)
+    c = np.zeros(len(out), abi.CANON_DTYPE)
+    for i, (s, e, lf, d, l, h) in enumerate(out):
+        c[i]["start"], c[i]["end"], c[i]["leaf"], c[i]["depth"] = s, e, lf, d
+        c[i]["lo"][:3], c[i]["hi"][:3] = l, h
+    return c
+
+
+def _negative_soup():
+    sc = scenes.soup(2500, seed=8)
+    pos = sc.pos4.copy()
+    pos[:, :3] -= np.float32(5.0)       # every coordinate negative
+    return scenes.Scene(pos, sc.nrm4, sc.idx, sc.mats, sc.mat_map, sc.lights)
+
+
+@pytest.mark.parametrize("kind", ["soup", "terrain", "negative"])
+def test_pin_sah(orc, ref, kind):
+    """BVH::construct (bvh.cpp:92-141) against the oracle's restatement: the
+    same nodes in the same numbering, the same triangle order; and the
+    reference's trace / shadow / shade kernels over the reference's SAH tree
+    against the oracle's render over its own, pixel for pixel.  The negative
+    scene makes the empty-bucket boxes' FLT_MIN maximum count."""
+    sc = {"soup": lambda: scenes.soup(4000, seed=2),
+          "terrain": lambda: tiny_terrain(48, 24, 3).scene(0),
+          "negative": _negative_soup}[kind]()
+    sc.lights = single_light("point")          # the reference's kernels hold one light
+    rlo, rhi, ra, rb, rleaf, rorder = ref.sah_build(sc.pos4, sc.idx)
+    s = orc.new_scene(sc)
+    s.build_sah()
+    olo, ohi, oa, ob, oleaf, oorder = s.sah_nodes()
+    assert np.array_equal(rorder, oorder)
+    assert np.array_equal(rleaf, oleaf)
+    assert np.array_equal(ra, oa) and np.array_equal(rb, ob)
+    assert rlo.tobytes() == olo.tobytes() and rhi.tobytes() == ohi.tobytes()
+    assert int(rleaf.sum()) > sc.n_tris // 3
+    canon = _canon_of_numbered(rlo, rhi, ra, rb, rleaf)
+    assert s.canon().tobytes() == canon.tobytes()
+    rh = ref.new_scene(sc)
+    ref.apply_perm(rh, _p(rorder))
+    assert ref.set_tree(rh, _p(canon), canon.shape[0]) == 0
+    cam = camera_small() if kind != "negative" else scenes.camera((-5.0, -4.0, -9.0),
+                                                                  (-5.0, -5.0, -5.0))
+    w = h = 160
+    img_r = np.zeros((w * h, 3), np.uint32)
+    st_r = abi.RenderStats()
+    assert ref.render(rh, C.byref(cam), w, h, 3, 0, w * h, 1 << 20, _p(img_r), C.byref(st_r),
+                      4) == 0
+    img_o, st_o = s.render(cam, w, h, 3, tile=1 << 20)
+    assert st_o.hits > 1000
+    assert np.array_equal(img_o, img_r)
+    assert st_o.secondary_rays == st_r.secondary_rays   # the driver counts no hits
+    ref.scene_free(rh)
