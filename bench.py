@@ -502,6 +502,53 @@ def measure_instances(ctx, torch, frames=5):
     return out
 
 
+def measure_sah(ctx, torch, frames=5):
+    """LBVH against the reference's CPU SAH BVH (rt_bvh_build_sah) on a
+    1M-triangle soup (the small workload's kind of scene; the mid-scale
+    terrain's SAH tree is 36 levels deep, beyond the traversal's 32-entry
+    stack, and is refused): the SAH build's wall time (device to host copy,
+    the host build on all cores, the tree back on the device) and the same
+    1920x1080 depth-4 frame rendered over either tree."""
+    from rtgb import capi, scenes
+    sc = scenes.soup(1_000_000, seed=1)
+    cam = scenes.camera((0.0, 0.0, -4.0), (0.0, 0.0, 0.0), fov_deg=60.0, aspect=1920 / 1080)
+    wl = {"camera": cam, "width": 1920, "height": 1080, "max_bounces": 4}
+    stream = torch.cuda.Stream()
+    sh = C.c_void_p(stream.cuda_stream)
+    w, h, nb = wl["width"], wl["height"], wl["max_bounces"]
+    rgba = ctx.alloc(4 * w * h)
+    stats = ctx.alloc(32)
+    out = {"workload": "soup1M_1920x1080_d4", "triangles": sc.n_tris,
+           "host_threads": os.cpu_count()}
+    for kind in ("lbvh", "sah"):
+        g = capi.Scene(ctx, sc)
+        stream.synchronize()
+        t0 = time.perf_counter()
+        if kind == "sah":
+            g.build_sah(stream=sh)
+        else:
+            g.build(30, 1, stream=sh)
+        stream.synchronize()
+        t_build = time.perf_counter() - t0
+        g.render(wl["camera"], w, h, nb, rgba, None, None, stream=sh)
+        stats.zero(sh)
+        ts = []
+        for _ in range(frames):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            g.render(wl["camera"], w, h, nb, rgba, None, stats, stream=sh)
+            e1.record(stream)
+            stream.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        st = stats.read(np.uint64)
+        out[kind] = {"build_wall_ms": t_build * 1e3, "render_ms": statistics.median(ts),
+                     "mrays_s": int(st[0] + st[1]) / (sum(ts) * 1e-3) / 1e6,
+                     "image_crc": int(np.bitwise_xor.reduce(rgba.read(np.uint32)))}
+        g.close()
+    out["device_status"] = ctx.device_status()
+    return out
+
+
 def measure_served(ctx, rates=(2000, 1000, 300, 50), n_req=400, seed=5):
     """Served workload: 32 resident scenes (soups and fBm fields alternating,
     10k-2M triangles log-uniform), a 120 GB admission budget and a scene cap
@@ -783,6 +830,12 @@ def run_gpu(args):
             refraction_leg = measure_refraction(ctx, torch)
         except Exception as e:
             refraction_leg = {"error": str(e)}
+    sah_leg = None
+    if world == 1 and not args.no_sah:
+        try:
+            sah_leg = measure_sah(ctx, torch)
+        except Exception as e:
+            sah_leg = {"error": str(e)}
     instances_leg = None
     if world == 1 and not args.no_instances:
         try:
@@ -828,6 +881,7 @@ def run_gpu(args):
            "obj": obj_leg,
            "refraction": refraction_leg,
            "instances": instances_leg,
+           "sah": sah_leg,
            "e2e": {"value": e2e_value, "unit": UNIT,
                    "h2d_bytes_per_step": 2 * 16 * V,
                    "d2h_bytes_per_step": 4 * w * h + 32,
@@ -859,6 +913,7 @@ def main():
     ap.add_argument("--no-obj", action="store_true")
     ap.add_argument("--no-refraction", action="store_true")
     ap.add_argument("--no-instances", action="store_true")
+    ap.add_argument("--no-sah", action="store_true")
     ap.add_argument("--render-variant", type=int, default=None,
                     help="render kernel variant instead of the autotuner's pick")
     ap.add_argument("--render-blocks", type=int, default=0, help="resident blocks per SM (0: all)")

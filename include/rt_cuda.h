@@ -297,6 +297,13 @@ RT_API int32_t rt_bvh_build_lbvh(rt_ctx* ctx, rt_scene* scene, const rt_bvh_cfg*
 /* BVHBuilder::refit_lbvh (src/rt/bvh-builder.cpp:743-850): recompute AABBs on
  * the existing topology and triangle order. */
 RT_API int32_t rt_bvh_refit_lbvh(rt_ctx* ctx, rt_scene* scene, rt_stream s);
+/* The reference's CPU SAH BVH (BVH::construct, src/rt/bvh.cpp:6-179) over the
+ * scene's triangles in their current order, built on the host's threads and
+ * laid out as the LBVH's device tree (the triangles reordered likewise), so
+ * that every render call traverses it; returns when it is on the device.
+ * RT_ERR_INVALID when an interior node lies deeper than the traversal's
+ * 32-entry stack; such a tree cannot be refit (build it again). */
+RT_API int32_t rt_bvh_build_sah(rt_ctx* ctx, rt_scene* scene, rt_stream s);
 /* Canonical pre-order tree (synchronous).  *count receives the node count;
  * pass out == NULL to query it. */
 RT_API int32_t rt_bvh_export(rt_ctx* ctx, rt_scene* scene, rt_canon_node* out,

@@ -17,10 +17,12 @@
 #include <algorithm>
 #include <cmath>
 #include <new>
+#include <thread>
 #include <vector>
 
 #include "../../include/rt_cuda.h"
 #include "lbvh.cuh"
+#include "sah.cuh"
 #include "rt_internal.cuh"
 #include "trace.cuh"
 #include "ctx_internal.h"
@@ -721,12 +723,56 @@ int32_t rt_bvh_build_lbvh(rt_ctx* c, rt_scene* s, const rt_bvh_cfg* cfg, rt_stre
     CU(scene_write_end(s, cs));
     s->cur ^= 1;   // the sorted index buffer / material map are now current
     s->built = true;
+    s->sah = false;
+    return RT_OK;
+}
+
+int32_t rt_bvh_build_sah(rt_ctx* c, rt_scene* s, rt_stream stream) {
+    if (!c || !s) return fail(RT_ERR_INVALID, "rt_bvh_build_sah: null argument");
+    if (s->N == 0) return fail(RT_ERR_INVALID, "rt_bvh_build_sah: scene has no triangles");
+    int32_t r = rt::scene_ensure_build(s);
+    if (r) return r;
+    cudaStream_t cs = st(c, stream);
+    CU(scene_write_begin(s, cs));
+    CU(cudaEventRecord(s->ev0, cs));
+    // the reference builds this tree on the host from its own copy of the mesh
+    std::vector<float4> pos(s->V);
+    std::vector<uint32_t> idx(3 * (size_t)s->N);
+    CU(cudaMemcpyAsync(pos.data(), s->d_pos, sizeof(float4) * s->V, cudaMemcpyDeviceToHost, cs));
+    CU(cudaMemcpyAsync(idx.data(), s->d_idx[s->cur], 12 * (size_t)s->N, cudaMemcpyDeviceToHost,
+                       cs));
+    CU(cudaStreamSynchronize(cs));
+    rt::SahTree t;
+    const unsigned hw = std::thread::hardware_concurrency();
+    const int rc = rt::sah_build(pos.data(), s->V, idx.data(), s->N,
+                                 hw ? (int)std::min(hw, 64u) : 1, &t);
+    if (rc == -2)
+        return fail(RT_ERR_INVALID, "rt_bvh_build_sah: the tree is deeper than the traversal's "
+                    "32-entry stack");
+    if (rc) return fail(RT_ERR_INVALID, "rt_bvh_build_sah: vertex index out of range");
+    rt::LbvhArgs a = lbvh_args(c, s);
+    CU(cudaMemcpyAsync(s->d_vals_sorted, t.order.data(), 4 * (size_t)s->N, cudaMemcpyHostToDevice,
+                       cs));
+    if (!t.nodes.empty())
+        CU(cudaMemcpyAsync(s->d_nodes, t.nodes.data(), sizeof(float4) * t.nodes.size(),
+                           cudaMemcpyHostToDevice, cs));
+    CU(cudaMemcpyAsync(s->d_hdr, &t.hdr, sizeof(t.hdr), cudaMemcpyHostToDevice, cs));
+    CU(rt::lbvh_permute(a, s->d_vals_sorted, cs));
+    CU(cudaEventRecord(s->ev1, cs));
+    CU(cudaStreamSynchronize(cs));   // the host tree lives until its copies are done
+    CU(scene_write_end(s, cs));
+    s->cur ^= 1;
+    s->built = true;
+    s->sah = true;
     return RT_OK;
 }
 
 int32_t rt_bvh_refit_lbvh(rt_ctx* c, rt_scene* s, rt_stream stream) {
     if (!c || !s) return fail(RT_ERR_INVALID, "rt_bvh_refit_lbvh: null argument");
     if (!s->built) return fail(RT_ERR_NOT_BUILT, "rt_bvh_refit_lbvh: no BVH built");
+    if (s->sah)
+        return fail(RT_ERR_INVALID, "rt_bvh_refit_lbvh: the tree came from rt_bvh_build_sah; "
+                    "build it again");
     cudaStream_t cs = st(c, stream);
     CU(scene_write_begin(s, cs));
     CU(cudaEventRecord(s->ev0, cs));

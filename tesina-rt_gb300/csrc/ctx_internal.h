@@ -69,6 +69,7 @@ struct rt_scene {
     uint32_t buildN = 0;             // capacity of the build buffers
     bool built = false;
     bool refracts = false;           // some material has refractive_index > 0
+    bool sah = false;                // the tree came from rt_bvh_build_sah (no refit)
     int depth = 30, min_leaf = 1;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     // Order of the rt_* calls on this scene across streams: the completion

@@ -297,6 +297,14 @@ cudaError_t radix_sort_pairs(const uint32_t* kin, const uint32_t* vin, uint32_t*
     return cudaGetLastError();
 }
 
+cudaError_t lbvh_permute(const LbvhArgs& a, const uint32_t* order, cudaStream_t s) {
+    k_permute<<<grid_for(a.n, 256, a.num_sms * 16), 256, 0, s>>>(a.n, order, a.idx_in, a.map_in,
+                                                                 a.orig_in, a.pos, a.idx_out,
+                                                                 a.map_out, a.orig_out, a.tris,
+                                                                 a.leafbox);
+    return cudaGetLastError();
+}
+
 cudaError_t lbvh_refit(const LbvhArgs& a, cudaStream_t s) {
     const uint32_t n = a.n;
     k_refit_leaves<<<grid_for(n, 256, a.num_sms * 16), 256, 0, s>>>(n, a.idx_out, a.pos, a.tris,

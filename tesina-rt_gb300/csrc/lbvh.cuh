@@ -45,6 +45,10 @@ cudaError_t launch_mangle(float4* pos, float4* nrm, uint32_t V, float arg, float
                           cudaStream_t s);
 cudaError_t lbvh_build(const LbvhArgs& a, cudaStream_t s);
 cudaError_t lbvh_refit(const LbvhArgs& a, cudaStream_t s);
+// The triangle data (indices, materials, ids, triangle records, leaf boxes)
+// of a.*_in rearranged into a.*_out by `order` (slot -> triangle), as the
+// LBVH build does with its sorted permutation.
+cudaError_t lbvh_permute(const LbvhArgs& a, const uint32_t* order, cudaStream_t s);
 
 // Stable LSD radix sort of (key, value) pairs on the low key_bits bits with
 // caller-provided scratch (radix_scratch_words words) and temporaries of n

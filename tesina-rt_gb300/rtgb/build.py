@@ -14,10 +14,12 @@ CSRC = os.path.join(PKG, "csrc")
 LIB = os.path.join(PKG, "librt_cuda.so")
 OBJDIR = os.path.join(PKG, "_build")
 NVCC = os.environ.get("NVCC", "nvcc")
-UNITS = ["lbvh", "trace", "capi", "noalloc", "batch", "batch_api", "server", "animate", "obj", "instances"]
+UNITS = ["lbvh", "trace", "capi", "noalloc", "batch", "batch_api", "server", "animate", "obj", "instances", "sah"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# host code as the device code: no fused multiply-add (gcc contracts by default
+# where the machine has FMA, as the Arm hosts do)
 FLAGS = ARCH + ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
-                "-Xcompiler", "-fvisibility=hidden"]
+                "-Xcompiler", "-fvisibility=hidden", "-Xcompiler", "-ffp-contract=off"]
 
 
 def _run(cmd):

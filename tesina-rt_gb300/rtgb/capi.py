@@ -44,6 +44,7 @@ SIGNATURES = {
     "rt_scene_read_orig": (I32, [P, P, P]),
     "rt_bvh_build_lbvh": (I32, [P, P, P, P]),
     "rt_bvh_refit_lbvh": (I32, [P, P, P]),
+    "rt_bvh_build_sah": (I32, [P, P, P]),
     "rt_scene_mangle": (I32, [P, P, F, F, F, P]),
     "rt_obj_load": (I32, [C.c_char_p, C.POINTER(P)]),
     "rt_obj_info": (I32, [P, C.POINTER(U32), C.POINTER(U32), C.POINTER(U32)]),
@@ -292,6 +293,10 @@ class Scene:
 
     def refit(self, stream=None):
         check(self.lib, self.lib.rt_bvh_refit_lbvh(self.ctx.h, self.h, stream))
+
+    def build_sah(self, stream=None):
+        """The reference's CPU SAH BVH, on the host, then on the device."""
+        check(self.lib, self.lib.rt_bvh_build_sah(self.ctx.h, self.h, stream))
 
     def mangle(self, arg, last_arg=-1000.0, height=0.2, stream=None):
         """Device-side vertex animation (mangler.cl); follow with refit() or build()."""

@@ -141,3 +141,24 @@ def test_bitonic_sorts_and_is_unstable(orc):
     assert not np.array_equal(p, stable)     # same key runs, different order
     for v in range(8):
         assert set(p[keys[p] == v]) == set(stable[keys[stable] == v])
+
+
+def test_oracle_sah_refuses_deep_trees(orc):
+    """The oracle's SAH build refuses a tree deeper than the traversal's
+    32-entry stack (240 tiny triangles at x = 2^k, k = -120..119: 44 levels)."""
+    c = (2.0 ** np.arange(-120, 120)).astype(np.float32)
+    n = c.shape[0]
+    pos = np.zeros((3 * n, 4), np.float32)
+    pos[:, 0] = np.repeat(c, 3)
+    pos[1::3, 1] = 1e-3
+    pos[2::3, 2] = 1e-3
+    base = scenes.soup(n, seed=1)
+    sc = scenes.Scene(pos, pos.copy(), np.arange(3 * n, dtype=np.uint32).reshape(-1, 3),
+                      base.mats, base.mat_map, base.lights)
+    s = orc.new_scene(sc)
+    with pytest.raises(ValueError):
+        s.build_sah()
+    s2 = orc.new_scene(scenes.soup(3000, seed=3))
+    s2.build_sah()
+    c2 = s2.canon()
+    assert c2["depth"].max() <= 32 and c2[c2["leaf"] == 1]["end"].max() == 3000
