@@ -1070,9 +1070,10 @@ int32_t rt_render(rt_ctx* c, rt_scene* s, const rt_camera* cam, int32_t w, int32
     a.work_counter = work;
     a.status = c->d_status;
     rt_render_config cfg = c->render_cfg;
-    if (s->refracts && !rt::render_variant_refracts(cfg.variant)) {
-        // refracting materials branch each hit: the variant that walks ray trees
-        cfg.variant = rt::render_refract_variant();
+    if ((s->refracts && !rt::render_variant_refracts(cfg.variant)) ||
+        !rt::render_variant_fits(cfg.variant, max_bounces)) {
+        // refracting materials branch each hit: a variant that follows both rays
+        cfg.variant = rt::render_refract_variant(max_bounces);
         cfg.blocks_per_sm = 0;
     }
     CU(scene_read_begin(s, cs));
@@ -1134,6 +1135,7 @@ int32_t rt_autotune_render(rt_ctx* c, rt_scene* s, const rt_camera* cam, int32_t
     const int chunks[] = {32, 64, 128};
     for (int v = 0; v < rt::render_variant_count(); ++v) {
         if (rt::render_variant_refracts(v) != s->refracts) continue;   // the variants that fit the scene
+        if (!rt::render_variant_fits(v, max_bounces)) continue;
         // full residency, one and two blocks fewer (more L1 per block:
         // the carveout follows the launched blocks), and half residency
         const int occ = c->variant_occupancy[v];

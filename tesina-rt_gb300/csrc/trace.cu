@@ -250,6 +250,204 @@ __global__ void __launch_bounds__(THREADS, MINB) k_render_pool(RenderArgs a) {
 }
 
 // ---------------------------------------------------------------------------
+// k_render_pool_refr: k_render_pool for scenes with refracting materials.  A
+// hit may continue two rays (the refracted one, contribution * reflectiveness
+// * (1 - R), and the reflected one, * R, as generate_secondary_rays_disc
+// makes them), and both go into the warp's pool.  The pool is taken from the
+// top (last in, first out), so it holds at most 32 (max_bounces + 2) rays;
+// it is sized for max_bounces <= REFR_POOL_MAXB (deeper frames use the
+// ray-tree variant) and a push beyond it raises RT_DEV_OVERFLOW instead of
+// writing.  Sums are integers, so the image is the ray-tree variant's.
+// ---------------------------------------------------------------------------
+namespace {
+constexpr int RPOOL = 32 * (REFR_POOL_MAXB + 2);
+
+struct RefrPool {
+    float ro[3][RPOOL], rd[3][RPOOL], rc[RPOOL];
+    int rpix[RPOOL], rbounce[RPOOL];
+    float hp[3][32], hn[3][32], hd[3][32], hc[32];
+    int hid[32], hpix[32], hbounce[32];
+    unsigned hmask[32];
+    unsigned char hinv[32];
+    int pool_n;
+};
+}  // namespace
+
+template <int THREADS, int MINB>
+__global__ void __launch_bounds__(THREADS, MINB) k_render_pool_refr(RenderArgs a) {
+    const SceneView S = a.scene;
+    __shared__ BvhHeader sH;
+    __shared__ rt_lights sL;
+    __shared__ RefrPool sQ[THREADS / 32];
+    if (threadIdx.x == 0) sH = *S.hdr;
+    for (int i = threadIdx.x; i < (int)(sizeof(rt_lights) / 4); i += blockDim.x)
+        reinterpret_cast<uint32_t*>(&sL)[i] = reinterpret_cast<const uint32_t*>(&a.lights)[i];
+    const int lane = threadIdx.x & 31;
+    RefrPool& Q = sQ[threadIdx.x >> 5];
+    if (lane == 0) Q.pool_n = 0;
+    __syncthreads();
+    const BvhHeader& H = sH;
+    const int pixels = a.width * a.height;
+    const unsigned lt = (1u << lane) - 1u;
+    uint64_t n_sec = 0, n_shadow = 0, n_hits = 0, n_prim = 0;
+    bool tiles = true;
+    for (;;) {
+        const int pn = Q.pool_n;
+        bool have = false;
+        f3 o = mk3(0.f, 0.f, 0.f), d = o;
+        float c = 1.0f, tmin = 0.0f, tmax = 1e36f;
+        int pix = 0, bounce = 0;
+        if (pn >= 32 || (!tiles && pn > 0)) {
+            const int k = min(32, pn);
+            const int j = pn - k + lane;
+            have = lane < k;
+            if (have) {
+                o = mk3(Q.ro[0][j], Q.ro[1][j], Q.ro[2][j]);
+                d = mk3(Q.rd[0][j], Q.rd[1][j], Q.rd[2][j]);
+                c = Q.rc[j];
+                pix = Q.rpix[j];
+                bounce = Q.rbounce[j];
+                tmin = 0.0001f;
+                tmax = 1e37f;
+            }
+            __syncwarp();
+            if (lane == 0) Q.pool_n = pn - k;
+        } else if (tiles) {
+            int base = 0;
+            if (lane == 0) base = (int)atomicAdd(a.work_counter, 32u);
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (base >= pixels) {
+                tiles = false;
+                continue;
+            }
+            const int gid = base + lane;
+            have = gid < pixels;
+            if (have) {
+                int x, y;
+                pixel_of(warp_tile_order(gid, a.width, a.height), a.width, a.height, 32, x, y);
+                pix = a.width * y + x;
+                o = mk3(a.cam.pos[0], a.cam.pos[1], a.cam.pos[2]);
+                d = primary_dir(a.cam, x, y, a.width, a.height, 0.0f, 0.0f);
+                ++n_prim;
+            }
+        } else {
+            break;
+        }
+        bool hit_ok = false;
+        Hit hit{-1, 0.f, 0.f, 0.f};
+        if (have) {
+            const TRay r = make_tray(o, d, mk3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z), tmin);
+            hit = closest_hit(S, H, r, tmax, a.status);
+            hit_ok = hit.id >= 0;
+        }
+        const unsigned hm = __ballot_sync(0xffffffffu, hit_ok);
+        const int nh = __popc(hm);
+        if (hit_ok) {
+            const int k = __popc(hm & lt);
+            const HitInfo hi = complete_hit(S, o, d, hit);
+            Q.hp[0][k] = hi.hp.x; Q.hp[1][k] = hi.hp.y; Q.hp[2][k] = hi.hp.z;
+            Q.hn[0][k] = hi.n.x; Q.hn[1][k] = hi.n.y; Q.hn[2][k] = hi.n.z;
+            Q.hd[0][k] = d.x; Q.hd[1][k] = d.y; Q.hd[2][k] = d.z;
+            Q.hc[k] = c;
+            Q.hid[k] = hit.id;
+            Q.hpix[k] = pix;
+            Q.hbounce[k] = bounce;
+            Q.hinv[k] = hi.inverse_n;
+            Q.hmask[k] = 0u;
+        }
+        __syncwarp();
+        const int nl = sL.count;
+        for (int t = lane; t < nh * nl; t += 32) {
+            const int k = t / nl, l = t - k * nl;
+            const f3 p = mk3(Q.hp[0][k], Q.hp[1][k], Q.hp[2][k]);
+            if (occluded(S, H, sL.light[l], p, a.status)) atomicOr(&Q.hmask[k], 1u << l);
+        }
+        __syncwarp();
+        // shading; the continuing rays of each hit: reflected, refracted
+        bool push_r = false, push_t = false;
+        f3 np = mk3(0.f, 0.f, 0.f), nd = np, td = np;
+        float nc = 0.f, tc = 0.f;
+        int npix = 0, nbounce = 0;
+        if (lane < nh) {
+            const int k = lane;
+            const f3 p = mk3(Q.hp[0][k], Q.hp[1][k], Q.hp[2][k]);
+            const f3 n = mk3(Q.hn[0][k], Q.hn[1][k], Q.hn[2][k]);
+            const f3 dk = mk3(Q.hd[0][k], Q.hd[1][k], Q.hd[2][k]);
+            const float ck = Q.hc[k];
+            const rt_material mat = S.mats[__ldg(&S.map[Q.hid[k]])];
+            const uint3 col = shade_hit(sL, mat, p, n, dk, ck, Q.hmask[k]);
+            const int pk = Q.hpix[k];
+            atomicAdd(&a.accum[3 * (size_t)pk], col.x);
+            atomicAdd(&a.accum[3 * (size_t)pk + 1], col.y);
+            atomicAdd(&a.accum[3 * (size_t)pk + 2], col.z);
+            ++n_hits;
+            n_shadow += (uint32_t)nl;
+            const int bk = Q.hbounce[k];
+            if (bk < a.max_bounces) {
+                float R = 1.0f;
+                if (mat.refractive_index > 0.0f &&
+                    refract_ray(dk, n, Q.hinv[k] != 0, mat.refractive_index, R, td)) {
+                    tc = ck * mat.reflectiveness * (1.0f - R);
+                    push_t = true;
+                }
+                if (mat.reflectiveness > 0.0f) {
+                    reflect_ray(dk, n, nd);
+                    nc = ck * mat.reflectiveness * R;
+                    push_r = true;
+                }
+                np = p;
+                npix = pk;
+                nbounce = bk + 1;
+            }
+        }
+        const unsigned pr = __ballot_sync(0xffffffffu, push_r);
+        const unsigned pt = __ballot_sync(0xffffffffu, push_t);
+        const int pbase = Q.pool_n;
+        if (push_r) {
+            const int j = pbase + __popc(pr & lt);
+            if (j < RPOOL) {
+                Q.ro[0][j] = np.x; Q.ro[1][j] = np.y; Q.ro[2][j] = np.z;
+                Q.rd[0][j] = nd.x; Q.rd[1][j] = nd.y; Q.rd[2][j] = nd.z;
+                Q.rc[j] = nc;
+                Q.rpix[j] = npix;
+                Q.rbounce[j] = nbounce;
+                ++n_sec;
+            } else {
+                atomicOr(a.status, RT_DEV_OVERFLOW);
+            }
+        }
+        if (push_t) {
+            const int j = pbase + __popc(pr) + __popc(pt & lt);
+            if (j < RPOOL) {
+                Q.ro[0][j] = np.x; Q.ro[1][j] = np.y; Q.ro[2][j] = np.z;
+                Q.rd[0][j] = td.x; Q.rd[1][j] = td.y; Q.rd[2][j] = td.z;
+                Q.rc[j] = tc;
+                Q.rpix[j] = npix;
+                Q.rbounce[j] = nbounce;
+                ++n_sec;
+            } else {
+                atomicOr(a.status, RT_DEV_OVERFLOW);
+            }
+        }
+        __syncwarp();
+        if (lane == 0) Q.pool_n = min(RPOOL, pbase + __popc(pr) + __popc(pt));
+        __syncwarp();
+    }
+    if (a.stats) {
+        n_prim = __reduce_add_sync(0xffffffffu, (unsigned)n_prim);
+        n_sec = __reduce_add_sync(0xffffffffu, (unsigned)n_sec);
+        n_shadow = __reduce_add_sync(0xffffffffu, (unsigned)n_shadow);
+        n_hits = __reduce_add_sync(0xffffffffu, (unsigned)n_hits);
+        if (lane == 0) {
+            atomicAdd((unsigned long long*)&a.stats->primary_rays, (unsigned long long)n_prim);
+            atomicAdd((unsigned long long*)&a.stats->secondary_rays, (unsigned long long)n_sec);
+            atomicAdd((unsigned long long*)&a.stats->shadow_rays, (unsigned long long)n_shadow);
+            atomicAdd((unsigned long long*)&a.stats->hits, (unsigned long long)n_hits);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // stage-wise kernels on reference-layout buffers
 // ---------------------------------------------------------------------------
 __global__ void k_gen_primary(rt_camera cam, int w, int h, int q, const rt_pixel_sample* ps,
@@ -516,6 +714,7 @@ static const RenderVariant kVariants[] = {
     {128, 6, k_render_pool<128, 6>, true}, {128, 8, k_render_pool<128, 8>, true},
     {256, 3, k_render_pool<256, 3>, true}, {256, 4, k_render_pool<256, 4>, true},
     {128, 6, k_render<128, 6, true>, false, true},
+    {128, 4, k_render_pool_refr<128, 4>, true, true},
 };
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
@@ -533,10 +732,16 @@ bool render_variant_pooled(int v) { return v >= 0 && v < kNumVariants && kVarian
 
 bool render_variant_refracts(int v) { return v >= 0 && v < kNumVariants && kVariants[v].refract; }
 
-int render_refract_variant() {
+bool render_variant_fits(int v, int max_bounces) {
+    if (v < 0 || v >= kNumVariants) return false;
+    return !(kVariants[v].refract && kVariants[v].pooled) || max_bounces <= REFR_POOL_MAXB;
+}
+
+int render_refract_variant(int max_bounces) {
+    int tree = -1, pooled = -1;
     for (int v = 0; v < kNumVariants; ++v)
-        if (kVariants[v].refract) return v;
-    return -1;
+        if (kVariants[v].refract) (kVariants[v].pooled ? pooled : tree) = v;
+    return pooled >= 0 && max_bounces <= REFR_POOL_MAXB ? pooled : tree;
 }
 
 cudaError_t launch_render(const RenderArgs& a, int variant, int grid, cudaStream_t s) {

@@ -28,10 +28,17 @@ int render_variant_count();
 int render_variant_info(int v, int* threads, int* min_blocks, const void** fn);
 // True for variants that accumulate into RenderArgs::accum (k_render_pool).
 bool render_variant_pooled(int v);
-// True for the variant that walks refraction trees; the scenes with
-// refracting materials render with it.
+// True for the variants that follow refracted rays; the scenes with
+// refracting materials render with one of them.
 bool render_variant_refracts(int v);
-int render_refract_variant();
+// The pooled refraction variant holds 32 (max_bounces + 2) rays per warp,
+// sized for up to REFR_POOL_MAXB bounces.
+constexpr int REFR_POOL_MAXB = 6;
+// Whether variant v renders frames of max_bounces bounces.
+bool render_variant_fits(int v, int max_bounces);
+// The refraction variant for frames of max_bounces bounces: the pooled one
+// where it fits, else the ray-tree walk.
+int render_refract_variant(int max_bounces);
 cudaError_t launch_render(const RenderArgs& a, int variant, int grid, cudaStream_t s);
 cudaError_t launch_gen_primary(const rt_camera& cam, int w, int h, int q, const rt_pixel_sample* ps,
                                size_t count, size_t offset, rt_sample* out, cudaStream_t s);

@@ -288,27 +288,34 @@ def test_refraction_secondary_rays_match_oracle(ctx, orc, fill):
     assert out_d.read(abi.SAMPLE_DTYPE, k).tobytes() == ref_sec.tobytes()
 
 
-@pytest.mark.parametrize("bounces", [1, 4])
+@pytest.mark.parametrize("bounces", [1, 4, 6, 8])
 def test_render_refraction_bit_exact(ctx, orc, bounces):
     """rt_render of a soup with glass: each hit on glass spawns a refracted
-    and a reflected ray, walked as a tree per pixel; the fixed-point image and
-    the ray counts equal the oracle's wavefront render (a tile large enough
-    that no wavefront is cut)."""
+    and a reflected ray, followed by the pooled refraction variant (up to 6
+    bounces) or walked as a tree per pixel; with every configured variant
+    (those that cannot follow refraction, or hold too few rays, give way to
+    one that can) the fixed-point image and the ray counts equal the
+    oracle's wavefront render (a tile large enough that no wavefront is
+    cut)."""
     sc = scenes.with_glass(scenes.soup(8000, seed=5), frac=0.4, seed=1)
     g, o = _pair(ctx, orc, sc)
     cam = scenes.camera((0.0, 0.0, -4.0), (0.0, 0.0, 0.0), aspect=1.0)
     w = h = 256
     n = w * h
-    rgba_d, img_d, st_d = ctx.alloc(4 * n), ctx.alloc(12 * n), ctx.alloc(32)
-    st_d.zero()
-    g.render(cam, w, h, bounces, rgba_d, img_d, st_d)
-    ctx.sync()
-    img = img_d.read(np.uint32).reshape(-1, 3)
-    st = st_d.read(np.uint64)
     rimg, rst = o.render(cam, w, h, bounces, tile=1 << 20)
-    assert np.array_equal(img, rimg)
-    assert st[1] == rst.secondary_rays and st[2] == rst.shadow_rays and st[3] == rst.hits
     assert rst.secondary_rays > 5000
+    rgba_d, img_d, st_d = ctx.alloc(4 * n), ctx.alloc(12 * n), ctx.alloc(32)
+    cfg0 = ctx.render_config()
+    for v in range(len(ctx.variants())):
+        ctx.set_render_config(v, 0, 64)
+        st_d.zero()
+        g.render(cam, w, h, bounces, rgba_d, img_d, st_d)
+        ctx.sync()
+        img = img_d.read(np.uint32).reshape(-1, 3)
+        st = st_d.read(np.uint64)
+        assert np.array_equal(img, rimg), v
+        assert st[1] == rst.secondary_rays and st[2] == rst.shadow_rays and st[3] == rst.hits, v
+    ctx.set_render_config(cfg0.variant, cfg0.blocks_per_sm, cfg0.chunk)
     assert ctx.device_status() == 0
 
 
