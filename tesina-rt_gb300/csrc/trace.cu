@@ -255,13 +255,12 @@ __global__ void __launch_bounds__(THREADS, MINB) k_render_pool(RenderArgs a) {
 // * (1 - R), and the reflected one, * R, as generate_secondary_rays_disc
 // makes them), and both go into the warp's pool.  The pool is taken from the
 // top (last in, first out), so it holds at most 32 (max_bounces + 2) rays;
-// it is sized for max_bounces <= REFR_POOL_MAXB (deeper frames use the
-// ray-tree variant) and a push beyond it raises RT_DEV_OVERFLOW instead of
-// writing.  Sums are integers, so the image is the ray-tree variant's.
+// it is sized for max_bounces <= MAXB (deeper frames use a larger pool or
+// the ray-tree variant) and a push beyond it raises RT_DEV_OVERFLOW instead
+// of writing.  Sums are integers, so the image is the ray-tree variant's.
 // ---------------------------------------------------------------------------
 namespace {
-constexpr int RPOOL = 32 * (REFR_POOL_MAXB + 2);
-
+template <int RPOOL>
 struct RefrPool {
     float ro[3][RPOOL], rd[3][RPOOL], rc[RPOOL];
     int rpix[RPOOL], rbounce[RPOOL];
@@ -273,17 +272,18 @@ struct RefrPool {
 };
 }  // namespace
 
-template <int THREADS, int MINB>
+template <int THREADS, int MINB, int MAXB>
 __global__ void __launch_bounds__(THREADS, MINB) k_render_pool_refr(RenderArgs a) {
+    constexpr int RPOOL = 32 * (MAXB + 2);
     const SceneView S = a.scene;
     __shared__ BvhHeader sH;
     __shared__ rt_lights sL;
-    __shared__ RefrPool sQ[THREADS / 32];
+    __shared__ RefrPool<RPOOL> sQ[THREADS / 32];
     if (threadIdx.x == 0) sH = *S.hdr;
     for (int i = threadIdx.x; i < (int)(sizeof(rt_lights) / 4); i += blockDim.x)
         reinterpret_cast<uint32_t*>(&sL)[i] = reinterpret_cast<const uint32_t*>(&a.lights)[i];
     const int lane = threadIdx.x & 31;
-    RefrPool& Q = sQ[threadIdx.x >> 5];
+    RefrPool<RPOOL>& Q = sQ[threadIdx.x >> 5];
     if (lane == 0) Q.pool_n = 0;
     __syncthreads();
     const BvhHeader& H = sH;
@@ -704,7 +704,8 @@ struct RenderVariant {
     int threads, min_blocks;
     void (*fn)(RenderArgs);
     bool pooled;
-    bool refract;   // walks the ray tree of refracting materials
+    bool refract;     // follows the refracted rays of refracting materials
+    int max_bounces;  // deepest frame it holds (0: any)
 };
 static const RenderVariant kVariants[] = {
     {64, 8, k_render<64, 8>, false},    {64, 12, k_render<64, 12>, false},
@@ -714,7 +715,8 @@ static const RenderVariant kVariants[] = {
     {128, 6, k_render_pool<128, 6>, true}, {128, 8, k_render_pool<128, 8>, true},
     {256, 3, k_render_pool<256, 3>, true}, {256, 4, k_render_pool<256, 4>, true},
     {128, 6, k_render<128, 6, true>, false, true},
-    {128, 4, k_render_pool_refr<128, 4>, true, true},
+    {128, 4, k_render_pool_refr<128, 4, 6>, true, true, 6},
+    {128, 5, k_render_pool_refr<128, 5, 4>, true, true, 4},
 };
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
@@ -734,14 +736,20 @@ bool render_variant_refracts(int v) { return v >= 0 && v < kNumVariants && kVari
 
 bool render_variant_fits(int v, int max_bounces) {
     if (v < 0 || v >= kNumVariants) return false;
-    return !(kVariants[v].refract && kVariants[v].pooled) || max_bounces <= REFR_POOL_MAXB;
+    return kVariants[v].max_bounces == 0 || max_bounces <= kVariants[v].max_bounces;
 }
 
 int render_refract_variant(int max_bounces) {
-    int tree = -1, pooled = -1;
-    for (int v = 0; v < kNumVariants; ++v)
-        if (kVariants[v].refract) (kVariants[v].pooled ? pooled : tree) = v;
-    return pooled >= 0 && max_bounces <= REFR_POOL_MAXB ? pooled : tree;
+    // the pooled variant with the smallest pool that holds the frame, else
+    // the ray-tree walk
+    int best = -1;
+    for (int v = 0; v < kNumVariants; ++v) {
+        if (!kVariants[v].refract || !render_variant_fits(v, max_bounces)) continue;
+        if (best < 0 || (kVariants[v].pooled && (!kVariants[best].pooled ||
+                                                 kVariants[v].max_bounces < kVariants[best].max_bounces)))
+            best = v;
+    }
+    return best;
 }
 
 cudaError_t launch_render(const RenderArgs& a, int variant, int grid, cudaStream_t s) {

@@ -31,10 +31,8 @@ bool render_variant_pooled(int v);
 // True for the variants that follow refracted rays; the scenes with
 // refracting materials render with one of them.
 bool render_variant_refracts(int v);
-// The pooled refraction variant holds 32 (max_bounces + 2) rays per warp,
-// sized for up to REFR_POOL_MAXB bounces.
-constexpr int REFR_POOL_MAXB = 6;
-// Whether variant v renders frames of max_bounces bounces.
+// Whether variant v renders frames of max_bounces bounces (the pooled
+// refraction variants hold 32 (b + 2) rays per warp for up to b bounces).
 bool render_variant_fits(int v, int max_bounces);
 // The refraction variant for frames of max_bounces bounces: the pooled one
 // where it fits, else the ray-tree walk.
