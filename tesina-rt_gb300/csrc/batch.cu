@@ -282,7 +282,9 @@ __global__ void k_batch_stamp(unsigned long long* t) { *t = globaltimer(); }
 // ---------------------------------------------------------------------------
 // many-image render
 // ---------------------------------------------------------------------------
-template <int THREADS, int MINB>
+// REFR: each pixel's ray tree, refracted rays included (scenes with
+// refracting materials).
+template <int THREADS, int MINB, bool REFR = false>
 __global__ void __launch_bounds__(THREADS, MINB) k_render_batch(BatchRenderArgs A) {
     __shared__ uint32_t s_poff[kMaxBatchViews + 1];
     for (int i = threadIdx.x; i <= A.count; i += blockDim.x) s_poff[i] = A.pix_off[i];
@@ -307,7 +309,7 @@ __global__ void __launch_bounds__(THREADS, MINB) k_render_batch(BatchRenderArgs 
                 int x, y;
                 pixel_of(warp_tile_order(local, V.width, V.height), V.width, V.height, 32, x, y);
                 const BvhHeader H = *V.scene.hdr;
-                const PixelResult pr = render_pixel<RT_WW_SERVED>(
+                const PixelResult pr = render_pixel<RT_WW_SERVED, REFR>(
                     V.scene, H, *V.lights, V.cam, x, y, V.width, V.height, V.max_bounces, A.status);
                 ++n_prim;
                 n_sec += pr.secondary;
@@ -345,26 +347,31 @@ __global__ void __launch_bounds__(THREADS, MINB) k_render_batch(BatchRenderArgs 
 // integer sums being independent of order) and k_batch_fb writes RGBA8 at
 // each view's offset afterwards.  Bit-identical to k_render_batch.
 // ---------------------------------------------------------------------------
+// MAXB > 0: scenes with refracting materials, as k_render_pool_refr
+// (trace.cu) follows them: a hit continues its reflected and refracted rays,
+// the pool is taken from the top and holds 32 (MAXB + 2) rays, enough for
+// views of up to MAXB bounces; a push past it raises RT_DEV_OVERFLOW.
 namespace {
-constexpr int BPOOL = 64;
-
+template <int BPOOL>
 struct WarpPoolB {
     float ro[3][BPOOL], rd[3][BPOOL], rc[BPOOL];
     int rv[BPOOL], rai[BPOOL], rbounce[BPOOL];   // view, sum index, bounce
     float hp[3][32], hn[3][32], hd[3][32], hc[32];
     int hid[32], hv[32], hai[32], hbounce[32], hoff[33];
     unsigned hmask[32];
+    unsigned char hinv[32];
     int pool_n;
 };
 }  // namespace
 
-template <int THREADS, int MINB>
+template <int THREADS, int MINB, int MAXB = 0>
 __global__ void __launch_bounds__(THREADS, MINB) k_render_batch_pool(BatchRenderArgs A) {
+    constexpr int BPOOL = MAXB ? 32 * (MAXB + 2) : 64;
     __shared__ uint32_t s_poff[kMaxBatchViews + 1];
-    __shared__ WarpPoolB sQ[THREADS / 32];
+    __shared__ WarpPoolB<BPOOL> sQ[THREADS / 32];
     for (int i = threadIdx.x; i <= A.count; i += blockDim.x) s_poff[i] = A.pix_off[i];
     const int lane = threadIdx.x & 31;
-    WarpPoolB& Q = sQ[threadIdx.x >> 5];
+    WarpPoolB<BPOOL>& Q = sQ[threadIdx.x >> 5];
     if (lane == 0) Q.pool_n = 0;
     __syncthreads();
     const uint32_t total = s_poff[A.count];
@@ -441,6 +448,7 @@ __global__ void __launch_bounds__(THREADS, MINB) k_render_batch_pool(BatchRender
             Q.hv[k] = v;
             Q.hai[k] = ai;
             Q.hbounce[k] = bounce;
+            Q.hinv[k] = hi.inverse_n;
             Q.hmask[k] = 0u;
             nl = A.views[v].lights->count;
         }
@@ -472,9 +480,9 @@ __global__ void __launch_bounds__(THREADS, MINB) k_render_batch_pool(BatchRender
                 atomicOr(&Q.hmask[lo], 1u << l);
         }
         __syncwarp();
-        bool push = false;
-        f3 np = mk3(0.f, 0.f, 0.f), nd = np;
-        float nc = 0.f;
+        bool push = false, push_t = false;
+        f3 np = mk3(0.f, 0.f, 0.f), nd = np, td = np;
+        float nc = 0.f, tc = 0.f;
         int nv = 0, nai = 0, nbounce = 0;
         if (lane < nh) {
             const int k = lane;
@@ -492,30 +500,57 @@ __global__ void __launch_bounds__(THREADS, MINB) k_render_batch_pool(BatchRender
             ++n_hits;
             n_shadow += (uint32_t)V.lights->count;
             const int bk = Q.hbounce[k];
-            if (bk != V.max_bounces && mat.reflectiveness > 0.0f) {
-                reflect_ray(dk, n, nd);
+            if (bk < V.max_bounces) {
+                float R = 1.0f;
+                if (MAXB > 0 && mat.refractive_index > 0.0f &&
+                    refract_ray(dk, n, Q.hinv[k] != 0, mat.refractive_index, R, td)) {
+                    tc = ck * mat.reflectiveness * (1.0f - R);
+                    push_t = true;
+                }
+                if (mat.reflectiveness > 0.0f) {
+                    reflect_ray(dk, n, nd);
+                    nc = ck * mat.reflectiveness * R;
+                    push = true;
+                }
                 np = p;
-                nc = ck * mat.reflectiveness * 1.0f;
                 nv = Q.hv[k];
                 nai = ak;
                 nbounce = bk + 1;
-                push = true;
-                ++n_sec;
             }
         }
         const unsigned pm = __ballot_sync(0xffffffffu, push);
+        const unsigned pt = MAXB > 0 ? __ballot_sync(0xffffffffu, push_t) : 0u;
         const int pbase = Q.pool_n;
         if (push) {
             const int j = pbase + __popc(pm & lt);
-            Q.ro[0][j] = np.x; Q.ro[1][j] = np.y; Q.ro[2][j] = np.z;
-            Q.rd[0][j] = nd.x; Q.rd[1][j] = nd.y; Q.rd[2][j] = nd.z;
-            Q.rc[j] = nc;
-            Q.rv[j] = nv;
-            Q.rai[j] = nai;
-            Q.rbounce[j] = nbounce;
+            if (MAXB == 0 || j < BPOOL) {
+                Q.ro[0][j] = np.x; Q.ro[1][j] = np.y; Q.ro[2][j] = np.z;
+                Q.rd[0][j] = nd.x; Q.rd[1][j] = nd.y; Q.rd[2][j] = nd.z;
+                Q.rc[j] = nc;
+                Q.rv[j] = nv;
+                Q.rai[j] = nai;
+                Q.rbounce[j] = nbounce;
+                ++n_sec;
+            } else {
+                atomicOr(A.status, RT_DEV_OVERFLOW);
+            }
+        }
+        if (MAXB > 0 && push_t) {
+            const int j = pbase + __popc(pm) + __popc(pt & lt);
+            if (j < BPOOL) {
+                Q.ro[0][j] = np.x; Q.ro[1][j] = np.y; Q.ro[2][j] = np.z;
+                Q.rd[0][j] = td.x; Q.rd[1][j] = td.y; Q.rd[2][j] = td.z;
+                Q.rc[j] = tc;
+                Q.rv[j] = nv;
+                Q.rai[j] = nai;
+                Q.rbounce[j] = nbounce;
+                ++n_sec;
+            } else {
+                atomicOr(A.status, RT_DEV_OVERFLOW);
+            }
         }
         __syncwarp();
-        if (lane == 0) Q.pool_n = pbase + __popc(pm);
+        if (lane == 0) Q.pool_n = min(BPOOL, pbase + __popc(pm) + __popc(pt));
         __syncwarp();
     }
     if (A.stats) {
@@ -550,6 +585,8 @@ struct BatchRenderVariant {
     int threads, min_blocks;
     void (*fn)(BatchRenderArgs);
     bool pooled;
+    bool refract;      // follows refracted rays
+    int max_bounces;   // deepest view it holds (0: any)
 };
 // Variant 0 serves the request loop (many short launches, where the unpooled
 // kernel measured faster); rt_batch takes the first pooled one (one large
@@ -560,6 +597,9 @@ static const BatchRenderVariant kBatchVariants[] = {
     {256, 4, k_render_batch<256, 4>, false},
     {128, 6, k_render_batch<128, 6>, false},
     {128, 8, k_render_batch_pool<128, 8>, true},
+    {128, 6, k_render_batch<128, 6, true>, false, true},
+    {128, 5, k_render_batch_pool<128, 5, 4>, true, true, 4},
+    {128, 4, k_render_batch_pool<128, 4, 6>, true, true, 6},
 };
 
 int batch_render_variant_count() { return (int)(sizeof(kBatchVariants) / sizeof(kBatchVariants[0])); }
@@ -573,6 +613,23 @@ int batch_render_variant_info(int v, int* threads, const void** fn) {
 
 bool batch_render_variant_pooled(int v) {
     return v >= 0 && v < batch_render_variant_count() && kBatchVariants[v].pooled;
+}
+
+bool batch_render_variant_refracts(int v) {
+    return v >= 0 && v < batch_render_variant_count() && kBatchVariants[v].refract;
+}
+
+int batch_refract_variant(bool pooled, int max_bounces) {
+    int best = -1;
+    for (int v = 0; v < batch_render_variant_count(); ++v) {
+        const BatchRenderVariant& k = kBatchVariants[v];
+        if (!k.refract || k.pooled != pooled) continue;
+        if (k.max_bounces != 0 && max_bounces > k.max_bounces) continue;
+        if (best < 0 || (k.max_bounces != 0 && (kBatchVariants[best].max_bounces == 0 ||
+                                                k.max_bounces < kBatchVariants[best].max_bounces)))
+            best = v;
+    }
+    return best;
 }
 
 cudaError_t launch_batch_render(const BatchRenderArgs& a, int variant, int grid, cudaStream_t s) {

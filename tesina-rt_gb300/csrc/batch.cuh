@@ -86,6 +86,12 @@ int batch_render_variant_count();
 int batch_render_variant_info(int v, int* threads, const void** fn);
 // True for variants that sum into BatchRenderArgs::accum before RGBA8.
 bool batch_render_variant_pooled(int v);
+// True for the variants that follow refracted rays (scenes with refracting
+// materials); batch_refract_variant gives the unpooled one (pooled = false)
+// or the pooled one with the smallest ray pool that holds views of
+// max_bounces bounces (-1: none does).
+bool batch_render_variant_refracts(int v);
+int batch_refract_variant(bool pooled, int max_bounces);
 cudaError_t launch_batch_render(const BatchRenderArgs& a, int variant, int grid, cudaStream_t s);
 
 }  // namespace rt

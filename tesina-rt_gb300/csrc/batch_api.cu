@@ -220,9 +220,6 @@ int32_t rt_batch_set(rt_ctx* c, rt_batch* b, const rt_batch_view* views, int32_t
         const rt_batch_view& bv = views[v];
         if (!bv.scene || bv.scene->N == 0)
             return fail(RT_ERR_INVALID, "rt_batch_set: view %d has no uploaded scene", v);
-        if (bv.scene->refracts)
-            return fail(RT_ERR_INVALID, "rt_batch_set: view %d's scene refracts (rt_render and "
-                        "the stage-wise calls render refraction)", v);
         if (bv.width <= 0 || bv.height <= 0 || bv.max_bounces < 0 || bv.max_bounces > 64)
             return fail(RT_ERR_INVALID, "rt_batch_set: view %d has a bad size or depth", v);
         if (bv.rgba_offset != pixels)
@@ -328,11 +325,24 @@ int32_t rt_batch_set(rt_ctx* c, rt_batch* b, const rt_batch_view* views, int32_t
     int threads = 0;
     const void* fn = nullptr;
     b->render_variant = 0;
-    for (int v = 0; v < rt::batch_render_variant_count(); ++v)
-        if (rt::batch_render_variant_pooled(v)) {
-            b->render_variant = v;
-            break;
-        }
+    bool refracts = false;
+    int deepest = 0;
+    for (int v = 0; v < count; ++v) {
+        refracts = refracts || views[v].scene->refracts;
+        deepest = std::max(deepest, (int)views[v].max_bounces);
+    }
+    if (refracts) {
+        // both rays of a glass hit: the pooled kernel whose pool holds the
+        // deepest view, else each pixel's ray tree
+        b->render_variant = rt::batch_refract_variant(true, deepest);
+        if (b->render_variant < 0) b->render_variant = rt::batch_refract_variant(false, deepest);
+    } else {
+        for (int v = 0; v < rt::batch_render_variant_count(); ++v)
+            if (rt::batch_render_variant_pooled(v) && !rt::batch_render_variant_refracts(v)) {
+                b->render_variant = v;
+                break;
+            }
+    }
     rt::batch_render_variant_info(b->render_variant, &threads, &fn);
     int rbps = 0;
     CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&rbps, fn, threads, 0));

@@ -271,9 +271,6 @@ int32_t create_scene(rt_server* S, const rt_scene_desc* d, cudaStream_t stream, 
     if (r) return r;
     rt::scene_use_pool(sc, S->pool, stream);
     r = rt_scene_upload(S->ctx, sc, d, stream);
-    if (!r && sc->refracts)
-        r = fail(RT_ERR_INVALID, "rt_server: a scene with refracting materials (rt_render and "
-                 "the stage-wise calls render refraction)");
     if (r) {
         rt_scene_destroy(S->ctx, sc);
         return r;
@@ -413,9 +410,11 @@ bool launch_renders(rt_server* S) {
         rt::BatchView* hv = S->h_views[slot];
         uint32_t* hp = S->h_pix_off[slot];
         hp[0] = 0;
+        bool refracts = false;
         for (size_t v = 0; v < take.size(); ++v) {
             Req& q = S->reqs[take[v]];
             ServedScene& sc = S->scenes[q.r.scene_id];
+            refracts = refracts || sc.scene->refracts;
             rt::BatchView& V = hv[v];
             V.scene = rt::scene_view(sc.scene);
             V.lights = sc.d_lights;
@@ -453,7 +452,8 @@ bool launch_renders(rt_server* S) {
         const int cap = building && S->render_bps > 2
                             ? (S->render_bps - 2) * S->ctx->num_sms : S->render_grid;
         const int grid = (int)std::min<uint64_t>(cap, std::max<uint64_t>(1, need));
-        rt::launch_batch_render(a, 0, grid, cs);
+        // a launch with a refracting scene walks each pixel's ray tree
+        rt::launch_batch_render(a, refracts ? rt::batch_refract_variant(false, 0) : 0, grid, cs);
     }
     for (uint64_t tk : take) {
         Req& q = S->reqs[tk];

@@ -103,3 +103,31 @@ def test_batch_rejects_bad_views(ctx):
     arr[1].rgba_offset = 7                          # not packed
     r = ctx.lib.rt_batch_set(ctx.h, batch.h, arr, 2, None)
     assert r == -2 and b"packed" in ctx.lib.rt_last_error()
+
+
+@pytest.mark.parametrize("deepest", [4, 6, 8])
+def test_batch_refraction_matches_plain(ctx, deepest):
+    """Glass scenes in one batch: the pooled kernel whose ray pool holds the
+    deepest view (4 or 6 bounces), or each pixel's ray tree beyond that; every
+    image equals rt_render's (itself equal to the oracle's)."""
+    scs = [scenes.with_glass(scenes.soup(6000, seed=70), frac=0.4, seed=1),
+           scenes.soup(3000, seed=71),
+           scenes.with_glass(tiny_terrain(48, 24, 4).scene(0), frac=0.5, seed=2)]
+    gscenes = [capi.Scene(ctx, sc) for sc in scs]
+    items = []
+    for k, (g, b) in enumerate(zip(gscenes * 2, [deepest, 2, 3, 1, deepest - 1, 0])):
+        w, h = [(96, 64), (64, 64), (80, 50)][k % 3]
+        cam = scenes.camera((0.3 * k, 0.5, -4.0), (0.0, 0.0, 0.0), aspect=w / h)
+        items.append((g, cam, w, h, b))
+    batch = capi.Batch(ctx)
+    batch.set(items)
+    batch.build()
+    rgba = ctx.alloc(4 * batch.pixels)
+    batch.render(rgba)
+    ctx.sync()
+    out = rgba.read(np.uint8)
+    assert ctx.device_status() == 0
+    for (g, cam, w, h, b), (off, _, _) in zip(items, batch.offsets):
+        sc = scs[gscenes.index(g)]
+        _, ref = _plain(ctx, sc, cam, w, h, b)
+        assert np.array_equal(out[4 * off:4 * (off + w * h)], ref)

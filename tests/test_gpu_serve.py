@@ -157,3 +157,26 @@ def test_stream_images_equal_plain_and_served(ctx):
     assert a["uploads"] >= 3 and a["evicted"] == b["evicted"] == a["uploads"]
     assert a["crc"] == b["crc"] and len(a["crc"]) == a["renders"]
     assert b["mean_batch_views"] > 1 and a["mean_batch_views"] == 1
+
+
+def test_served_refraction_equals_plain(ctx):
+    """Scenes with glass are served like any other (launches that hold one
+    walk each pixel's ray tree): every image equals rt_render's."""
+    pool = [scenes.with_glass(scenes.soup(8000, seed=51), frac=0.4, seed=3),
+            scenes.soup(6000, seed=52)]
+    srv = capi.Server(ctx, budget=4 << 30, arena=256 << 20, max_views=64, max_inflight=2)
+    ids = [srv.add_scene(sc) for sc in pool]
+    rng = np.random.default_rng(5)
+    reqs = []
+    for k in range(16):
+        w, h = int(rng.integers(24, 120)), int(rng.integers(24, 120))
+        i = k % 2
+        cam = scenes.camera(tuple(rng.normal(size=3) + [0, 0, -4]), (0, 0, 0), aspect=w / h)
+        b = int(rng.integers(0, 6))
+        reqs.append((i, cam, w, h, b, srv.submit_render(ids[i], cam, w, h, b)))
+    for i, cam, w, h, b, t in reqs:
+        img, inf = srv.result(t, w, h)
+        assert inf.status == 0
+        assert np.array_equal(img, _plain(ctx, pool[i], cam, w, h, b))
+    srv.close()
+    assert ctx.device_status() == 0

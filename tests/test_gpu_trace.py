@@ -317,14 +317,3 @@ def test_render_refraction_bit_exact(ctx, orc, bounces):
         assert st[1] == rst.secondary_rays and st[2] == rst.shadow_rays and st[3] == rst.hits, v
     ctx.set_render_config(cfg0.variant, cfg0.blocks_per_sm, cfg0.chunk)
     assert ctx.device_status() == 0
-
-
-def test_refraction_outside_plain_path_rejected(ctx):
-    """The batched and served forms take no refracting scenes (yet)."""
-    sc = scenes.with_glass(scenes.soup(500, seed=1), frac=0.5)
-    g = capi.Scene(ctx, sc)
-    g.build(30, 1)
-    b = capi.Batch(ctx)
-    with pytest.raises(capi.RtError) as e:
-        b.set([(g, scenes.camera((0.0, 0.0, -4.0), (0.0, 0.0, 0.0)), 32, 32, 1)])
-    assert e.value.code == -2
