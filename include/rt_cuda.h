@@ -256,8 +256,8 @@ RT_API int32_t rt_obj_free(rt_obj* obj);
  * shadow_trace_multi, src/kernel/shadow-trace-bvh.cl:317-373).  Instance i
  * draws built scene inst_scene[i] under the row-major 4x4 transform tr[16 i]
  * whose inverse is tr_inv[16 i] (both given, as BVHRoot holds both).  Each
- * scene keeps its materials; lights are the instance set's.  Scenes with
- * refracting materials are not taken.  The set refers to its scenes: destroy
+ * scene keeps its materials; lights are the instance set's.  With refracting
+ * materials a frame renders up to 6 bounces.  The set refers to its scenes: destroy
  * it before them; a scene rebuilt (on any stream) is seen by the next render. */
 typedef struct rt_instances rt_instances;
 RT_API int32_t rt_instances_create(rt_ctx* ctx, rt_scene* const* scenes, int32_t scene_count,

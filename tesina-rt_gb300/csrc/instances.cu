@@ -227,7 +227,7 @@ __device__ __forceinline__ bool occluded_multi(const InstanceArgs& A, const rt_l
 // the instance's mesh moved by its transform (not renormalised), turned
 // against the ray.
 __device__ __forceinline__ void multi_surface(const InstanceArgs& A, const MultiHit& mh, f3 o, f3 d,
-                                              f3& hp, f3& n) {
+                                              f3& hp, f3& n, bool& inverse_n) {
     const SceneView& S = A.roots[mh.root].scene;
     hp = add(o, muls(d, mh.h.t));
     const uint32_t* ix = S.idx + 3 * (size_t)mh.h.id;
@@ -237,7 +237,8 @@ __device__ __forceinline__ void multi_surface(const InstanceArgs& A, const Multi
     const float w = 1.0f - (mh.h.u + mh.h.v);
     n = normalize(add(add(muls(n0, w), muls(n2, mh.h.v)), muls(n1, mh.h.u)));
     n = mat_apply(A.roots[mh.root].tr, n, 0.0f);
-    if (dot(n, d) > 0.0f) n = muls(n, -1.0f);
+    inverse_n = dot(n, d) > 0.0f;
+    if (inverse_n) n = muls(n, -1.0f);
 }
 
 // k_render_instances: the rays of the reference's multi-root render
@@ -248,15 +249,19 @@ __device__ __forceinline__ void multi_surface(const InstanceArgs& A, const Multi
 // a pool in shared memory, 32 at a time whichever pixels they belong to.
 // Contributions are fixed-point sums per pixel (independent of order), so
 // the image is the one the per-pixel loop gives.
+// MAXB > 0: meshes with refracting materials: a hit continues its reflected
+// and refracted rays (as k_render_pool_refr does), the pool is taken from the
+// top and holds 32 (MAXB + 2) rays, enough for frames of up to MAXB bounces;
+// a push past it raises RT_DEV_OVERFLOW instead of writing.
 namespace {
-constexpr int IPOOL = 64;   // reflection rays a warp can hold: < 32 left + 32 new
-
+template <int IPOOL>
 struct InstPool {
     float ro[3][IPOOL], rd[3][IPOOL], rc[IPOOL];
     int rpix[IPOOL], rbounce[IPOOL];
     float hp[3][32], hn[3][32], hd[3][32], hc[32];
     int hid[32], hroot[32], hpix[32], hbounce[32];
     unsigned hmask[32];
+    unsigned char hinv[32];
     int pool_n;
 };
 }  // namespace
@@ -264,12 +269,14 @@ struct InstPool {
 #ifndef RT_INST_MINB
 #define RT_INST_MINB 6
 #endif
-__global__ void __launch_bounds__(128, RT_INST_MINB) k_render_instances(InstanceArgs A) {
+template <int MAXB>
+__global__ void __launch_bounds__(128, MAXB == 6 ? 5 : RT_INST_MINB) k_render_instances(InstanceArgs A) {
+    constexpr int IPOOL = MAXB ? 32 * (MAXB + 2) : 64;   // reflections only: < 32 left + 32 new
     __shared__ InstanceArgs sA;
-    __shared__ InstPool sQ[4];
+    __shared__ InstPool<IPOOL> sQ[4];
     if (threadIdx.x == 0) sA = A;
     const int lane = threadIdx.x & 31;
-    InstPool& Q = sQ[threadIdx.x >> 5];
+    InstPool<IPOOL>& Q = sQ[threadIdx.x >> 5];
     if (lane == 0) Q.pool_n = 0;
     __syncthreads();
     const int pixels = sA.width * sA.height;
@@ -326,7 +333,9 @@ __global__ void __launch_bounds__(128, RT_INST_MINB) k_render_instances(Instance
         if (hit_ok) {
             const int k = __popc(hm & lt);
             f3 hp, n;
-            multi_surface(sA, mh, o, d, hp, n);
+            bool inv;
+            multi_surface(sA, mh, o, d, hp, n, inv);
+            Q.hinv[k] = inv;
             Q.hp[0][k] = hp.x; Q.hp[1][k] = hp.y; Q.hp[2][k] = hp.z;
             Q.hn[0][k] = n.x; Q.hn[1][k] = n.y; Q.hn[2][k] = n.z;
             Q.hd[0][k] = d.x; Q.hd[1][k] = d.y; Q.hd[2][k] = d.z;
@@ -345,9 +354,9 @@ __global__ void __launch_bounds__(128, RT_INST_MINB) k_render_instances(Instance
             if (occluded_multi(sA, sA.lights.light[l], p)) atomicOr(&Q.hmask[k], 1u << l);
         }
         __syncwarp();
-        bool push = false;
-        f3 np = mk3(0.f, 0.f, 0.f), nd = np;
-        float nc = 0.f;
+        bool push = false, push_t = false;
+        f3 np = mk3(0.f, 0.f, 0.f), nd = np, td = np;
+        float nc = 0.f, tc = 0.f;
         int npix = 0, nbounce = 0;
         if (lane < nh) {
             const int k = lane;
@@ -365,28 +374,54 @@ __global__ void __launch_bounds__(128, RT_INST_MINB) k_render_instances(Instance
             ++n_hits;
             n_shadow += (uint32_t)nl;
             const int bk = Q.hbounce[k];
-            if (bk != sA.max_bounces && mat.reflectiveness > 0.0f) {
-                reflect_ray(dk, n, nd);
+            if (bk < sA.max_bounces) {
+                float R = 1.0f;
+                if (MAXB > 0 && mat.refractive_index > 0.0f &&
+                    refract_ray(dk, n, Q.hinv[k] != 0, mat.refractive_index, R, td)) {
+                    tc = ck * mat.reflectiveness * (1.0f - R);
+                    push_t = true;
+                }
+                if (mat.reflectiveness > 0.0f) {
+                    reflect_ray(dk, n, nd);
+                    nc = ck * mat.reflectiveness * R;
+                    push = true;
+                }
                 np = p;
-                nc = ck * mat.reflectiveness * 1.0f;
                 npix = pk;
                 nbounce = bk + 1;
-                push = true;
-                ++n_sec;
             }
         }
         const unsigned pm = __ballot_sync(0xffffffffu, push);
+        const unsigned pt = MAXB > 0 ? __ballot_sync(0xffffffffu, push_t) : 0u;
         const int pbase = Q.pool_n;
         if (push) {
             const int j = pbase + __popc(pm & lt);
-            Q.ro[0][j] = np.x; Q.ro[1][j] = np.y; Q.ro[2][j] = np.z;
-            Q.rd[0][j] = nd.x; Q.rd[1][j] = nd.y; Q.rd[2][j] = nd.z;
-            Q.rc[j] = nc;
-            Q.rpix[j] = npix;
-            Q.rbounce[j] = nbounce;
+            if (MAXB == 0 || j < IPOOL) {
+                Q.ro[0][j] = np.x; Q.ro[1][j] = np.y; Q.ro[2][j] = np.z;
+                Q.rd[0][j] = nd.x; Q.rd[1][j] = nd.y; Q.rd[2][j] = nd.z;
+                Q.rc[j] = nc;
+                Q.rpix[j] = npix;
+                Q.rbounce[j] = nbounce;
+                ++n_sec;
+            } else {
+                atomicOr(sA.status, RT_DEV_OVERFLOW);
+            }
+        }
+        if (MAXB > 0 && push_t) {
+            const int j = pbase + __popc(pm) + __popc(pt & lt);
+            if (j < IPOOL) {
+                Q.ro[0][j] = np.x; Q.ro[1][j] = np.y; Q.ro[2][j] = np.z;
+                Q.rd[0][j] = td.x; Q.rd[1][j] = td.y; Q.rd[2][j] = td.z;
+                Q.rc[j] = tc;
+                Q.rpix[j] = npix;
+                Q.rbounce[j] = nbounce;
+                ++n_sec;
+            } else {
+                atomicOr(sA.status, RT_DEV_OVERFLOW);
+            }
         }
         __syncwarp();
-        if (lane == 0) Q.pool_n = pbase + __popc(pm);
+        if (lane == 0) Q.pool_n = min(IPOOL, pbase + __popc(pm) + __popc(pt));
         __syncwarp();
     }
     if (sA.stats) {
@@ -467,9 +502,6 @@ int32_t rt_instances_create(rt_ctx* c, rt_scene* const* scenes, int32_t scene_co
     for (int k = 0; k < scene_count; ++k) {
         if (!scenes[k] || !scenes[k]->built)
             return fail(RT_ERR_NOT_BUILT, "rt_instances_create: scene %d has no BVH", k);
-        if (scenes[k]->refracts)
-            return fail(RT_ERR_INVALID, "rt_instances_create: scene %d refracts (rt_render "
-                        "renders refraction)", k);
     }
     for (int i = 0; i < count; ++i)
         if (inst_scene[i] < 0 || inst_scene[i] >= scene_count)
@@ -514,9 +546,21 @@ int32_t rt_instances_render(rt_ctx* c, rt_instances* I, const rt_camera* cam, in
     if (!c || !I || !cam || !rgba) return fail(RT_ERR_INVALID, "rt_instances_render: null argument");
     if (w <= 0 || h <= 0 || (int64_t)w * h > (1ll << 30) || max_bounces < 0 || max_bounces > 64)
         return fail(RT_ERR_INVALID, "rt_instances_render: bad size or depth");
-    for (rt_scene* s : I->scenes)
-        if (!s->built || s->refracts)
-            return fail(RT_ERR_INVALID, "rt_instances_render: a scene is not built or refracts");
+    bool refracts = false;
+    for (rt_scene* s : I->scenes) {
+        if (!s->built) return fail(RT_ERR_NOT_BUILT, "rt_instances_render: a scene has no BVH");
+        refracts = refracts || s->refracts;
+    }
+    // glass: both rays of a hit share the warp's pool, sized by the depth
+    int kind = 0;
+    void (*kern)(rt::InstanceArgs) = rt::k_render_instances<0>;
+    if (refracts) {
+        if (max_bounces > 6)
+            return fail(RT_ERR_INVALID, "rt_instances_render: instance sets with refracting "
+                        "materials render up to 6 bounces (%d asked)", max_bounces);
+        kind = max_bounces <= 4 ? 1 : 2;
+        kern = kind == 1 ? rt::k_render_instances<4> : rt::k_render_instances<6>;
+    }
     cudaStream_t cs = stream ? (cudaStream_t)stream : c->stream;
     if (!I->ev_render) CU(cudaEventCreateWithFlags(&I->ev_render, cudaEventDisableTiming));
     uint32_t* work = rt::work_counter(c, cs);
@@ -538,13 +582,13 @@ int32_t rt_instances_render(rt_ctx* c, rt_instances* I, const rt_camera* cam, in
     A.work_counter = work;
     A.status = c->d_status;
     A.inv1e6 = c->inv1e6;
-    static int occ = -1;
-    if (occ < 0) {
+    static int occ[3] = {-1, -1, -1};
+    if (occ[kind] < 0) {
         int b = 0;
-        CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, rt::k_render_instances, 128, 0));
-        occ = b > 0 ? b : 1;
+        CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, 128, 0));
+        occ[kind] = b > 0 ? b : 1;
     }
-    int64_t grid = (int64_t)c->num_sms * occ;
+    int64_t grid = (int64_t)c->num_sms * occ[kind];
     const int64_t useful = ((int64_t)px + 127) / 128;   // one 32-pixel tile per warp
     if (grid > useful) grid = useful;
     for (size_t k = 0; k < I->scenes.size(); ++k) {
@@ -562,7 +606,7 @@ int32_t rt_instances_render(rt_ctx* c, rt_instances* I, const rt_camera* cam, in
     rt::k_instance_boxes<<<(unsigned)((A.count + 127) / 128), 128, 0, cs>>>(I->d_roots, A.count,
                                                                             I->d_cull);
     CU(cudaMemsetAsync(A.accum, 0, 3 * sizeof(uint32_t) * px, cs));
-    rt::k_render_instances<<<(unsigned)grid, 128, 0, cs>>>(A);
+    kern<<<(unsigned)grid, 128, 0, cs>>>(A);
     CU(cudaGetLastError());
     CU(rt::launch_fb_copy(A.accum, rgba, px, c->inv1e6, cs));
     for (rt_scene* s : I->scenes) CU(rt::scene_read_end(s, cs));

@@ -62,7 +62,7 @@ def test_instances_render_bit_exact(ctx, orc, light):
     assert ctx.device_status() == 0
 
 
-def test_instances_reject_refraction_and_unbuilt(ctx):
+def test_instances_reject_unbuilt_and_deep_glass(ctx):
     sc = scenes.soup(500, seed=1)
     g = capi.Scene(ctx, sc)
     inst, T, Ti = [0], np.eye(4, dtype=np.float32)[None], np.eye(4, dtype=np.float32)[None]
@@ -70,8 +70,46 @@ def test_instances_reject_refraction_and_unbuilt(ctx):
         capi.Instances(ctx, [g], inst, T, Ti, sc.lights)          # not built
     glass = capi.Scene(ctx, scenes.with_glass(sc, 0.5))
     glass.build(30, 1)
-    with pytest.raises(capi.RtError):
-        capi.Instances(ctx, [glass], inst, T, Ti, sc.lights)
+    I = capi.Instances(ctx, [glass], inst, T, Ti, sc.lights)
+    rgba = ctx.alloc(4 * 32 * 32)
+    with pytest.raises(capi.RtError):                                 # glass: up to 6 bounces
+        I.render(scenes.camera((0, 0, -4), (0, 0, 0)), 32, 32, 7, rgba)
+    I.close()
+
+
+@pytest.mark.parametrize("bounces", [2, 4, 6])
+def test_instances_glass_bit_exact(ctx, orc, bounces):
+    """Instances of meshes with glass: reflected and refracted rays of the
+    moved, unnormalised normals, against the oracle's multi-root render
+    (pinned against the reference's kernels with glass)."""
+    meshes = [scenes.with_glass(scenes.soup(3000, seed=4), frac=0.5, seed=2),
+              scenes.with_glass(tiny_terrain(32, 16, 2).scene(0), frac=0.5, seed=3)]
+    gs, os_ = [], []
+    for sc in meshes:
+        g = capi.Scene(ctx, sc)
+        g.build(30, 1)
+        o = orc.new_scene(sc)
+        o.build(30, 1, 0)
+        gs.append(g)
+        os_.append(o)
+    inst, T, Ti = _instances()
+    lights = abi.make_lights((0.1, 0.1, 0.1), [dict(type=abi.RT_POINT_L, pos=(0.0, 4.0, -3.0),
+                                                    color=(1.0, 1.0, 1.0))])
+    I = capi.Instances(ctx, gs, inst, T, Ti, lights)
+    om = orc.multi([o.h for o in os_], inst, T, Ti, lights)
+    cam = scenes.camera((0.0, 1.5, -6.0), (0.0, 0.0, 0.5), aspect=1.0)
+    w = h = 160
+    rgba_d, img_d, st_d = ctx.alloc(4 * w * h), ctx.alloc(12 * w * h), ctx.alloc(32)
+    st_d.zero()
+    I.render(cam, w, h, bounces, rgba_d, img_d, st_d)
+    ctx.sync()
+    rimg, rst = orc.multi_render(om, cam, w, h, bounces, tile=1 << 20)
+    st = st_d.read(np.uint64)
+    assert np.array_equal(img_d.read(np.uint32).reshape(-1, 3), rimg)
+    assert st[1] == rst.secondary_rays > 3000 and st[3] == rst.hits
+    orc.multi_free(om)
+    I.close()
+    assert ctx.device_status() == 0
 
 
 def test_instances_many_roots_and_ties(ctx, orc):

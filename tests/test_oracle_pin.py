@@ -220,11 +220,16 @@ def _instances():
     return [0, 1, 1, 0], T, Ti
 
 
-def test_pin_multi_root(orc, ref):
+@pytest.mark.parametrize("glass", [False, True])
+def test_pin_multi_root(orc, ref, glass):
     """trace_multi / shadow_trace_multi (trace-bvh.cl:420-463,
     shadow-trace-bvh.cl:317-373) and the render over several roots: the
-    oracle against the reference's kernels on the same trees, bit for bit."""
+    oracle against the reference's kernels on the same trees, bit for bit;
+    with glass, the refracted rays of the moved, unnormalised normals too."""
     meshes = [scenes.soup(3000, seed=4), tiny_terrain(32, 16, 2).scene(0)]
+    if glass:
+        meshes = [scenes.with_glass(meshes[0], frac=0.5, seed=2),
+                  scenes.with_glass(meshes[1], frac=0.5, seed=3)]
     o_h, r_h = [], []
     for sc in meshes:
         s, rh = _pair(orc, ref, sc)
@@ -254,8 +259,8 @@ def test_pin_multi_root(orc, ref):
     orc.multi_shadow(om, smp, ho)
     ref.multi_shadow(rm, smp, hr)
     assert np.array_equal(ho["shadow_hit"][m], hr["shadow_hit"][m])
-    img_o, st_o = orc.multi_render(om, cam, w, h, 3)
-    img_r, st_r = ref.multi_render(rm, cam, w, h, 3)
+    img_o, st_o = orc.multi_render(om, cam, w, h, 3, tile=1 << 20)
+    img_r, st_r = ref.multi_render(rm, cam, w, h, 3, tile=1 << 20)
     assert np.array_equal(img_o, img_r) and st_o.secondary_rays == st_r.secondary_rays > 0
     orc.multi_free(om)
     ref.multi_free(rm)
