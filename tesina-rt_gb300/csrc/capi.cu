@@ -379,7 +379,8 @@ int32_t rt_init(rt_ctx** out, int32_t device) {
     CU(cudaMalloc(&c->d_status, sizeof(uint32_t)));
     CU(cudaMemset(c->d_status, 0, sizeof(uint32_t)));
     CU(cudaMalloc(&c->d_work, 64 * sizeof(uint32_t)));
-    for (int v = 0; v < rt::render_variant_count() && v < 16; ++v) {
+    for (int v = 0; v < rt::kMaxRenderVariants; ++v) c->variant_carveout[v] = -1;
+    for (int v = 0; v < rt::render_variant_count(); ++v) {
         int threads = 0, minb = 0, bps = 0;
         const void* fn = nullptr;
         rt::render_variant_info(v, &threads, &minb, &fn);

@@ -33,9 +33,8 @@ struct rt_ctx {
     rt_render_stats* d_stats = nullptr;  // rt_render_host counters
     float inv1e6 = 1.0f / 1e6f;
     rt_render_config render_cfg = {4, 0, 32, 32};   // variant (128 threads, 8 blocks/SM)
-    int variant_occupancy[16] = {0};                // resident blocks per SM per variant
-    int variant_carveout[16] = {-1, -1, -1, -1, -1, -1, -1, -1,
-                                -1, -1, -1, -1, -1, -1, -1, -1};   // shared-memory carveout set (%)
+    int variant_occupancy[rt::kMaxRenderVariants] = {0};   // resident blocks per SM per variant
+    int variant_carveout[rt::kMaxRenderVariants];          // shared-memory carveout set (%), -1 unset
     int smem_per_sm = 0;                            // bytes of shared memory an SM offers
     std::map<uint64_t, rt_render_config> tuned;     // autotuner cache by workload class
 };

@@ -38,6 +38,9 @@ struct TriRec {
 };
 
 // Views passed to kernels.
+// Render kernel variants a context keeps per-variant state for.
+constexpr int kMaxRenderVariants = 32;
+
 struct SceneView {
     const float4* __restrict__ nodes;
     const float4* __restrict__ tris;      // 3 float4 per triangle

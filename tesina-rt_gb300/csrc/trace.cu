@@ -719,6 +719,7 @@ static const RenderVariant kVariants[] = {
     {128, 5, k_render_pool_refr<128, 5, 4>, true, true, 4},
 };
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
+static_assert(kNumVariants <= kMaxRenderVariants, "per-variant context arrays");
 
 int render_variant_count() { return kNumVariants; }
 
