@@ -36,6 +36,9 @@ METRIC = "Whitted Mrays/s (primary+secondary), full LBVH rebuild per frame"
 UNIT = "Mrays/s"
 B_BUILD_PER_TRI = 312 + 16 * 4      # algorithmic LBVH bytes per triangle, 4 radix passes
 B_RAY_CLOSEST, B_RAY_SHADOW, B_SHADE = 40, 25, 48
+# DRAM bytes (read + write) of one k_render_pool<128, 6> launch on the
+# mid-scale frame, from the ncu capture summarised in profiles/.
+RENDER_POOL_DRAM_BYTES = (324.8 + 35.7) * 1e6
 
 
 def log(*a):
@@ -792,7 +795,12 @@ def run_gpu(args):
     roofline = {"kernel": ("k_render_pool (pooled trace + shadow + shade + reflect)" if pooled
                            else "k_render (fused trace + shadow + shade + reflect)"), "bound": "hbm",
                 "achieved": render_gbs, "peak": peak, "unit": "GB/s",
-                "frac": render_gbs / peak, "traffic": None,
+                "frac": render_gbs / peak,
+                # dram__bytes_read.sum + dram__bytes_write.sum of one launch of
+                # k_render_pool<128, 6> on this frame (ncu, 324.8 + 35.7 MB)
+                "traffic": RENDER_POOL_DRAM_BYTES if pooled else None,
+                "traffic_source": ("profiles/k_render_pool_terrain1M_1920x1080.md" if pooled
+                                   else None),
                 "peak_kind": peak_kind,
                 "algorithmic_bytes_per_launch": render_bytes,
                 "note": "traversal is latency/L2-bound; algorithmic bytes = 88 B per traced "
