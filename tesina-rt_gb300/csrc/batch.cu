@@ -22,6 +22,7 @@
 
 #include <algorithm>
 #include <vector>
+#include <mutex>
 
 #include "../../include/rt_cuda.h"
 #include "batch.cuh"
@@ -663,14 +664,25 @@ cudaError_t launch_batch_build(const BatchBuildArgs& a, int grid, cudaStream_t s
     cfg.numAttrs = 1;
     cudaError_t e = cudaLaunchKernelEx(&cfg, k_batch_build, a);
     if (e != cudaSuccess) return e;
-    static const cudaError_t attr0 = cudaFuncSetAttribute(
-        k_batch_emit<EMIT_C0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-        (int)sizeof(EmitSmem<EMIT_C0>));
-    static const cudaError_t attr1 = cudaFuncSetAttribute(
-        k_batch_emit<EMIT_C1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-        (int)sizeof(EmitSmem<EMIT_C1>));
-    if (attr0 != cudaSuccess) return attr0;
-    if (attr1 != cudaSuccess) return attr1;
+    {
+        // the shared-memory opt-in is a property of the kernel on each device
+        static std::mutex mu;
+        static uint64_t done = 0;   // devices 0..63 set up
+        int dev = 0;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (e != cudaSuccess) return e;
+        std::lock_guard<std::mutex> lk(mu);
+        if (dev >= 64 || !((done >> dev) & 1)) {
+            e = cudaFuncSetAttribute(k_batch_emit<EMIT_C0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)sizeof(EmitSmem<EMIT_C0>));
+            if (e == cudaSuccess)
+                e = cudaFuncSetAttribute(k_batch_emit<EMIT_C1>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)sizeof(EmitSmem<EMIT_C1>));
+            if (e != cudaSuccess) return e;
+            if (dev < 64) done |= 1ull << dev;
+        }
+    }
     for (int L = 0; L < a.emit_levels; ++L) {
         if (a.emit_jobs[L] == 0) continue;
         const uint32_t* off = a.emit_off + (size_t)L * (a.count + 1);

@@ -36,6 +36,7 @@ struct rt_ctx {
     int variant_occupancy[rt::kMaxRenderVariants] = {0};   // resident blocks per SM per variant
     int variant_carveout[rt::kMaxRenderVariants];          // shared-memory carveout set (%), -1 unset
     int smem_per_sm = 0;                            // bytes of shared memory an SM offers
+    int instance_occupancy[3] = {0, 0, 0};          // k_render_instances<0 / 4 / 6> blocks per SM
     std::map<uint64_t, rt_render_config> tuned;     // autotuner cache by workload class
 };
 

@@ -582,13 +582,13 @@ int32_t rt_instances_render(rt_ctx* c, rt_instances* I, const rt_camera* cam, in
     A.work_counter = work;
     A.status = c->d_status;
     A.inv1e6 = c->inv1e6;
-    static int occ[3] = {-1, -1, -1};
-    if (occ[kind] < 0) {
+    int& occ = c->instance_occupancy[kind];   // per context: its device's residency
+    if (occ <= 0) {
         int b = 0;
         CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, 128, 0));
-        occ[kind] = b > 0 ? b : 1;
+        occ = b > 0 ? b : 1;
     }
-    int64_t grid = (int64_t)c->num_sms * occ[kind];
+    int64_t grid = (int64_t)c->num_sms * occ;
     const int64_t useful = ((int64_t)px + 127) / 128;   // one 32-pixel tile per warp
     if (grid > useful) grid = useful;
     for (size_t k = 0; k < I->scenes.size(); ++k) {

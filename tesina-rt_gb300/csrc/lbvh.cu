@@ -23,6 +23,7 @@
 // persistent build of batch.cu.
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <mutex>
 
 #include "lbvh.cuh"
 #include "lbvh_dev.cuh"
@@ -181,14 +182,25 @@ static size_t emit_scratch_bytes(uint32_t n) { return emit_buffers_bytes(n); }
 // buffers alternate: A holds level 0, 2, ... and B level 1, 3, ....
 static cudaError_t launch_emit(const LbvhArgs& a, uint8_t* emit_scratch, cudaStream_t s) {
     const uint32_t n = a.n;
-    static const cudaError_t attr0 = cudaFuncSetAttribute(
-        k_emit_level<EMIT_C0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-        (int)sizeof(EmitSmem<EMIT_C0>));
-    static const cudaError_t attr1 = cudaFuncSetAttribute(
-        k_emit_level<EMIT_C1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-        (int)sizeof(EmitSmem<EMIT_C1>));
-    if (attr0 != cudaSuccess) return attr0;
-    if (attr1 != cudaSuccess) return attr1;
+    {
+        // the shared-memory opt-in is a property of the kernel on each device
+        static std::mutex mu;
+        static uint64_t done = 0;   // devices 0..63 set up
+        int dev = 0;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (e != cudaSuccess) return e;
+        std::lock_guard<std::mutex> lk(mu);
+        if (dev >= 64 || !((done >> dev) & 1)) {
+            e = cudaFuncSetAttribute(k_emit_level<EMIT_C0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)sizeof(EmitSmem<EMIT_C0>));
+            if (e == cudaSuccess)
+                e = cudaFuncSetAttribute(k_emit_level<EMIT_C1>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)sizeof(EmitSmem<EMIT_C1>));
+            if (e != cudaSuccess) return e;
+            if (dev < 64) done |= 1ull << dev;
+        }
+    }
     const uint32_t nb0 = emit_blocks0(n);
     const EmitBuffers B = emit_buffers(n, emit_scratch);
     k_emit_level<EMIT_C0><<<nb0, EMIT_C0, sizeof(EmitSmem<EMIT_C0>), s>>>(
