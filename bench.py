@@ -552,6 +552,58 @@ def measure_sah(ctx, torch, frames=5):
     return out
 
 
+def measure_pipelined(ctx, lib, torch, wl, dpos, dnrm, V, frames=30):
+    """The threaded renderer's overlap (RendererT: the next frame's LBVH is
+    built on a second queue while the current frame renders), with two
+    scenes on two streams: frame f renders scene f % 2 on one stream while
+    scene (f + 1) % 2 takes frame f + 1's vertices and is rebuilt on the
+    other; the library orders each scene's calls across the streams.  The
+    same frames on one stream one after another are timed beside it."""
+    from rtgb import capi
+    ter = wl["terrain"]
+    w, h, nb = wl["width"], wl["height"], wl["max_bounces"]
+    nf = len(dpos)
+    gs = [capi.Scene(ctx, ter.scene(0)), capi.Scene(ctx, ter.scene(0))]
+    sr, sb = torch.cuda.Stream(), torch.cuda.Stream()
+    hr, hb = C.c_void_p(sr.cuda_stream), C.c_void_p(sb.cuda_stream)
+    rgba = ctx.alloc(4 * w * h)
+    stats = ctx.alloc(32)
+
+    def update_build(g, i, hs):
+        capi.check(lib, lib.rt_scene_update_vertices_device(ctx.h, g.h, dpos[i % nf].ptr,
+                                                            dnrm[i % nf].ptr, V, hs))
+        g.build(30, 1, stream=hs)
+
+    def sequential():
+        for f in range(frames):
+            update_build(gs[0], f, hr)
+            gs[0].render(wl["camera"], w, h, nb, rgba, None, stats, stream=hr)
+
+    def pipelined():
+        update_build(gs[0], 0, hb)
+        for f in range(frames):
+            if f + 1 < frames:
+                update_build(gs[(f + 1) % 2], f + 1, hb)
+            gs[f % 2].render(wl["camera"], w, h, nb, rgba, None, stats, stream=hr)
+
+    out = {"workload": wl["name"], "frames": frames}
+    for name, fn in (("sequential", sequential), ("pipelined", pipelined), ("sequential", sequential),
+                     ("pipelined", pipelined)):
+        torch.cuda.synchronize()
+        stats.zero(hr)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        fn()
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        st = stats.read(np.uint64)
+        out[name] = {"ms_per_frame": dt * 1e3 / frames,
+                     "mrays_s": int(st[0] + st[1]) / dt / 1e6}
+    out["speedup"] = out["pipelined"]["mrays_s"] / out["sequential"]["mrays_s"]
+    out["device_status"] = ctx.device_status()
+    return out
+
+
 def measure_served(ctx, rates=(2000, 1000, 300, 50), n_req=400, seed=5):
     """Served workload: 32 resident scenes (soups and fBm fields alternating,
     10k-2M triangles log-uniform), a 120 GB admission budget and a scene cap
@@ -838,6 +890,12 @@ def run_gpu(args):
             refraction_leg = measure_refraction(ctx, torch)
         except Exception as e:
             refraction_leg = {"error": str(e)}
+    pipelined_leg = None
+    if world == 1 and not args.no_pipelined:
+        try:
+            pipelined_leg = measure_pipelined(ctx, lib, torch, wl, dpos, dnrm, V)
+        except Exception as e:
+            pipelined_leg = {"error": str(e)}
     sah_leg = None
     if world == 1 and not args.no_sah:
         try:
@@ -890,6 +948,7 @@ def run_gpu(args):
            "refraction": refraction_leg,
            "instances": instances_leg,
            "sah": sah_leg,
+           "pipelined": pipelined_leg,
            "e2e": {"value": e2e_value, "unit": UNIT,
                    "h2d_bytes_per_step": 2 * 16 * V,
                    "d2h_bytes_per_step": 4 * w * h + 32,
@@ -922,6 +981,7 @@ def main():
     ap.add_argument("--no-refraction", action="store_true")
     ap.add_argument("--no-instances", action="store_true")
     ap.add_argument("--no-sah", action="store_true")
+    ap.add_argument("--no-pipelined", action="store_true")
     ap.add_argument("--render-variant", type=int, default=None,
                     help="render kernel variant instead of the autotuner's pick")
     ap.add_argument("--render-blocks", type=int, default=0, help="resident blocks per SM (0: all)")
