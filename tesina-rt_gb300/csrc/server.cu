@@ -399,8 +399,9 @@ bool launch_renders(rt_server* S) {
     rt_render_stats* dstats = S->d_stats[slot];
     uint64_t launch_px = 0;
     cudaMemsetAsync(dstats, 0, sizeof(rt_render_stats), cs);
-    if (S->cfg.max_batch_views == 1) {
-        // plain per-request path: the one-scene render kernel
+    if (S->cfg.max_batch_views == 1 || take.size() == 1) {
+        // one request: the one-scene render kernel (pooled, tuned), which
+        // renders a lone image faster than the many-view kernel
         Req& q = S->reqs[take[0]];
         ServedScene& sc = S->scenes[q.r.scene_id];
         rt_render(S->ctx, sc.scene, &q.r.cam, q.r.width, q.r.height, q.r.max_bounces,
