@@ -66,6 +66,7 @@ class Oracle(_Lib):
         self.multi_render_raw = b(L, "orc_multi_render", C.c_int,
                                   [P, P, I32, I32, I32, SZ, P, P, C.c_int])
         self.build_sah_raw = b(L, "orc_build_sah", C.c_int, [P])
+        self.traversal_counts_raw = b(L, "orc_traversal_counts", C.c_int, [P, P, I32, C.c_int, P])
         self.sah_nodes_raw = b(L, "orc_sah_nodes", C.c_int, [P, P, P, P, P, P, P, C.POINTER(U32)])
 
     def multi(self, scene_handles, inst_scene, tr, trinv, lights):
@@ -152,6 +153,16 @@ class OracleScene:
                                 C.byref(cnt)):
             raise RuntimeError("no SAH tree")
         return lo, hi, a, b, leaf, order
+
+    def traversal_counts(self, samples, threads=0):
+        """{nodes, tris} entered / tested by the closest-hit rays of samples
+        and by the shadow rays of their hits, and the shadow ray count."""
+        out = np.zeros(5, np.uint64)
+        if self.o.traversal_counts_raw(self.h, _p(samples), samples.shape[0],
+                                       threads or os.cpu_count(), _p(out)):
+            raise RuntimeError("oracle scene not built")
+        return {"nodes": int(out[0]), "tris": int(out[1]), "shadow_nodes": int(out[2]),
+                "shadow_tris": int(out[3]), "shadow_rays": int(out[4])}
 
     def sort_arrays(self):
         n = self.n

@@ -422,7 +422,14 @@ static inline bool mt(const orc_scene* s, uint32_t tri, const Ray& r, float* T, 
 
 /* trace_ray (trace-bvh.cl:330-417): 32-entry stack, near child first by
  * dot(dir, right.lo - left.lo) > 0, own box tested when a node is visited. */
-static Best trace_ray(const orc_scene* s, Ray ray) {
+/* Traversal work of one ray, as the device layout pays for it: interior
+ * nodes entered (one 64-byte record each: both children's boxes and
+ * references) and triangles tested (48 bytes each). */
+struct TravCounts {
+    uint64_t nodes = 0, tris = 0;
+};
+
+static Best trace_ray(const orc_scene* s, Ray ray, TravCounts* tc = nullptr) {
     Best best{-1, ray.tmax, 0.f, 0.f};
     uint32_t levels[32];
     uint32_t level = 0, curr = 0;
@@ -437,6 +444,7 @@ static Best trace_ray(const orc_scene* s, Ray ray) {
             return best;
         }
         if (nd.leaf) {
+            if (tc) tc->tris += nd.b - nd.a;
             for (uint32_t i = nd.a; i < nd.b; ++i) {
                 float t, u, v;
                 if (!mt(s, i, ray, &t, &u, &v)) continue;
@@ -449,6 +457,7 @@ static Best trace_ray(const orc_scene* s, Ray ray) {
             }
             return best;
         }
+        if (tc) ++tc->nodes;
         const Node& l = nodes[nd.a];
         const Node& r = nodes[nd.b];
         v3 dl = sub(ld3(r.lo), ld3(l.lo));
@@ -461,7 +470,7 @@ static Best trace_ray(const orc_scene* s, Ray ray) {
 }
 
 /* trace_shadow_ray (shadow-trace-bvh.cl:237-315). */
-static bool trace_shadow(const orc_scene* s, const Ray& ray) {
+static bool trace_shadow(const orc_scene* s, const Ray& ray, TravCounts* tc = nullptr) {
     uint32_t levels[32];
     uint32_t level = 0, curr = 0;
     const Node* nodes = s->nodes.data();
@@ -475,6 +484,7 @@ static bool trace_shadow(const orc_scene* s, const Ray& ray) {
             return false;
         }
         if (nd.leaf) {
+            if (tc) tc->tris += nd.b - nd.a;
             for (uint32_t i = nd.a; i < nd.b; ++i) {
                 float t, u, v;
                 if (!mt(s, i, ray, &t, &u, &v)) continue;
@@ -486,6 +496,7 @@ static bool trace_shadow(const orc_scene* s, const Ray& ray) {
             }
             return false;
         }
+        if (tc) ++tc->nodes;
         const Node& l = nodes[nd.a];
         const Node& r = nodes[nd.b];
         v3 dl = sub(ld3(r.lo), ld3(l.lo));
@@ -531,7 +542,8 @@ static void complete(const orc_scene* s, const Ray& ray, const Best& b, rt_hit* 
 
 /* Per-light shadow ray setup of shadow_trace_single
  * (shadow-trace-bvh.cl:375-418), extended to point lights. */
-static bool light_occluded(const orc_scene* s, const rt_light& L, v3 hp) {
+static bool light_occluded(const orc_scene* s, const rt_light& L, v3 hp,
+                           TravCounts* tc = nullptr) {
     Ray r;
     r.ori = hp;
     if (L.type == RT_DIR_L) {
@@ -547,7 +559,7 @@ static bool light_occluded(const orc_scene* s, const rt_light& L, v3 hp) {
     r.inv = mk(1.0f / r.dir.x, 1.0f / r.dir.y, 1.0f / r.dir.z);
     r.tmin = 0.01f;
     r.tmax = 1e37f;
-    return trace_shadow(s, r);
+    return trace_shadow(s, r, tc);
 }
 
 /* shade_sample (ray-shader.cl:116-333), untextured, no cubemap. */
@@ -1170,6 +1182,36 @@ int orc_trace(const orc_scene* s, const rt_sample* smp, int32_t n, rt_hit* hits,
         Best b = trace_ray(s, r);
         complete(s, r, b, &hits[i]);
     });
+    return 0;
+}
+
+/* Traversal work of the closest-hit rays smp[0, n) and of the shadow rays
+ * of their hits toward each light: out = {interior nodes entered, triangles
+ * tested} of the closest-hit traversals, the same of the shadow ones, and
+ * the number of shadow rays (hits x lights). */
+int orc_traversal_counts(const orc_scene* s, const rt_sample* smp, int32_t n, int threads,
+                         uint64_t out[5]) {
+    if (!s->built) return -1;
+    std::atomic<uint64_t> acc[5];
+    for (auto& a : acc) a = 0;
+    parallel_for(n, threads, [&](int64_t i) {
+        const Ray r = ray_of(smp[i]);
+        TravCounts c, cs;
+        const Best b = trace_ray(s, r, &c);
+        if (b.id >= 0) {
+            rt_hit h;
+            std::memset(&h, 0, sizeof h);
+            complete(s, r, b, &h);
+            const v3 hp = ld3(h.hit_point);
+            for (int l = 0; l < s->lights.count; ++l) light_occluded(s, s->lights.light[l], hp, &cs);
+            acc[4] += (uint64_t)s->lights.count;
+        }
+        acc[0] += c.nodes;
+        acc[1] += c.tris;
+        acc[2] += cs.nodes;
+        acc[3] += cs.tris;
+    });
+    for (int k = 0; k < 5; ++k) out[k] = acc[k];
     return 0;
 }
 
