@@ -162,3 +162,23 @@ def test_oracle_sah_refuses_deep_trees(orc):
     s2.build_sah()
     c2 = s2.canon()
     assert c2["depth"].max() <= 32 and c2[c2["leaf"] == 1]["end"].max() == 3000
+
+
+def test_oracle_traversal_counts(orc):
+    """Traversal work counts: every ray that hits tested a triangle, shadow
+    rays number hits x lights, and a ray that misses the scene's box enters
+    no node."""
+    from helpers import tiny_terrain
+    sc = tiny_terrain(32, 16, 3).scene(0)
+    s = orc.new_scene(sc)
+    s.build(30, 1, 0)
+    cam = scenes.camera((0.0, 3.0, -6.0), (0.0, 0.0, 0.5), aspect=1.0)
+    smp = pyoracle.gen_primary(orc, cam, 64, 64)
+    c = s.traversal_counts(smp)
+    hits = int(s.trace(smp)["hit"].sum())
+    assert hits > 500 and c["shadow_rays"] == hits * sc.lights.count
+    assert c["tris"] >= hits and c["nodes"] >= hits and c["shadow_nodes"] > 0
+    # level rays 50 units above the field, looking away from it
+    away = pyoracle.gen_primary(orc, scenes.camera((0.0, 50.0, 0.0), (100.0, 50.0, 0.0)), 8, 8)
+    assert s.traversal_counts(away) == {"nodes": 0, "tris": 0, "shadow_nodes": 0,
+                                        "shadow_tris": 0, "shadow_rays": 0}
