@@ -127,7 +127,7 @@ typedef struct rt_scene_desc {
  * (src/rt/bvh-builder.cpp:194-199; clamps depth to [1,32] here, min_leaf to
  * [1,256]). */
 typedef struct rt_bvh_cfg {
-    int32_t depth;               /* Morton bits, 1..32 (spec: 30)        */
+    int32_t depth;               /* Morton bits, 1..32 (the workloads use 30)  */
     int32_t min_leaf_size;       /* 1..256                                     */
 } rt_bvh_cfg;
 
