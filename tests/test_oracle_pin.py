@@ -334,5 +334,5 @@ def test_pin_sah(orc, ref, kind):
     img_o, st_o = s.render(cam, w, h, 3, tile=1 << 20)
     assert st_o.hits > 1000
     assert np.array_equal(img_o, img_r)
-    assert st_o.secondary_rays == st_r.secondary_rays   # the driver counts no hits
+    assert st_o.secondary_rays == st_r.secondary_rays   # ref_driver.cpp counts no hits
     ref.scene_free(rh)
