@@ -4,8 +4,10 @@
 - ``_ref/libref.so``: the reference's own OpenCL kernels
   (``src/kernel/{bvh-builder,bvh-builder-sort,trace-bvh,shadow-trace-bvh,
   ray-shader,secondary-ray-generator,primary-ray-generator}.cl``) compiled
-  unmodified for the CPU through ``ref_shim/cl_shim_body.hpp``, plus the host
-  loop driver ``ref_shim/ref_driver.cpp``.  Built only where the reference
+  unmodified for the CPU through ``ref_shim/cl_shim_body.hpp`` (the two
+  work-group kernels of the LBVH build as emulated work-groups,
+  ``ref_shim/ref_emit.cpp``), plus the host loop driver
+  ``ref_shim/ref_driver.cpp``.  Built only where the reference
   checkout exists (``REFERENCE_ROOT``, default ``/root/reference``); its
   outputs stay in the git-ignored ``oracle/_ref/``.
 
@@ -22,7 +24,7 @@ REFERENCE_ROOT = os.environ.get("REFERENCE_ROOT", "/root/reference")
 CXX = os.environ.get("CXX", "g++")
 FLAGS = ["-std=c++17", "-O3", "-fPIC", "-ffp-contract=off", "-fno-strict-aliasing", "-pthread"]
 
-REF_UNITS = ["ref_bvh", "ref_sort", "ref_trace", "ref_shadow", "ref_shade",
+REF_UNITS = ["ref_bvh", "ref_emit", "ref_sort", "ref_trace", "ref_shadow", "ref_shade",
              "ref_secondary", "ref_primary", "ref_driver", "ref_mangle", "ref_obj", "ref_sah"]
 # the reference's host sources its OBJ import and CPU SAH BVH need, compiled
 # where they lie

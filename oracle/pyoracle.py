@@ -265,6 +265,9 @@ class RefKernels(_Lib):
         self.apply_perm = b(L, "refd_apply_perm", C.c_int, [P, P])
         self.get_buffers = b(L, "refd_get_buffers", C.c_int, [P, P, P])
         self.set_tree = b(L, "refd_set_tree", C.c_int, [P, P, U32])
+        self.build_lbvh_raw = b(L, "refd_build_lbvh", C.c_int,
+                                [P, C.c_int, C.c_int, C.c_int, C.c_int, P, P, P, P])
+        self.canon_raw = b(L, "refd_canon", C.c_int, [P, P, U32, C.POINTER(U32)])
         self.get_tree = b(L, "refd_get_tree", C.c_int, [P, P])
         self.gen_primary = b(L, "refd_gen_primary", C.c_int,
                              [P, I32, I32, I32, I32, P, SZ, SZ, P])
@@ -295,6 +298,27 @@ class RefKernels(_Lib):
     multi_trace = Oracle.multi_trace
     multi_shadow = Oracle.multi_shadow
     multi_render = Oracle.multi_render
+
+    def build_lbvh(self, rh, n, depth=30, min_leaf=1, group_size=16, compute_units=2):
+        """BVHBuilder::build_lbvh over the reference's own kernels (process_task
+        and max_local_bbox as emulated work-groups of group_size work-items,
+        up to compute_units groups at once).  Returns (keys, perm, glo, ghi);
+        the tree stays in the scene handle, in the reference's numbering."""
+        keys, perm = np.zeros(n, np.uint32), np.zeros(n, np.uint32)
+        glo, ghi = np.zeros(3, np.float32), np.zeros(3, np.float32)
+        if self.build_lbvh_raw(rh, depth, min_leaf, group_size, compute_units, _p(keys),
+                               _p(perm), _p(glo), _p(ghi)):
+            raise RuntimeError("reference build_lbvh failed")
+        return keys, perm, glo, ghi
+
+    def canon(self, rh):
+        """The canonical range tree (pre-order, left first) of the scene's tree."""
+        cnt = U32(0)
+        if self.canon_raw(rh, None, 0, C.byref(cnt)):
+            raise RuntimeError("malformed reference tree")
+        out = np.zeros(cnt.value, abi.CANON_DTYPE)
+        self.canon_raw(rh, _p(out), cnt.value, C.byref(cnt))
+        return out
 
     def sah_build(self, pos4, idx):
         """BVH::construct of the reference over (pos4, idx): (lo, hi, a, b,

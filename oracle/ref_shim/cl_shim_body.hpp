@@ -188,7 +188,13 @@ inline size_t get_group_id(int) { return g_wi.grp; }
 inline size_t get_num_groups(int) { return g_wi.ngrp; }
 
 enum { CLK_LOCAL_MEM_FENCE = 1, CLK_GLOBAL_MEM_FENCE = 2 };
-inline void barrier(int) {}
+/* A kernel run one work-item at a time has nothing to wait for; a kernel run
+ * as an emulated work-group (ref_emit.cpp) sets the hook to its group's
+ * barrier on every thread of the group. */
+inline thread_local void (*g_barrier_hook)(void) = nullptr;
+inline void barrier(int) {
+    if (g_barrier_hook) g_barrier_hook();
+}
 inline int atomic_add(int* p, int v) { return __atomic_fetch_add(p, v, __ATOMIC_SEQ_CST); }
 inline unsigned atomic_add(unsigned* p, unsigned v) { return __atomic_fetch_add(p, v, __ATOMIC_SEQ_CST); }
 

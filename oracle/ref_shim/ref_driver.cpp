@@ -10,12 +10,14 @@
  *   secondary generation      src/rt/secondary-ray-generator.cpp:148-244
  *                             (mark -> exclusive scan -> generate, "disc")
  *   tile / bounce loop        src/rt/renderer.cpp:113-214
- * Two device stages are restated rather than compiled because they rely on
- * work-group barriers and __local variables that a one-work-item-at-a-time
- * CPU run cannot express: the global AABB reduction (max_local_bbox,
- * bvh-builder.cl:318-391: an order-free min/max) and the hierarchy emit
- * (process_task, bvh-builder.cl:582-671), which is taken from the caller as a
- * canonical range tree.
+ *   level loop, OC readback   src/rt/bvh-builder.cpp:548-625 (ref_emit.cpp)
+ * The two work-group kernels, max_local_bbox (bvh-builder.cl:318-391) and
+ * process_task (bvh-builder.cl:582-671), run as emulated work-groups in
+ * ref_emit.cpp; refd_build_lbvh chains every stage of build_lbvh
+ * (bvh-builder.cpp:201-741) over the reference's own kernels.  The older
+ * entry points refd_morton (order-free global AABB) and refd_set_tree (a
+ * canonical range tree laid out and refitted by the reference's kernels) stay
+ * for pins of single stages.
  */
 #include <algorithm>
 #include <cmath>
@@ -39,6 +41,7 @@ void refk_bbox_get(const void* bboxes, size_t i, float* lo3, float* hi3);
 void refk_morton_get(const void* codes, size_t n, unsigned* lo, unsigned* hi);
 void refk_rearrange_indices(int* in, unsigned* tris, int* out, size_t n);
 void refk_rearrange_map(int* in, unsigned* tris, int* out, size_t n);
+void refk_rearrange_morton_codes(void* in, unsigned* tris, void* out, size_t n);
 void refk_node_set(void* nodes, size_t i, unsigned a, unsigned b, unsigned parent, int leaf);
 void refk_node_get(const void* nodes, size_t i, float* lo3, float* hi3, unsigned* a, unsigned* b,
                    int* leaf);
@@ -65,6 +68,13 @@ void refk_mark_secondary_rays_disc(rt_hit* info, rt_sample* samples, rt_material
 void refk_generate_secondary_rays_disc(rt_hit* info, rt_sample* samples, rt_material* mats,
                                        unsigned* map, rt_sample* out, int* count,
                                        int refract_offset, int max_count, size_t n);
+int refe_global_bbox(const void* bboxes, uint32_t n, int group_size, int concurrent, float* lo3,
+                     float* hi3);
+int64_t refe_process_levels(const uint32_t* sorted, uint32_t n, int depth, int min_leaf,
+                            int group_size, int compute_units, void* nodes_out,
+                            uint32_t* level_end);
+size_t refe_sizeof_node(void);
+size_t refe_sizeof_bbox(void);
 void refk_generate_primary_rays(rt_sample* samples, const float* pos, const float* dir,
                                 const float* right, const float* up, int w, int h, int quad, int spp,
                                 const rt_pixel_sample* ps, size_t count, size_t offset);
@@ -256,6 +266,109 @@ int refd_set_tree(refd_scene* s, const rt_canon_node* canon, uint32_t n) {
         uint32_t b = start[d], e = start[d + 1];
         if (e > b) refk_build_node_bbox(s->nodes.data(), b, e - b);
     }
+    return 0;
+}
+
+/* Pre-order walk (left first) of the reference's node array from the root:
+ * the canonical range tree.  Interior ranges come from the subtrees, since
+ * set_children overwrites an interior node's range with its child indices;
+ * any nonzero `leaf` byte is a leaf (nodes of the last launched level keep
+ * the level they would have checked next). */
+static int canon_walk(refd_scene* s, uint32_t k, uint32_t depth, std::vector<rt_canon_node>& out,
+                      std::vector<uint32_t>& ref_of) {
+    if (k >= s->nnodes || out.size() >= s->nnodes || depth > 64) return -1;
+    const size_t me = out.size();
+    out.emplace_back();
+    ref_of.push_back(k);
+    rt_canon_node c;
+    std::memset(&c, 0, sizeof(c));
+    unsigned a, b;
+    int leaf;
+    refk_node_get(s->nodes.data(), k, c.lo, c.hi, &a, &b, &leaf);
+    c.depth = depth;
+    if (leaf) {
+        c.leaf = 1;
+        c.start = a;
+        c.end = b;
+    } else {
+        if (canon_walk(s, a, depth + 1, out, ref_of)) return -1;
+        const size_t r = out.size();
+        if (canon_walk(s, b, depth + 1, out, ref_of)) return -1;
+        c.start = out[me + 1].start;
+        c.end = out[r].end;
+    }
+    out[me] = c;
+    return 0;
+}
+
+/* BVHBuilder::build_lbvh (bvh-builder.cpp:201-741) over the reference's own
+ * kernels: build_primitive_bbox, the max_local_bbox reduction, morton_encode,
+ * the bitonic network, rearrange_indices / map / morton_codes, process_task
+ * level by level, build_leaf_bbox over every node and build_node_bbox level
+ * by level from the deepest.  depth and min_leaf are clamped as
+ * update_configuration does (bvh-builder.cpp:194-199); depths above 32 are
+ * refused (the keys here are one 32-bit word).  group_size and
+ * compute_units shape the emulated launches (the device's
+ * max_group_size() and CL_DEVICE_MAX_COMPUTE_UNITS).  Outputs: the
+ * unsorted keys, the permutation, the global AABB; the tree stays in the
+ * scene (reference numbering) for refd_canon, trace and render. */
+int refd_build_lbvh(refd_scene* s, int depth, int min_leaf, int group_size, int compute_units,
+                    uint32_t* keys_out, uint32_t* perm_out, float* glo_out, float* ghi_out) {
+    depth = std::min(std::max(depth, 1), 64);
+    min_leaf = std::min(std::max(min_leaf, 1), 256);
+    if (depth > 32 || s->N == 0) return -1;
+    const size_t N = s->N;
+    std::vector<uint8_t> bboxes(refk_sizeof_bbox() * N);
+    std::vector<unsigned> tris(N);
+    refk_build_primitive_bbox(s->vtx.data(), s->idx.data(), bboxes.data(), tris.data(), N);
+    float glo[3], ghi[3];
+    if (refe_global_bbox(bboxes.data(), s->N, group_size, 2, glo, ghi)) return -1;
+    std::vector<uint8_t> codes(refk_sizeof_morton() * N);
+    refk_morton_encode(bboxes.data(), glo, ghi, codes.data(), depth, N);
+    std::vector<uint32_t> keys(N), hi(N), perm(N);
+    refk_morton_get(codes.data(), N, keys.data(), hi.data());
+    for (size_t i = 0; i < N; ++i)
+        if (hi[i] != 0) return -1;
+    if (refd_bitonic(keys.data(), s->N, perm.data())) return -1;
+    refd_apply_perm(s, perm.data());
+    std::vector<uint8_t> sorted_codes(codes.size());
+    refk_rearrange_morton_codes(codes.data(), perm.data(), sorted_codes.data(), N);
+    std::vector<uint32_t> sorted(N);
+    refk_morton_get(sorted_codes.data(), N, sorted.data(), nullptr);
+    s->nodes.assign(refe_sizeof_node() * 2 * N, 0);
+    uint32_t level_end[64];
+    const int64_t cnt = refe_process_levels(sorted.data(), s->N, depth, min_leaf, group_size,
+                                            compute_units, s->nodes.data(), level_end);
+    if (cnt < 1) return -1;
+    s->nnodes = (uint32_t)cnt;
+    refk_build_leaf_bbox(perm.data(), bboxes.data(), s->nodes.data(), s->nnodes);
+    for (int i = depth - 1; i >= 0; --i) {
+        const uint32_t start = i ? level_end[i - 1] : 0;
+        const uint32_t count = level_end[i] - start;
+        if (count) refk_build_node_bbox(s->nodes.data(), start, count);
+    }
+    std::vector<rt_canon_node> canon;
+    std::vector<uint32_t> ref_of;
+    if (canon_walk(s, 0, 0, canon, ref_of)) return -1;
+    s->canon_to_ref = ref_of;
+    if (keys_out) std::memcpy(keys_out, keys.data(), 4 * N);
+    if (perm_out) std::memcpy(perm_out, perm.data(), 4 * N);
+    if (glo_out) std::memcpy(glo_out, glo, sizeof(glo));
+    if (ghi_out) std::memcpy(ghi_out, ghi, sizeof(ghi));
+    return 0;
+}
+
+/* The canonical range tree of the scene's reference-numbered tree (after
+ * refd_build_lbvh): the node count in *count; nodes into out when cap holds
+ * them.  The walk visits every node once when the tree is well formed. */
+int refd_canon(refd_scene* s, rt_canon_node* out, uint32_t cap, uint32_t* count) {
+    std::vector<rt_canon_node> canon;
+    std::vector<uint32_t> ref_of;
+    if (canon_walk(s, 0, 0, canon, ref_of)) return -1;
+    *count = (uint32_t)canon.size();
+    if (!out) return 0;
+    if (cap < canon.size()) return -1;
+    std::memcpy(out, canon.data(), sizeof(rt_canon_node) * canon.size());
     return 0;
 }
 

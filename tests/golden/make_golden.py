@@ -43,20 +43,11 @@ def cases():
 def golden_for(R, name, sc, cam, w, h, bounces):
     n = sc.n_tris
     rh = R.new_scene(sc)
-    keys = np.zeros(n, np.uint32)
-    assert R.morton(rh, 30, _p(keys), None, None) == 0
-    perm = np.zeros(n, np.uint32)
-    assert R.bitonic(_p(keys), n, _p(perm)) == 0
-    # the tree's AABBs come from the reference's leaf/node refit kernels on
-    # the oracle's canonical ranges
-    orc = pyoracle.Oracle()
-    os_ = orc.new_scene(sc)
-    os_.build(30, 1, 1)                         # bitonic order = the reference's
-    canon = os_.canon()
-    R.apply_perm(rh, _p(perm))
-    assert R.set_tree(rh, _p(canon), canon.shape[0]) == 0
-    tree = canon.copy()
-    R.get_tree(rh, _p(tree))
+    # BVHBuilder::build_lbvh over the reference's own kernels: Morton keys,
+    # bitonic permutation, the process_task tree (emulated work-groups) and
+    # its refit boxes, all from the reference
+    keys, perm, _, _ = R.build_lbvh(rh, n, 30, 1)
+    tree = R.canon(rh)
     smp = np.zeros(w * h, abi.SAMPLE_DTYPE)
     R.gen_primary(C.byref(cam), w, h, 32, 1, None, w * h, 0, _p(smp))
     hits = np.zeros(w * h, abi.HIT_DTYPE)

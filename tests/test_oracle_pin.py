@@ -99,6 +99,80 @@ def test_pin_full_render_small_workload(orc, ref):
     ref.scene_free(rh)
 
 
+def _ref_vs_oracle_tree(orc, ref, sc, depth, min_leaf, group_size=16, compute_units=2):
+    """BVHBuilder::build_lbvh run over the reference's own kernels (the emit
+    and the global AABB reduction as emulated work-groups) against the
+    oracle's build: keys, permutation, sorted buffers and the canonical tree
+    (ranges, leaf flags, depths, AABBs) byte for byte."""
+    rh = ref.new_scene(sc)
+    keys, perm, glo, ghi = ref.build_lbvh(rh, sc.n_tris, depth, min_leaf, group_size,
+                                          compute_units)
+    s = orc.new_scene(sc)
+    s.build(depth, min_leaf, 1)
+    ok, op, _, _ = s.sort_arrays()
+    assert np.array_equal(keys, ok), "Morton keys"
+    assert np.array_equal(perm, op), "bitonic permutation"
+    ir, mr = np.zeros((sc.n_tris, 3), np.uint32), np.zeros(sc.n_tris, np.uint32)
+    ref.get_buffers(rh, _p(ir), _p(mr))
+    io, mo = s.buffers()
+    assert np.array_equal(ir, io) and np.array_equal(mr, mo)
+    # the max_local_bbox reduction equals the order-free min / max
+    tri = sc.pos4[sc.idx.astype(np.int64)][:, :, :3]
+    assert np.array_equal(glo, tri.min(axis=(0, 1))) and np.array_equal(ghi, tri.max(axis=(0, 1)))
+    rc, oc = ref.canon(rh), s.canon()
+    assert rc.shape == oc.shape, "node count %d vs %d" % (rc.shape[0], oc.shape[0])
+    assert rc.tobytes() == oc.tobytes()
+    return rh, s, rc
+
+
+def test_pin_emit_soup_10k(orc, ref):
+    """The 10k soup: the reference's process_task tree is the oracle's."""
+    rh, _, rc = _ref_vs_oracle_tree(orc, ref, scenes.soup(10000, seed=1), 30, 1)
+    assert int(rc["leaf"].sum()) > 2000
+    ref.scene_free(rh)
+
+
+@pytest.mark.parametrize("min_leaf", [1, 4, 256])
+@pytest.mark.parametrize("depth", [1, 10, 16, 30, 32])
+def test_pin_emit_terrain_duplicates(orc, ref, depth, min_leaf):
+    """The duplicate-heavy terrain (shared grid vertices, flat cells, so many
+    equal keys) over the depth and minimum-leaf range: large leaves of equal
+    keys, the bit-exhausted leaf rule and the last launched level."""
+    rh, _, _ = _ref_vs_oracle_tree(orc, ref, tiny_terrain().scene(1), depth, min_leaf)
+    ref.scene_free(rh)
+
+
+@pytest.mark.parametrize("n", [17, 2047, 4097])
+def test_pin_emit_sizes(orc, ref, n):
+    rh, _, _ = _ref_vs_oracle_tree(orc, ref, scenes.soup(n, seed=n), 30, 1)
+    ref.scene_free(rh)
+
+
+@pytest.mark.parametrize("group_size,compute_units", [(2, 1), (8, 4), (64, 3)])
+def test_pin_emit_launch_shapes(orc, ref, group_size, compute_units):
+    """Work-group size and group count change the reference's node numbering,
+    not its range tree."""
+    rh, _, _ = _ref_vs_oracle_tree(orc, ref, tiny_terrain(48, 24, 2, seed=9).scene(3), 30, 1,
+                                   group_size, compute_units)
+    ref.scene_free(rh)
+
+
+def test_pin_render_over_reference_tree(orc, ref):
+    """The 512x512, depth-3 soup rendered by the reference's kernels over the
+    tree its own builder emitted (reference node numbering, boxes from its
+    refit kernels) equals the oracle's render."""
+    wl = scenes.workload_small()
+    rh, s, _ = _ref_vs_oracle_tree(orc, ref, wl["scene"], 30, 1)
+    img_o, st_o = s.render(wl["camera"], 512, 512, 3)
+    img_r = np.zeros((512 * 512, 3), np.uint32)
+    st_r = abi.RenderStats()
+    ref.render(rh, C.byref(wl["camera"]), 512, 512, 3, 0, 512 * 512, 1 << 18, _p(img_r),
+               C.byref(st_r), 8)
+    assert np.array_equal(img_o, img_r)
+    assert st_o.secondary_rays == st_r.secondary_rays > 0
+    ref.scene_free(rh)
+
+
 @pytest.mark.parametrize("depth", [30, 10, 1])
 def test_pin_terrain_duplicates(orc, ref, depth):
     """Equal keys: the oracle's bitonic restatement reproduces the reference's
