@@ -199,6 +199,16 @@ RT_API int32_t rt_init(rt_ctx** ctx, int32_t device);
 RT_API int32_t rt_shutdown(rt_ctx* ctx);
 /* Reads (and clears) the device status word: RT_DEV_* bits. */
 RT_API int32_t rt_device_status(rt_ctx* ctx, uint32_t* bits);
+/* Self-test of the device-side timeout (no reference counterpart; the
+ * failure-detection form of a bounded wait): launches one radix-pass tile
+ * whose predecessor tile is never launched, so its decoupled look-back polls
+ * an unpublished word until its limit (1,024 polls here) runs out.  The
+ * kernel then sets RT_DEV_TIMEOUT, finishes its tile inside its buffers and
+ * returns; the call synchronises and maps the status as rt_render_host does:
+ * RT_ERR_TIMEOUT when the timeout path worked (RT_OK would mean it did not).
+ * The status stays set for rt_device_status to read and clear; the context
+ * stays usable. */
+RT_API int32_t rt_selftest_wait_timeout(rt_ctx* ctx, rt_stream s);
 RT_API int32_t rt_stream_create(rt_ctx* ctx, rt_stream* stream);
 RT_API int32_t rt_stream_destroy(rt_ctx* ctx, rt_stream stream);
 RT_API int32_t rt_stream_sync(rt_ctx* ctx, rt_stream stream);
@@ -523,9 +533,14 @@ RT_API int32_t rt_render_host(rt_ctx* ctx, rt_scene* scene, const float* h_pos4,
  * reference.  Allocates nothing: its scratch is a fixed ~9 MiB array in
  * device memory that every GPU loading this library keeps until exit.
  *   - n > RT_NOALLOC_MAX_PAIRS is rejected with RT_ERR_INVALID;
- *   - inputs are not modified; outputs must not alias them;
- *   - every call on a device shares the one scratch array: calls that
- *     overlap on the GPU race; order them on one stream;
+ *   - inputs are not modified; an output that overlaps an input or the
+ *     other output is rejected with RT_ERR_INVALID;
+ *   - every call on a device shares the one scratch array, whichever rt_ctx
+ *     it comes from: calls that overlap on the GPU race, also across
+ *     contexts; order them on one stream, or with events between streams;
+ *   - the return code covers the arguments and the launches; a device-side
+ *     failure (a look-back wait that gave up) is reported as RT_DEV_TIMEOUT
+ *     by rt_device_status, which the caller reads after synchronising;
  *   - the first call on a device looks up the array's device address; make
  *     that call before any stream capture. */
 RT_API int32_t rt_sort_pairs_noalloc(rt_ctx* ctx, const uint32_t* d_keys_in,

@@ -418,6 +418,23 @@ int32_t rt_device_status(rt_ctx* c, uint32_t* bits) {
     return RT_OK;
 }
 
+int32_t rt_selftest_wait_timeout(rt_ctx* c, rt_stream stream) {
+    if (!c) return fail(RT_ERR_INVALID, "rt_selftest_wait_timeout: null context");
+    cudaStream_t cs = stream ? (cudaStream_t)stream : c->stream;
+    uint32_t* buf = nullptr;
+    CU(cudaMalloc(&buf, sizeof(uint32_t) * rt::wait_probe_words()));
+    const cudaError_t e = rt::wait_probe(buf, c->d_status, cs);
+    const cudaError_t e2 = cudaStreamSynchronize(cs);
+    cudaFree(buf);
+    CU(e);
+    CU(e2);
+    uint32_t bits = 0;
+    CU(cudaMemcpy(&bits, c->d_status, sizeof(bits), cudaMemcpyDeviceToHost));
+    if (bits & RT_DEV_TIMEOUT)
+        return fail(RT_ERR_TIMEOUT, "rt_selftest_wait_timeout: device wait timed out");
+    return RT_OK;
+}
+
 int32_t rt_stream_create(rt_ctx* c, rt_stream* s) {
     if (!c || !s) return fail(RT_ERR_INVALID, "rt_stream_create: null argument");
     cudaStream_t x;

@@ -124,6 +124,19 @@ __global__ void __launch_bounds__(SORT_THREADS, 3) k_onesweep(
     onesweep_tile(S, S.tile, kin, vin, kout, vout, n, shift, hist, lookback, status);
 }
 
+// Self-test of the look-back timeout: one block sorts tile 1 of a pass
+// whose tile 0 is never launched, so its look-back word stays unpublished;
+// with a spin limit of 1,024 polls the wait gives up at once.
+constexpr uint32_t kProbeSpinLimit = 1024;
+__global__ void __launch_bounds__(SORT_THREADS, 1) k_onesweep_wait_probe(
+    const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin, uint32_t* __restrict__ kout,
+    uint32_t* __restrict__ vout, uint32_t n, const uint32_t* __restrict__ hist,
+    uint32_t* __restrict__ lookback, uint32_t* __restrict__ status) {
+    __shared__ SortSmem S;
+    onesweep_tile<SORT_ITEMS, kProbeSpinLimit>(S, 1, kin, vin, kout, vout, n, 0, hist, lookback,
+                                               status);
+}
+
 __global__ void __launch_bounds__(256) k_permute(
     uint32_t n, const uint32_t* __restrict__ vals, const uint32_t* __restrict__ idx_old,
     const uint32_t* __restrict__ map_old, const uint32_t* __restrict__ orig_old,
@@ -280,6 +293,25 @@ size_t radix_scratch_words(uint32_t n, int passes) {
 }
 
 int radix_tile_size() { return SORT_TILE; }
+
+size_t wait_probe_words() { return (size_t)2 * SORT_TILE * 4 + 256 + 2 * 256; }
+
+cudaError_t wait_probe(uint32_t* buf, uint32_t* status, cudaStream_t s) {
+    // buf: keys | vals | kout | vout (2 tiles each) | hist[256] | lookback[2 * 256]
+    const uint32_t n = 2 * SORT_TILE;
+    uint32_t* keys = buf;
+    uint32_t* vals = keys + n;
+    uint32_t* kout = vals + n;
+    uint32_t* vout = kout + n;
+    uint32_t* hist = vout + n;
+    uint32_t* lookback = hist + 256;
+    cudaError_t e = cudaMemsetAsync(buf, 0, sizeof(uint32_t) * wait_probe_words(), s);
+    if (e) return e;
+    k_radix_hist<<<1, 256, 0, s>>>(keys, n, 1, hist);
+    k_onesweep_wait_probe<<<1, SORT_THREADS, 0, s>>>(keys, vals, kout, vout, n, hist, lookback,
+                                                     status);
+    return cudaGetLastError();
+}
 
 cudaError_t radix_sort_pairs(const uint32_t* kin, const uint32_t* vin, uint32_t* kout,
                              uint32_t* vout, uint32_t* ktmp, uint32_t* vtmp, uint32_t n,

@@ -54,6 +54,11 @@ cudaError_t lbvh_permute(const LbvhArgs& a, const uint32_t* order, cudaStream_t 
 // caller-provided scratch (radix_scratch_words words) and temporaries of n
 // pairs; passes alternate between out and tmp so that the last lands in out.
 size_t radix_scratch_words(uint32_t n, int passes);
+// Self-test of the device timeout path: a radix-pass tile whose predecessor
+// never publishes, in a zeroed buffer of wait_probe_words() words; sets
+// RT_DEV_TIMEOUT in *status.
+size_t wait_probe_words();
+cudaError_t wait_probe(uint32_t* buf, uint32_t* status, cudaStream_t s);
 int radix_tile_size();
 cudaError_t radix_sort_pairs(const uint32_t* kin, const uint32_t* vin, uint32_t* kout,
                              uint32_t* vout, uint32_t* ktmp, uint32_t* vtmp, uint32_t n,

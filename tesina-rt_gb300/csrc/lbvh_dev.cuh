@@ -173,8 +173,13 @@ using SortSmem = SortSmemT<SORT_ITEMS>;
 // loads, ballot ranking in index order, decoupled look-back over
 // the earlier tiles of the same sequence, shared-memory staging and a
 // coalesced scatter.  Must be called by all SORT_THREADS threads of a block;
-// a tile holds SORT_THREADS * ITEMS keys.
-template <int ITEMS = SORT_ITEMS>
+// a tile holds SORT_THREADS * ITEMS keys.  A look-back that polls an
+// unpublished word more than SPIN_LIMIT times gives up: it sets
+// RT_DEV_TIMEOUT in *status and goes on with the counts it has, so every
+// block ends; the tile's writes then stay inside [0, n), since a partial
+// prefix only lowers the scatter offsets, which start at the digit's global
+// offset.
+template <int ITEMS = SORT_ITEMS, uint32_t SPIN_LIMIT = LB_SPIN_LIMIT>
 __device__ __forceinline__ void onesweep_tile(SortSmemT<ITEMS>& S, uint32_t tile,
                                               const uint32_t* __restrict__ kin,
                                               const uint32_t* __restrict__ vin,
@@ -280,7 +285,7 @@ __device__ __forceinline__ void onesweep_tile(SortSmemT<ITEMS>& S, uint32_t tile
             }
             if (done) break;
             p -= used;
-            if (wait && ++spins > LB_SPIN_LIMIT) {
+            if (wait && ++spins > SPIN_LIMIT) {
                 atomicOr(status, RT_DEV_TIMEOUT);
                 break;
             }

@@ -14,9 +14,13 @@
 //     RT_ERR_INVALID and leave the outputs untouched;
 //   - the array (about 9 MiB) is reserved on every GPU that loads the
 //     library, for the life of the process;
-//   - all calls on a device share the one array: calls that overlap on the
-//     GPU (different streams, or different host threads without ordering)
-//     race and corrupt each other's results.  Serialize them on one stream;
+//   - all calls on a device share the one array, whichever rt_ctx they come
+//     from: calls that overlap on the GPU (different streams or contexts, or
+//     different host threads without ordering) race and corrupt each other's
+//     results.  Serialize them on one stream, or order them with events;
+//   - a device-side failure (a look-back wait that gave up) does not change
+//     the return code: it sets RT_DEV_TIMEOUT in the context's status, which
+//     rt_device_status reads after the caller synchronises;
 //   - the first call on a device looks up the array's device address
 //     (cudaGetSymbolAddress) and caches it; make that first call before
 //     any stream capture begins.
@@ -64,6 +68,21 @@ int32_t scratch_for_device(int dev, uint32_t** out) {
     return RT_OK;
 }
 
+// True when the byte range of an output, [p, p + 4n), meets an input's or
+// the other output's.  A pass that runs out of place reads one pair of
+// arrays while it writes the other, so any overlap corrupts the result
+// (with an odd pass count the first pass writes the outputs while it still
+// reads the inputs).
+bool overlapping(const uint32_t* ki, const uint32_t* vi, const uint32_t* ko, const uint32_t* vo,
+                 uint32_t n) {
+    const uintptr_t len = 4 * (uintptr_t)n;
+    auto meet = [len](const uint32_t* a, const uint32_t* b) {
+        const uintptr_t x = (uintptr_t)a, y = (uintptr_t)b;
+        return x < y + len && y < x + len;
+    };
+    return meet(ko, ki) || meet(ko, vi) || meet(vo, ki) || meet(vo, vi) || meet(ko, vo);
+}
+
 }  // namespace
 
 extern "C" RT_API int32_t rt_sort_pairs_noalloc(rt_ctx* ctx, const uint32_t* d_keys_in,
@@ -81,8 +100,9 @@ extern "C" RT_API int32_t rt_sort_pairs_noalloc(rt_ctx* ctx, const uint32_t* d_k
                              key_bits);
     if (n > 0 && (!d_keys_in || !d_vals_in || !d_keys_out || !d_vals_out))
         return rt::set_error(RT_ERR_INVALID, "rt_sort_pairs_noalloc: null buffer");
-    if (n > 0 && (d_keys_out == d_keys_in || d_vals_out == d_vals_in))
-        return rt::set_error(RT_ERR_INVALID, "rt_sort_pairs_noalloc: outputs must not alias inputs");
+    if (n > 0 && overlapping(d_keys_in, d_vals_in, d_keys_out, d_vals_out, n))
+        return rt::set_error(RT_ERR_INVALID,
+                             "rt_sort_pairs_noalloc: an output overlaps an input or the other output");
     int cur = -1;
     cudaError_t e = cudaGetDevice(&cur);
     if (e != cudaSuccess) return rt::set_error(RT_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e));

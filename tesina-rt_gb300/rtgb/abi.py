@@ -5,6 +5,8 @@ import numpy as np
 
 RT_MAX_LIGHTS = 8
 RT_SPOT_L, RT_DIR_L, RT_POINT_L = 0, 1, 2
+RT_OK, RT_ERR_TIMEOUT, RT_ERR_OVERFLOW = 0, -5, -7          # rt_status
+RT_DEV_TIMEOUT, RT_DEV_OVERFLOW, RT_DEV_BADINDEX = 0x1, 0x2, 0x4   # device status bits
 
 
 class Light(C.Structure):

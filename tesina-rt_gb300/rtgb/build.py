@@ -1,4 +1,6 @@
-"""In-tree build of librt_cuda.so for sm_103a (nvcc, no cmake).
+"""In-tree build of librt_cuda.so for sm_103a (nvcc, no cmake), and of
+librt_shim.so, the drop-in C++ classes over it (g++; headers in
+include/rt and include/gpu).
 
 All CUDA translation units are compiled with ``--fmad=false`` so that the
 single-precision math follows the reference kernels' operation order without
@@ -45,7 +47,40 @@ def stale():
     return any(os.path.getmtime(s) > t for s in _sources())
 
 
+SHIM = os.path.join(PKG, "librt_shim.so")
+SHIM_SRC = os.path.join(PKG, "shim")
+INCLUDE = os.path.join(PKG, "..", "include")
+CXX = os.environ.get("CXX", "g++")
+
+
+def _shim_sources():
+    return sorted(os.path.join(SHIM_SRC, f) for f in os.listdir(SHIM_SRC) if f.endswith(".cpp"))
+
+
+def build_shim(force=False):
+    """librt_shim.so: BVHBuilder, Tracer, RayShader, SecondaryRayGenerator,
+    PrimaryRayGenerator, FrameBuffer, Scene, RayBundle / HitBundle and
+    DeviceInterface / DeviceMemory over librt_cuda.so (found beside it)."""
+    deps = _shim_sources() + [LIB]
+    for d in ("rt", "gpu"):
+        deps += [os.path.join(INCLUDE, d, f) for f in os.listdir(os.path.join(INCLUDE, d))]
+    if not force and os.path.exists(SHIM) and all(os.path.getmtime(x) <= os.path.getmtime(SHIM)
+                                                  for x in deps):
+        return SHIM
+    tmp = SHIM + ".tmp"
+    _run([CXX, "-std=c++17", "-O2", "-fPIC", "-shared", "-Wall", "-I", INCLUDE] + _shim_sources() +
+         ["-L", PKG, "-lrt_cuda", "-Wl,-rpath,$ORIGIN", "-o", tmp])
+    os.replace(tmp, SHIM)
+    return SHIM
+
+
 def build(force=False, verbose=False):
+    _build_cuda(force, verbose)
+    build_shim(force)
+    return LIB
+
+
+def _build_cuda(force, verbose):
     if not force and not stale():
         return LIB
     os.makedirs(OBJDIR, exist_ok=True)

@@ -24,6 +24,7 @@ SIGNATURES = {
     "rt_init": (I32, [C.POINTER(P), I32]),
     "rt_shutdown": (I32, [P]),
     "rt_device_status": (I32, [P, C.POINTER(U32)]),
+    "rt_selftest_wait_timeout": (I32, [P, P]),
     "rt_stream_create": (I32, [P, C.POINTER(P)]),
     "rt_stream_destroy": (I32, [P, P]),
     "rt_stream_sync": (I32, [P, P]),
@@ -178,6 +179,11 @@ class Context:
         bits = U32(0)
         check(self.lib, self.lib.rt_device_status(self.h, C.byref(bits)))
         return bits.value
+
+    def selftest_wait_timeout(self, stream=None):
+        """rt_selftest_wait_timeout: the raw status (RT_ERR_TIMEOUT when the
+        device wait gave up, as it should)."""
+        return self.lib.rt_selftest_wait_timeout(self.h, stream)
 
     # stage-wise pipeline ---------------------------------------------------
     def gen_primary(self, cam, w, h, out_buf, count=None, offset=0, quad=32, stream=None):

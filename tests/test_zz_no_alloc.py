@@ -65,3 +65,48 @@ def test_noalloc_sort_limits(ctx):
     k, v = _noalloc_sort(ctx, keys, vals, key_bits=32)
     order = np.argsort(keys, kind="stable")
     assert np.array_equal(k, keys[order]) and np.array_equal(v, vals[order])
+
+
+@pytest.mark.parametrize("key_bits", [8, 24])
+def test_noalloc_sort_odd_pass_counts(ctx, key_bits):
+    """One and three 8-bit passes: the first pass writes the outputs and the
+    passes route through the scratch temporaries in the other order.  Stable
+    order of keys & mask, as numpy's stable argsort."""
+    rng = np.random.default_rng(key_bits)
+    n = 300_001
+    keys = rng.integers(0, 2 ** 32, size=n, dtype=np.uint64).astype(np.uint32)
+    vals = rng.permutation(n).astype(np.uint32)
+    k, v = _noalloc_sort(ctx, keys, vals, key_bits=key_bits)
+    order = np.argsort(keys & np.uint32((1 << key_bits) - 1), kind="stable")
+    assert np.array_equal(k, keys[order]) and np.array_equal(v, vals[order])
+    assert ctx.device_status() == 0
+
+
+def test_noalloc_sort_empty_and_overlap(ctx):
+    """n = 0 returns RT_OK; an output that overlaps an input, even by one
+    pair, or the other output is refused; buffers that only touch sort."""
+    lib = ctx.lib
+    assert lib.rt_sort_pairs_noalloc(ctx.h, None, None, None, None, 0, 30, None) == 0
+    n = 1024
+    rng = np.random.default_rng(11)
+    data = rng.integers(0, 2 ** 30, size=4 * n, dtype=np.uint64).astype(np.uint32)
+    buf = ctx.to_device(data)                  # 4 arrays of n pairs' worth, back to back
+    b, q = buf.ptr.value, 4 * n                # q: bytes of one array
+    refused = [(b, b + q, b + 2 * q, b + 4),              # values out inside keys in
+               (b, b + q, b, b + 3 * q),                  # keys out == keys in
+               (b, b + q, b + 2 * q, b + 2 * q + q // 2),  # the two outputs meet
+               (b, b + q, b + q - 4, b + 3 * q)]           # keys out starts in values in
+    for ki, vi, ko, vo in refused:
+        r = lib.rt_sort_pairs_noalloc(ctx.h, C.c_void_p(ki), C.c_void_p(vi), C.c_void_p(ko),
+                                      C.c_void_p(vo), n, 30, None)
+        assert r == -2 and b"overlaps" in lib.rt_last_error()
+    # inputs in arrays 2 and 3, outputs in 0 and 1: adjacent ranges, no overlap
+    r = lib.rt_sort_pairs_noalloc(ctx.h, C.c_void_p(b + 2 * q), C.c_void_p(b + 3 * q),
+                                  C.c_void_p(b), C.c_void_p(b + q), n, 30, None)
+    assert r == 0
+    ctx.sync()
+    out = buf.read(np.uint32)
+    keys, vals = data[2 * n:3 * n], data[3 * n:]
+    order = np.argsort(keys, kind="stable")
+    assert np.array_equal(out[:n], keys[order]) and np.array_equal(out[n:2 * n], vals[order])
+    assert ctx.device_status() == 0
