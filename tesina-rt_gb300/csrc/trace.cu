@@ -6,6 +6,7 @@
 #include "rt_internal.cuh"
 #include "trace.cuh"
 #include "trace_dev.cuh"
+#include "render_refill.cuh"
 
 namespace rt {
 
@@ -717,6 +718,9 @@ static const RenderVariant kVariants[] = {
     {128, 6, k_render<128, 6, true>, false, true},
     {128, 4, k_render_pool_refr<128, 4, 6>, true, true, 6},
     {128, 5, k_render_pool_refr<128, 5, 4>, true, true, 4},
+    {128, 6, k_render_refill<128, 6, 8>, true},  {128, 8, k_render_refill<128, 8, 8>, true},
+    {256, 3, k_render_refill<256, 3, 8>, true},  {128, 6, k_render_refill<128, 6, 4>, true},
+    {128, 6, k_render_refill<128, 6, 16>, true},
 };
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 static_assert(kNumVariants <= kMaxRenderVariants, "per-variant context arrays");
