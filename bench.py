@@ -36,9 +36,10 @@ METRIC = "Whitted Mrays/s (primary+secondary), full LBVH rebuild per frame"
 UNIT = "Mrays/s"
 B_BUILD_PER_TRI = 312 + 16 * 4      # algorithmic LBVH bytes per triangle, 4 radix passes
 B_RAY_CLOSEST, B_RAY_SHADOW, B_SHADE = 40, 25, 48
-# DRAM bytes (read + write) of one k_render_pool<128, 6> launch on the
-# mid-scale frame, from the ncu capture summarised in profiles/.
-RENDER_POOL_DRAM_BYTES = (324.8 + 35.7) * 1e6
+# dram__bytes_read.sum + dram__bytes_write.sum of one launch of a render
+# kernel on the mid-scale frame (ncu, --clock-control none), by kernel; the
+# line's roofline carries it only when the autotuner installed that kernel.
+RENDER_DRAM_BYTES = {"k_render_pool<128, 6>": (324.8 + 35.7) * 1e6}
 
 
 def log(*a):
@@ -110,49 +111,121 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def cpu_baseline(wl, frame_pos, frame_nrm, sample_rays=65536):
-    """Oracle (CPU restatement) on a bounded sample of one frame: a full LBVH
-    build plus the first `sample_rays` primary samples of the frame in the
-    reference's tile order, all host cores.  The build time is charged in
-    proportion to the sampled fraction of the frame."""
+def cpu_model():
+    """The host CPU's model name (lscpu, else /proc/cpuinfo)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=20).stdout
+        for line in out.splitlines():
+            if line.strip().startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith(("model name", "cpu part")):
+                    return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    return "unknown"
+
+
+def _oracle():
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import build as ob
     import pyoracle
     ob.build_oracle()
-    from rtgb import scenes
-    orc = pyoracle.Oracle()
-    ter = wl["terrain"]
-    sc = scenes.Scene(frame_pos, frame_nrm, ter.idx, ter.mats, ter.mat_map, ter.lights)
-    s = orc.new_scene(sc)
-    threads = os.cpu_count() or 1
+    return pyoracle, pyoracle.Oracle()
+
+
+def _block_rows(w, h, every):
+    """Sample ranges spread over the frame: every `every`-th row of the
+    reference's 32 x 32 pixel blocks (rays are generated block by block, so
+    one block row is one contiguous range of samples)."""
+    per_row = (w // 32) * 1024
+    rows = range(0, h // 32, every)
+    return [(r * per_row, per_row) for r in rows]
+
+
+def _oracle_sample(s, cam, w, h, nb, ranges, threads):
+    t0 = time.perf_counter()
+    rays = shadow = 0
+    for off, cnt in ranges:
+        _, st = s.render(cam, w, h, nb, offset=off, count=cnt, threads=threads)
+        rays += st.primary_rays + st.secondary_rays
+        shadow += st.shadow_rays
+    return time.perf_counter() - t0, rays, shadow
+
+
+def cpu_baseline(scene, cam, w, h, nb, every=8, one_thread=True):
+    """The oracle (CPU restatement of the reference's kernels) on a bounded,
+    spread sample of one frame: the full LBVH build (sequential, as the
+    restatement builds) and every `every`-th row of 32 x 32 pixel blocks
+    traced, shadowed, shaded and reflected to the frame's depth, on all host
+    cores and on one.  The build is charged in proportion to the sampled
+    fraction of the frame; Mrays/s counts primary + secondary rays."""
+    pyoracle, orc = _oracle()
+    s = orc.new_scene(scene)
     t0 = time.perf_counter()
     s.build(30, 1, 0)
     t_build = time.perf_counter() - t0
-    w, h = wl["width"], wl["height"]
+    ranges = _block_rows(w, h, every)
+    n_smp = sum(c for _, c in ranges)
+    frac = n_smp / float(w * h)
+    threads = os.cpu_count() or 1
+    t_n, rays, shadow = _oracle_sample(s, cam, w, h, nb, ranges, threads)
+    out = {"value": rays / (t_build * frac + t_n) / 1e6, "unit": UNIT, "cores": threads,
+           "kind": "port", "cpu_model": cpu_model(),
+           "sample": "oracle: full LBVH build of %d triangles (%.3f s, one thread, charged x%.4f) "
+                     "+ every %dth row of 32x32 pixel blocks of the %dx%d frame (%d samples, "
+                     "%.1f %%; %d primary + secondary rays) traced to depth %d on %d threads "
+                     "(%.3f s)" % (scene.n_tris, t_build, frac, every, w, h, n_smp, 100 * frac,
+                                   rays, nb, threads, t_n),
+           "lbvh_mtri_s": scene.n_tris / t_build / 1e6,
+           "mrays_all_incl_shadow": (rays + shadow) / (t_build * frac + t_n) / 1e6}
+    if one_thread:
+        t_1, rays1, _ = _oracle_sample(s, cam, w, h, nb, ranges, 1)
+        out["one_thread"] = {"value": rays1 / (t_build * frac + t_1) / 1e6, "cores": 1,
+                             "render_s": t_1}
+    return out, s
+
+
+def cpu_c0_full():
+    """The small workload (10k-triangle soup, 512 x 512, depth 3) run in full
+    on the oracle: LBVH build + the whole frame, one thread and all."""
+    from rtgb import scenes
+    pyoracle, orc = _oracle()
+    wl = scenes.workload_small()
+    s = orc.new_scene(wl["scene"])
     t0 = time.perf_counter()
-    _, st = s.render(wl["camera"], w, h, wl["max_bounces"], offset=0, count=sample_rays,
-                     threads=threads)
-    t_render = time.perf_counter() - t0
-    frac = sample_rays / float(w * h)
-    rays = st.primary_rays + st.secondary_rays
-    t = t_build * frac + t_render
-    # traversal work per ray of the same sample's primary rays and of their
-    # shadow rays (interior node records entered, 64 B; triangles tested, 48 B)
-    smp = pyoracle.gen_primary(orc, wl["camera"], w, h, count=sample_rays)
-    tc = s.traversal_counts(smp, threads=threads)
+    s.build(30, 1, 0)
+    t_build = time.perf_counter() - t0
+    out = {"workload": wl["name"], "build_s": t_build,
+           "lbvh_mtri_s": wl["scene"].n_tris / t_build / 1e6}
+    for name, thr in (("one_thread", 1), ("all_threads", os.cpu_count() or 1)):
+        t0 = time.perf_counter()
+        _, st = s.render(wl["camera"], 512, 512, 3, threads=thr)
+        t = time.perf_counter() - t0
+        rays = st.primary_rays + st.secondary_rays
+        out[name] = {"cores": thr, "render_s": t, "rays": rays,
+                     "mrays_s": rays / (t_build + t) / 1e6}
+    return out
+
+
+def traversal_work(s, cam, w, h, sample_rays=65536):
+    """Node and triangle records the oracle's traversal reads per primary ray
+    and per shadow ray of those rays (interior nodes entered, 64 B each;
+    triangles tested, 48 B), on the first `sample_rays` samples."""
+    pyoracle, orc = _oracle()
+    smp = pyoracle.gen_primary(orc, cam, w, h, count=sample_rays)
+    tc = s.traversal_counts(smp, threads=os.cpu_count() or 1)
     n_sh = max(1, tc["shadow_rays"])
-    trav = {"rays": sample_rays, "nodes_per_ray": tc["nodes"] / sample_rays,
+    return {"rays": sample_rays, "nodes_per_ray": tc["nodes"] / sample_rays,
             "tris_per_ray": tc["tris"] / sample_rays,
             "shadow_nodes_per_ray": tc["shadow_nodes"] / n_sh,
             "shadow_tris_per_ray": tc["shadow_tris"] / n_sh,
             "bytes_per_ray": (64 * tc["nodes"] + 48 * tc["tris"]) / sample_rays,
             "bytes_per_shadow_ray": (64 * tc["shadow_nodes"] + 48 * tc["shadow_tris"]) / n_sh}
-    return {"value": rays / t / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
-            "traversal": trav,
-            "sample": "oracle build of the full frame (%d tris, %.3f s, charged x%.4f) + first %d "
-                      "primary samples of 1920x1080 with their reflections (%.3f s)"
-                      % (sc.n_tris, t_build, frac, sample_rays, t_render),
-            "lbvh_mtri_s": sc.n_tris / t_build / 1e6}
 
 
 def emit_levels_of(n):
@@ -237,15 +310,18 @@ def measure_batched(ctx, lib, torch, reps=5):
             "launches_plain": sum(7 + emit_levels_of(it["scene"].n_tris) + 2 for it in items)}
 
 
-def measure_stress(ctx, torch, builds=5):
+def measure_stress(ctx, lib, torch, builds=5, cpu=True):
     """Plain method at stress scale: a 4096x2048-cell fBm field plus 1,000
     mirror spheres (17,737,216 triangles), one LBVH build timed `builds`
     times (median), then one 3840x2160 Whitted frame (3 point lights, depth
     6) from each of 8 camera poses on a radius-10 sphere.  Build Mtri/s is
     reported against the HBM roofline with the same 376 B/triangle model as
     the main workload; Mrays/s counts primary + secondary rays (and,
-    separately, shadow rays too)."""
-    from rtgb import capi, scenes
+    separately, shadow rays too).  The leg has its own e2e (build and the
+    first pose through rt_render_host from pinned host vertices to a host
+    RGBA8 image), render roofline and CPU baseline (the oracle on a spread
+    sample of the first pose)."""
+    from rtgb import abi, capi, scenes
     wl = scenes.workload_stress()
     t = time.time()
     sc = wl["terrain"].scene(0)
@@ -283,6 +359,34 @@ def measure_stress(ctx, torch, builds=5):
     mb = statistics.median(t_build)
     ach = B_BUILD_PER_TRI * sc.n_tris / (mb * 1e-3) / 1e9
     tr = sum(t_render)
+    render_bytes = rays * (B_RAY_CLOSEST + B_SHADE) + shadow * B_RAY_SHADOW
+    render_gbs = render_bytes / (tr * 1e-3) / 1e9
+    # e2e: upload + build + pose 0 + RGBA8 download per step
+    V = sc.n_verts
+    pin_pos = torch.from_numpy(np.ascontiguousarray(sc.pos4)).pin_memory()
+    pin_nrm = torch.from_numpy(np.ascontiguousarray(sc.nrm4)).pin_memory()
+    host_rgba = torch.empty((h * w, 4), dtype=torch.uint8).pin_memory()
+    cfg = abi.BvhCfg(wl["depth"], wl["min_leaf"])
+    hst = abi.RenderStats()
+    e2e_ms, e2e_rays = [], 0
+    for k in range(4):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        capi.check(lib, lib.rt_render_host(ctx.h, g.h, C.c_void_p(pin_pos.data_ptr()),
+                                           C.c_void_p(pin_nrm.data_ptr()), V, C.byref(cfg),
+                                           C.byref(wl["cameras"][0]), w, h, nb,
+                                           C.c_void_p(host_rgba.data_ptr()), C.byref(hst), sh))
+        e1.record(stream)
+        stream.synchronize()
+        if k:
+            e2e_ms.append(e0.elapsed_time(e1))
+            e2e_rays += int(hst.primary_rays + hst.secondary_rays)
+    cpu_leg = None
+    if cpu:
+        try:
+            cpu_leg, _ = cpu_baseline(sc, wl["cameras"][0], w, h, nb, every=16, one_thread=False)
+        except Exception as e:
+            cpu_leg = {"value": None, "sample": "failed: %s" % e}
     return {"workload": wl["name"], "triangles": sc.n_tris, "width": w, "height": h,
             "max_bounces": nb, "lights": 3, "poses": len(wl["cameras"]),
             "build_ms": mb, "lbvh_mtri_s": sc.n_tris / (mb * 1e-3) / 1e6,
@@ -292,6 +396,14 @@ def measure_stress(ctx, torch, builds=5):
             "render_ms_per_pose": tr / len(t_render), "rays": rays, "shadow_rays": shadow,
             "mrays_s": rays / (tr * 1e-3) / 1e6,
             "mrays_all_incl_shadow": (rays + shadow) / (tr * 1e-3) / 1e6,
+            "roofline": {"kernel": "render (installed variant)", "bound": "hbm",
+                         "achieved": render_gbs, "peak": hbm, "unit": "GB/s",
+                         "frac": render_gbs / hbm, "traffic": None, "peak_kind": kind,
+                         "algorithmic_bytes_per_pose": render_bytes / len(t_render)},
+            "e2e": {"value": e2e_rays / (sum(e2e_ms) * 1e-3) / 1e6, "unit": UNIT,
+                    "h2d_bytes_per_step": 2 * 16 * V, "d2h_bytes_per_step": 4 * w * h + 32,
+                    "ms_per_step": statistics.median(e2e_ms)},
+            "cpu_baseline": cpu_leg,
             "device_status": ctx.device_status()}
 
 
@@ -564,58 +676,6 @@ def measure_sah(ctx, torch, frames=5):
     return out
 
 
-def measure_pipelined(ctx, lib, torch, wl, dpos, dnrm, V, frames=30):
-    """The threaded renderer's overlap (RendererT: the next frame's LBVH is
-    built on a second queue while the current frame renders), with two
-    scenes on two streams: frame f renders scene f % 2 on one stream while
-    scene (f + 1) % 2 takes frame f + 1's vertices and is rebuilt on the
-    other; the library orders each scene's calls across the streams.  The
-    same frames on one stream one after another are timed beside it."""
-    from rtgb import capi
-    ter = wl["terrain"]
-    w, h, nb = wl["width"], wl["height"], wl["max_bounces"]
-    nf = len(dpos)
-    gs = [capi.Scene(ctx, ter.scene(0)), capi.Scene(ctx, ter.scene(0))]
-    sr, sb = torch.cuda.Stream(), torch.cuda.Stream()
-    hr, hb = C.c_void_p(sr.cuda_stream), C.c_void_p(sb.cuda_stream)
-    rgba = ctx.alloc(4 * w * h)
-    stats = ctx.alloc(32)
-
-    def update_build(g, i, hs):
-        capi.check(lib, lib.rt_scene_update_vertices_device(ctx.h, g.h, dpos[i % nf].ptr,
-                                                            dnrm[i % nf].ptr, V, hs))
-        g.build(30, 1, stream=hs)
-
-    def sequential():
-        for f in range(frames):
-            update_build(gs[0], f, hr)
-            gs[0].render(wl["camera"], w, h, nb, rgba, None, stats, stream=hr)
-
-    def pipelined():
-        update_build(gs[0], 0, hb)
-        for f in range(frames):
-            if f + 1 < frames:
-                update_build(gs[(f + 1) % 2], f + 1, hb)
-            gs[f % 2].render(wl["camera"], w, h, nb, rgba, None, stats, stream=hr)
-
-    out = {"workload": wl["name"], "frames": frames}
-    for name, fn in (("sequential", sequential), ("pipelined", pipelined), ("sequential", sequential),
-                     ("pipelined", pipelined)):
-        torch.cuda.synchronize()
-        stats.zero(hr)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        fn()
-        torch.cuda.synchronize()
-        dt = time.perf_counter() - t0
-        st = stats.read(np.uint64)
-        out[name] = {"ms_per_frame": dt * 1e3 / frames,
-                     "mrays_s": int(st[0] + st[1]) / dt / 1e6}
-    out["speedup"] = out["pipelined"]["mrays_s"] / out["sequential"]["mrays_s"]
-    out["device_status"] = ctx.device_status()
-    return out
-
-
 def measure_served(ctx, rates=(2000, 1000, 300, 50), n_req=400, seed=5):
     """Served workload: 32 resident scenes (soups and fBm fields alternating,
     10k-2M triangles log-uniform), a 120 GB admission budget and a scene cap
@@ -683,10 +743,13 @@ def run_reference(args):
         return 0
     from rtgb import scenes
     wl = scenes.workload_mid()
+    ter = wl["terrain"]
     vals = []
     for i in range(args.warmup + args.steps):
-        pos, nrm = wl["terrain"].frame_vertices(i % 60)
-        r = cpu_baseline(wl, pos, nrm)
+        pos, nrm = ter.frame_vertices(i % 60)
+        sc = scenes.Scene(pos, nrm, ter.idx, ter.mats, ter.mat_map, ter.lights)
+        r, _ = cpu_baseline(sc, wl["camera"], wl["width"], wl["height"], wl["max_bounces"],
+                            one_thread=False)
         if i >= args.warmup:
             vals.append(r)
     v = statistics.median([r["value"] for r in vals])
@@ -697,7 +760,8 @@ def run_reference(args):
                       "width": wl["width"], "height": wl["height"],
                       "max_bounces": wl["max_bounces"], "lights": 2, "lbvh_depth": 30},
            "cpu_baseline": {"value": v, "unit": UNIT, "cores": vals[-1]["cores"],
-                            "kind": "port", "sample": vals[-1]["sample"]},
+                            "kind": "port", "sample": vals[-1]["sample"],
+                            "cpu_model": vals[-1]["cpu_model"]},
            "lbvh_mtri_s": statistics.median([r["lbvh_mtri_s"] for r in vals]),
            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
@@ -856,15 +920,15 @@ def run_gpu(args):
     build_bytes = n_tris * B_BUILD_PER_TRI
     build_gbs = build_bytes / (med_build * 1e-3) / 1e9
     pooled = ctx.variant_pooled(tuned.variant)
-    roofline = {"kernel": ("k_render_pool (pooled trace + shadow + shade + reflect)" if pooled
-                           else "k_render (fused trace + shadow + shade + reflect)"), "bound": "hbm",
-                "achieved": render_gbs, "peak": peak, "unit": "GB/s",
+    vt, vm, _ = ctx.variants()[tuned.variant]
+    kname = ("k_render_pool<%d, %d>" if pooled else "k_render<%d, %d>") % (vt, vm)
+    roofline = {"kernel": kname + (" (pooled trace + shadow + shade + reflect)" if pooled
+                                   else " (fused trace + shadow + shade + reflect)"),
+                "bound": "hbm", "achieved": render_gbs, "peak": peak, "unit": "GB/s",
                 "frac": render_gbs / peak,
                 # dram__bytes_read.sum + dram__bytes_write.sum of one launch of
-                # k_render_pool<128, 6> on this frame (ncu, 324.8 + 35.7 MB)
-                "traffic": RENDER_POOL_DRAM_BYTES if pooled else None,
-                "traffic_source": ("profiles/k_render_pool_terrain1M_1920x1080.md" if pooled
-                                   else None),
+                # the installed kernel on this frame, when one was captured
+                "traffic": RENDER_DRAM_BYTES.get(kname),
                 "peak_kind": peak_kind,
                 "algorithmic_bytes_per_launch": render_bytes,
                 "note": "traversal is latency/L2-bound; algorithmic bytes = 88 B per traced "
@@ -887,7 +951,7 @@ def run_gpu(args):
     stress = None
     if world == 1 and not args.no_stress:
         try:
-            stress = measure_stress(ctx, torch)
+            stress = measure_stress(ctx, lib, torch, cpu=not args.no_cpu_baseline)
         except Exception as e:
             stress = {"error": str(e)}
     refit_leg = None
@@ -902,12 +966,6 @@ def run_gpu(args):
             refraction_leg = measure_refraction(ctx, torch)
         except Exception as e:
             refraction_leg = {"error": str(e)}
-    pipelined_leg = None
-    if world == 1 and not args.no_pipelined:
-        try:
-            pipelined_leg = measure_pipelined(ctx, lib, torch, wl, dpos, dnrm, V)
-        except Exception as e:
-            pipelined_leg = {"error": str(e)}
     sah_leg = None
     if world == 1 and not args.no_sah:
         try:
@@ -932,15 +990,18 @@ def run_gpu(args):
             served_leg = measure_served(ctx)
         except Exception as e:
             served_leg = {"error": str(e)}
-    cpu = None
+    cpu, tv = None, None
     if world == 1 and not args.no_cpu_baseline:
         try:
-            cpu = cpu_baseline(wl, frames[0][0], frames[0][1])
+            sc0 = scenes.Scene(frames[0][0], frames[0][1], ter.idx, ter.mats, ter.mat_map,
+                               ter.lights)
+            cpu, osc = cpu_baseline(sc0, wl["camera"], w, h, nb)
+            cpu["c0_full"] = cpu_c0_full()
+            tv = traversal_work(osc, wl["camera"], w, h)
         except Exception as e:   # the oracle must not break the GPU line
             cpu = {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
                    "sample": "failed: %s" % e}
-    if cpu and cpu.get("traversal"):
-        tv = cpu.pop("traversal")
+    if tv:
         tb = tv["bytes_per_ray"] * rays_step + tv["bytes_per_shadow_ray"] * shadow_step
         roofline["traversal"] = dict(tv, bytes_per_frame=tb,
                                      gbs=tb / (med_render * 1e-3) / 1e9,
@@ -969,7 +1030,6 @@ def run_gpu(args):
            "refraction": refraction_leg,
            "instances": instances_leg,
            "sah": sah_leg,
-           "pipelined": pipelined_leg,
            "e2e": {"value": e2e_value, "unit": UNIT,
                    "h2d_bytes_per_step": 2 * 16 * V,
                    "d2h_bytes_per_step": 4 * w * h + 32,
@@ -1002,7 +1062,6 @@ def main():
     ap.add_argument("--no-refraction", action="store_true")
     ap.add_argument("--no-instances", action="store_true")
     ap.add_argument("--no-sah", action="store_true")
-    ap.add_argument("--no-pipelined", action="store_true")
     ap.add_argument("--render-variant", type=int, default=None,
                     help="render kernel variant instead of the autotuner's pick")
     ap.add_argument("--render-blocks", type=int, default=0, help="resident blocks per SM (0: all)")

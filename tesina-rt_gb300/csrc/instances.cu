@@ -348,8 +348,8 @@ __global__ void __launch_bounds__(128, MAXB == 6 ? 5 : RT_INST_MINB) k_render_in
         }
         __syncwarp();
         const int nl = sA.lights.count;
-        for (int t = lane; t < nh * nl; t += 32) {
-            const int k = t / nl, l = t - k * nl;
+        for (int t = lane; t < nh * nl; t += 32) {   // light-major, as k_render_pool
+            const int l = t / nh, k = t - l * nh;
             const f3 p = mk3(Q.hp[0][k], Q.hp[1][k], Q.hp[2][k]);
             if (occluded_multi(sA, sA.lights.light[l], p)) atomicOr(&Q.hmask[k], 1u << l);
         }
