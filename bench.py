@@ -220,7 +220,8 @@ def traversal_work(s, cam, w, h, sample_rays=65536):
     smp = pyoracle.gen_primary(orc, cam, w, h, count=sample_rays)
     tc = s.traversal_counts(smp, threads=os.cpu_count() or 1)
     n_sh = max(1, tc["shadow_rays"])
-    return {"rays": sample_rays, "nodes_per_ray": tc["nodes"] / sample_rays,
+    return {"rays": sample_rays, "shadow_traced_frac": tc["shadow_traced"] / n_sh,
+            "nodes_per_ray": tc["nodes"] / sample_rays,
             "tris_per_ray": tc["tris"] / sample_rays,
             "shadow_nodes_per_ray": tc["shadow_nodes"] / n_sh,
             "shadow_tris_per_ray": tc["shadow_tris"] / n_sh,

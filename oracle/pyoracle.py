@@ -156,13 +156,15 @@ class OracleScene:
 
     def traversal_counts(self, samples, threads=0):
         """{nodes, tris} entered / tested by the closest-hit rays of samples
-        and by the shadow rays of their hits, and the shadow ray count."""
-        out = np.zeros(5, np.uint64)
+        and by the shadow rays of their hits that the fused renders trace,
+        the shadow ray count and the number traced."""
+        out = np.zeros(6, np.uint64)
         if self.o.traversal_counts_raw(self.h, _p(samples), samples.shape[0],
                                        threads or os.cpu_count(), _p(out)):
             raise RuntimeError("oracle scene not built")
         return {"nodes": int(out[0]), "tris": int(out[1]), "shadow_nodes": int(out[2]),
-                "shadow_tris": int(out[3]), "shadow_rays": int(out[4])}
+                "shadow_tris": int(out[3]), "shadow_rays": int(out[4]),
+                "shadow_traced": int(out[5])}
 
     def sort_arrays(self):
         n = self.n

@@ -1185,14 +1185,38 @@ int orc_trace(const orc_scene* s, const rt_sample* smp, int32_t n, rt_hit* hits,
     return 0;
 }
 
+/* Whether light L adds nothing to a hit's colour whatever its shadow ray
+ * finds (shade_one's term with cosL = clamp(dot(n, -Ld), 0, 1) = 0 and finite
+ * colours): the GPU's fused renders do not trace that shadow ray, and the
+ * work counts below follow them.  Counting aid only; the oracle's own
+ * shadow and render functions trace every shadow ray. */
+static bool light_vanishes(const rt_light& L, const rt_material& mat, v3 hp, v3 n) {
+    v3 Ld;
+    float LD = 1.0f;
+    if (L.type == RT_DIR_L) {
+        Ld = ld3(L.dir);
+    } else if (L.type == RT_SPOT_L) {
+        Ld = normalize(sub(hp, ld3(L.pos)));
+        LD = clamp01((dot(Ld, ld3(L.dir)) - L.angle) / (1.0f - L.angle));
+    } else {
+        Ld = normalize(sub(hp, ld3(L.pos)));
+    }
+    const v3 rgb = muls(ld3(L.color), LD);
+    return clamp01(dot(n, neg(Ld))) == 0.0f && std::isfinite(rgb.x) && std::isfinite(rgb.y) &&
+           std::isfinite(rgb.z) && std::isfinite(mat.diffuse[0]) &&
+           std::isfinite(mat.diffuse[1]) && std::isfinite(mat.diffuse[2]) &&
+           std::isfinite(mat.shininess);
+}
+
 /* Traversal work of the closest-hit rays smp[0, n) and of the shadow rays
  * of their hits toward each light: out = {interior nodes entered, triangles
- * tested} of the closest-hit traversals, the same of the shadow ones, and
- * the number of shadow rays (hits x lights). */
+ * tested} of the closest-hit traversals, the same of the shadow ones over
+ * the shadow rays the fused GPU renders trace, the number of shadow rays
+ * (hits x lights) and the number of them traced. */
 int orc_traversal_counts(const orc_scene* s, const rt_sample* smp, int32_t n, int threads,
-                         uint64_t out[5]) {
+                         uint64_t out[6]) {
     if (!s->built) return -1;
-    std::atomic<uint64_t> acc[5];
+    std::atomic<uint64_t> acc[6];
     for (auto& a : acc) a = 0;
     parallel_for(n, threads, [&](int64_t i) {
         const Ray r = ray_of(smp[i]);
@@ -1202,8 +1226,13 @@ int orc_traversal_counts(const orc_scene* s, const rt_sample* smp, int32_t n, in
             rt_hit h;
             std::memset(&h, 0, sizeof h);
             complete(s, r, b, &h);
-            const v3 hp = ld3(h.hit_point);
-            for (int l = 0; l < s->lights.count; ++l) light_occluded(s, s->lights.light[l], hp, &cs);
+            const v3 hp = ld3(h.hit_point), hn = ld3(h.n);
+            const rt_material& mat = s->mats[s->map[h.id]];
+            for (int l = 0; l < s->lights.count; ++l) {
+                if (light_vanishes(s->lights.light[l], mat, hp, hn)) continue;
+                light_occluded(s, s->lights.light[l], hp, &cs);
+                acc[5] += 1;
+            }
             acc[4] += (uint64_t)s->lights.count;
         }
         acc[0] += c.nodes;
@@ -1211,7 +1240,7 @@ int orc_traversal_counts(const orc_scene* s, const rt_sample* smp, int32_t n, in
         acc[2] += cs.nodes;
         acc[3] += cs.tris;
     });
-    for (int k = 0; k < 5; ++k) out[k] = acc[k];
+    for (int k = 0; k < 6; ++k) out[k] = acc[k];
     return 0;
 }
 

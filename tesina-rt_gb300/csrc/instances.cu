@@ -351,7 +351,11 @@ __global__ void __launch_bounds__(128, MAXB == 6 ? 5 : RT_INST_MINB) k_render_in
         for (int t = lane; t < nh * nl; t += 32) {   // light-major, as k_render_pool
             const int l = t / nh, k = t - l * nh;
             const f3 p = mk3(Q.hp[0][k], Q.hp[1][k], Q.hp[2][k]);
-            if (occluded_multi(sA, sA.lights.light[l], p)) atomicOr(&Q.hmask[k], 1u << l);
+            const f3 nk = mk3(Q.hn[0][k], Q.hn[1][k], Q.hn[2][k]);
+            const SceneView& Sk = sA.roots[Q.hroot[k]].scene;
+            if (!light_vanishes(sA.lights.light[l], Sk.mats[__ldg(&Sk.map[Q.hid[k]])], p, nk) &&
+                occluded_multi(sA, sA.lights.light[l], p))
+                atomicOr(&Q.hmask[k], 1u << l);
         }
         __syncwarp();
         bool push = false, push_t = false;

@@ -192,7 +192,10 @@ __global__ void __launch_bounds__(THREADS, MINB) k_render_pool(RenderArgs a) {
         for (int t = lane; t < nh * nl; t += 32) {
             const int l = t / nh, k = t - l * nh;
             const f3 p = mk3(Q.hp[0][k], Q.hp[1][k], Q.hp[2][k]);
-            if (occluded(S, H, sL.light[l], p, a.status)) atomicOr(&Q.hmask[k], 1u << l);
+            const f3 nk = mk3(Q.hn[0][k], Q.hn[1][k], Q.hn[2][k]);
+            if (!light_vanishes(sL.light[l], S.mats[__ldg(&S.map[Q.hid[k]])], p, nk) &&
+                occluded(S, H, sL.light[l], p, a.status))
+                atomicOr(&Q.hmask[k], 1u << l);
         }
         __syncwarp();
         // 4. shading; continuing paths put their reflection ray into the pool
@@ -364,7 +367,10 @@ __global__ void __launch_bounds__(THREADS, MINB) k_render_pool_refr(RenderArgs a
         for (int t = lane; t < nh * nl; t += 32) {   // light-major, as k_render_pool
             const int l = t / nh, k = t - l * nh;
             const f3 p = mk3(Q.hp[0][k], Q.hp[1][k], Q.hp[2][k]);
-            if (occluded(S, H, sL.light[l], p, a.status)) atomicOr(&Q.hmask[k], 1u << l);
+            const f3 nk = mk3(Q.hn[0][k], Q.hn[1][k], Q.hn[2][k]);
+            if (!light_vanishes(sL.light[l], S.mats[__ldg(&S.map[Q.hid[k]])], p, nk) &&
+                occluded(S, H, sL.light[l], p, a.status))
+                atomicOr(&Q.hmask[k], 1u << l);
         }
         __syncwarp();
         // shading; the continuing rays of each hit: reflected, refracted

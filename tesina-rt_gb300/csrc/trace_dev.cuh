@@ -371,6 +371,46 @@ __device__ __forceinline__ bool occluded(const SceneView& S, const BvhHeader& H,
     return WW ? any_hit_ww(S, H, r, 1e37f, status) : any_hit(S, H, r, 1e37f, status);
 }
 
+// Light direction (from the light toward the hit) and colour at a hit, as
+// shade_sample computes them (ray-shader.cl:116-333; point lights without a
+// cone).
+__device__ __forceinline__ void light_at(const rt_light& L, f3 hp, f3& Ld, f3& rgb) {
+    rgb = mk3(L.color[0], L.color[1], L.color[2]);
+    float LD;
+    if (L.type == RT_DIR_L) {
+        Ld = mk3(L.dir[0], L.dir[1], L.dir[2]);
+        LD = 1.0f;
+    } else if (L.type == RT_SPOT_L) {
+        Ld = normalize(sub(hp, mk3(L.pos[0], L.pos[1], L.pos[2])));
+        LD = dot(Ld, mk3(L.dir[0], L.dir[1], L.dir[2])) - L.angle;
+        LD /= 1.0f - L.angle;
+        LD = clamp01(LD);
+    } else {
+        Ld = normalize(sub(hp, mk3(L.pos[0], L.pos[1], L.pos[2])));
+        LD = 1.0f;
+    }
+    rgb = muls(rgb, LD);
+}
+
+// True when light L adds nothing to the hit's colour whether or not its
+// shadow ray is blocked: the light is behind the surface (cosL =
+// clamp(dot(n, -Ld), 0, 1) = 0, NaN included), which zeroes both the
+// diffuse term rgb * diffuse * cosL and the specular term
+// rgb * spec^8 * cosL * shininess as long as the light colour, the diffuse
+// colour and the shininess are finite.  Skipping that shadow ray leaves a
+// sum that differs at most in the sign of a zero, which floor(f * 1e6) to an
+// integer removes, so the image is the same.  Only the fused renders skip;
+// the stage-wise shadow pass reports every ray's result.
+__device__ __forceinline__ bool light_vanishes(const rt_light& L, const rt_material& mat, f3 hp,
+                                               f3 n) {
+    f3 Ld, rgb;
+    light_at(L, hp, Ld, rgb);
+    const float cosL = clamp01(dot(n, neg(Ld)));
+    return cosL == 0.0f && isfinite(rgb.x) && isfinite(rgb.y) && isfinite(rgb.z) &&
+           isfinite(mat.diffuse[0]) && isfinite(mat.diffuse[1]) && isfinite(mat.diffuse[2]) &&
+           isfinite(mat.shininess);
+}
+
 // Local Whitted term of shade_sample, as the fixed-point increments that
 // to_color_int + image[pixel] += produce (ray-shader.cl:101-109, 312-330).
 __device__ __forceinline__ uint3 shade_hit(const rt_lights& Ls, const rt_material& mat, f3 hp, f3 n,
@@ -379,21 +419,8 @@ __device__ __forceinline__ uint3 shade_hit(const rt_lights& Ls, const rt_materia
     f3 val = mul(mk3(Ls.ambient[0], Ls.ambient[1], Ls.ambient[2]), diffuse);
     for (int l = 0; l < Ls.count; ++l) {
         const rt_light& L = Ls.light[l];
-        f3 Ld, rgb = mk3(L.color[0], L.color[1], L.color[2]);
-        float LD;
-        if (L.type == RT_DIR_L) {
-            Ld = mk3(L.dir[0], L.dir[1], L.dir[2]);
-            LD = 1.0f;
-        } else if (L.type == RT_SPOT_L) {
-            Ld = normalize(sub(hp, mk3(L.pos[0], L.pos[1], L.pos[2])));
-            LD = dot(Ld, mk3(L.dir[0], L.dir[1], L.dir[2])) - L.angle;
-            LD /= 1.0f - L.angle;
-            LD = clamp01(LD);
-        } else {
-            Ld = normalize(sub(hp, mk3(L.pos[0], L.pos[1], L.pos[2])));
-            LD = 1.0f;
-        }
-        rgb = muls(rgb, LD);
+        f3 Ld, rgb;
+        light_at(L, hp, Ld, rgb);
         if (!((shadow_mask >> l) & 1u)) {
             const float dn = dot(d, n);
             const f3 rr = sub(d, muls(muls(n, 2.0f), dn));
@@ -552,7 +579,9 @@ __device__ __forceinline__ PixelResult render_pixel(const SceneView& S, const Bv
             const rt_material mat = S.mats[__ldg(&S.map[hit.id])];
             uint32_t mask = 0;
             for (int l = 0; l < L.count; ++l)
-                if (occluded<WW>(S, H, L.light[l], hi.hp, status)) mask |= 1u << l;
+                if (!light_vanishes(L.light[l], mat, hi.hp, hi.n) &&
+                    occluded<WW>(S, H, L.light[l], hi.hp, status))
+                    mask |= 1u << l;
             res.shadow += (uint32_t)L.count;
             const uint3 c = shade_hit(L, mat, hi.hp, hi.n, d, contribution, mask);
             res.r += c.x;

@@ -178,7 +178,10 @@ def test_oracle_traversal_counts(orc):
     hits = int(s.trace(smp)["hit"].sum())
     assert hits > 500 and c["shadow_rays"] == hits * sc.lights.count
     assert c["tris"] >= hits and c["nodes"] >= hits and c["shadow_nodes"] > 0
+    # the shadow rays of lights behind the surface are not traced (and the
+    # field's hits facing the lights are)
+    assert 0 < c["shadow_traced"] < c["shadow_rays"]
     # level rays 50 units above the field, looking away from it
     away = pyoracle.gen_primary(orc, scenes.camera((0.0, 50.0, 0.0), (100.0, 50.0, 0.0)), 8, 8)
     assert s.traversal_counts(away) == {"nodes": 0, "tris": 0, "shadow_nodes": 0,
-                                        "shadow_tris": 0, "shadow_rays": 0}
+                                        "shadow_tris": 0, "shadow_rays": 0, "shadow_traced": 0}
