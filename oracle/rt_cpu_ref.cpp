@@ -1186,11 +1186,13 @@ int orc_trace(const orc_scene* s, const rt_sample* smp, int32_t n, rt_hit* hits,
 }
 
 /* Whether light L adds nothing to a hit's colour whatever its shadow ray
- * finds (shade_one's term with cosL = clamp(dot(n, -Ld), 0, 1) = 0 and finite
- * colours): the GPU's fused renders do not trace that shadow ray, and the
- * work counts below follow them.  Counting aid only; the oracle's own
- * shadow and render functions trace every shadow ray. */
-static bool light_vanishes(const rt_light& L, const rt_material& mat, v3 hp, v3 n) {
+ * finds: both terms shade_one adds for an unblocked light (the diffuse
+ * rgb * diffuse * cosL and the specular rgb * spec) are zero, as for a light
+ * behind the surface or a surface without diffuse colour and shininess.  The
+ * GPU's fused renders do not trace that shadow ray, and the work counts below
+ * follow them.  Counting aid only; the oracle's own shadow and render
+ * functions trace every shadow ray. */
+static bool light_vanishes(const rt_light& L, const rt_material& mat, v3 hp, v3 n, v3 d) {
     v3 Ld;
     float LD = 1.0f;
     if (L.type == RT_DIR_L) {
@@ -1202,10 +1204,17 @@ static bool light_vanishes(const rt_light& L, const rt_material& mat, v3 hp, v3 
         Ld = normalize(sub(hp, ld3(L.pos)));
     }
     const v3 rgb = muls(ld3(L.color), LD);
-    return clamp01(dot(n, neg(Ld))) == 0.0f && std::isfinite(rgb.x) && std::isfinite(rgb.y) &&
-           std::isfinite(rgb.z) && std::isfinite(mat.diffuse[0]) &&
-           std::isfinite(mat.diffuse[1]) && std::isfinite(mat.diffuse[2]) &&
-           std::isfinite(mat.shininess);
+    const v3 r = sub(d, muls(muls(n, 2.0f), dot(d, n)));
+    float cosL = clamp01(dot(n, neg(Ld)));
+    cosL = cosL * cosL;
+    float spec = clamp01(dot(r, neg(Ld)));
+    spec = spec * spec;
+    spec = spec * spec;
+    spec = spec * spec;
+    spec *= cosL * mat.shininess;
+    const v3 dt = muls(mul(rgb, ld3(mat.diffuse)), cosL), st = muls(rgb, spec);
+    return dt.x == 0.0f && dt.y == 0.0f && dt.z == 0.0f && st.x == 0.0f && st.y == 0.0f &&
+           st.z == 0.0f;
 }
 
 /* Traversal work of the closest-hit rays smp[0, n) and of the shadow rays
@@ -1229,7 +1238,7 @@ int orc_traversal_counts(const orc_scene* s, const rt_sample* smp, int32_t n, in
             const v3 hp = ld3(h.hit_point), hn = ld3(h.n);
             const rt_material& mat = s->mats[s->map[h.id]];
             for (int l = 0; l < s->lights.count; ++l) {
-                if (light_vanishes(s->lights.light[l], mat, hp, hn)) continue;
+                if (light_vanishes(s->lights.light[l], mat, hp, hn, r.dir)) continue;
                 light_occluded(s, s->lights.light[l], hp, &cs);
                 acc[5] += 1;
             }

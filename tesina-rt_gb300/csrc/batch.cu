@@ -478,8 +478,9 @@ __global__ void __launch_bounds__(THREADS, MINB) k_render_batch_pool(BatchRender
             const BvhHeader H = *V.scene.hdr;
             const f3 p = mk3(Q.hp[0][lo], Q.hp[1][lo], Q.hp[2][lo]);
             const f3 nk = mk3(Q.hn[0][lo], Q.hn[1][lo], Q.hn[2][lo]);
+            const f3 dk = mk3(Q.hd[0][lo], Q.hd[1][lo], Q.hd[2][lo]);
             if (!light_vanishes(V.lights->light[l], V.scene.mats[__ldg(&V.scene.map[Q.hid[lo]])], p,
-                                nk) &&
+                                nk, dk) &&
                 occluded<true>(V.scene, H, V.lights->light[l], p, A.status))
                 atomicOr(&Q.hmask[lo], 1u << l);
         }

@@ -352,8 +352,9 @@ __global__ void __launch_bounds__(128, MAXB == 6 ? 5 : RT_INST_MINB) k_render_in
             const int l = t / nh, k = t - l * nh;
             const f3 p = mk3(Q.hp[0][k], Q.hp[1][k], Q.hp[2][k]);
             const f3 nk = mk3(Q.hn[0][k], Q.hn[1][k], Q.hn[2][k]);
+            const f3 dk = mk3(Q.hd[0][k], Q.hd[1][k], Q.hd[2][k]);
             const SceneView& Sk = sA.roots[Q.hroot[k]].scene;
-            if (!light_vanishes(sA.lights.light[l], Sk.mats[__ldg(&Sk.map[Q.hid[k]])], p, nk) &&
+            if (!light_vanishes(sA.lights.light[l], Sk.mats[__ldg(&Sk.map[Q.hid[k]])], p, nk, dk) &&
                 occluded_multi(sA, sA.lights.light[l], p))
                 atomicOr(&Q.hmask[k], 1u << l);
         }

@@ -193,7 +193,8 @@ __global__ void __launch_bounds__(THREADS, MINB) k_render_pool(RenderArgs a) {
             const int l = t / nh, k = t - l * nh;
             const f3 p = mk3(Q.hp[0][k], Q.hp[1][k], Q.hp[2][k]);
             const f3 nk = mk3(Q.hn[0][k], Q.hn[1][k], Q.hn[2][k]);
-            if (!light_vanishes(sL.light[l], S.mats[__ldg(&S.map[Q.hid[k]])], p, nk) &&
+            const f3 dk = mk3(Q.hd[0][k], Q.hd[1][k], Q.hd[2][k]);
+            if (!light_vanishes(sL.light[l], S.mats[__ldg(&S.map[Q.hid[k]])], p, nk, dk) &&
                 occluded(S, H, sL.light[l], p, a.status))
                 atomicOr(&Q.hmask[k], 1u << l);
         }
@@ -368,7 +369,8 @@ __global__ void __launch_bounds__(THREADS, MINB) k_render_pool_refr(RenderArgs a
             const int l = t / nh, k = t - l * nh;
             const f3 p = mk3(Q.hp[0][k], Q.hp[1][k], Q.hp[2][k]);
             const f3 nk = mk3(Q.hn[0][k], Q.hn[1][k], Q.hn[2][k]);
-            if (!light_vanishes(sL.light[l], S.mats[__ldg(&S.map[Q.hid[k]])], p, nk) &&
+            const f3 dk = mk3(Q.hd[0][k], Q.hd[1][k], Q.hd[2][k]);
+            if (!light_vanishes(sL.light[l], S.mats[__ldg(&S.map[Q.hid[k]])], p, nk, dk) &&
                 occluded(S, H, sL.light[l], p, a.status))
                 atomicOr(&Q.hmask[k], 1u << l);
         }

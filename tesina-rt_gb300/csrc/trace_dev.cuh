@@ -392,23 +392,42 @@ __device__ __forceinline__ void light_at(const rt_light& L, f3 hp, f3& Ld, f3& r
     rgb = muls(rgb, LD);
 }
 
-// True when light L adds nothing to the hit's colour whether or not its
-// shadow ray is blocked: the light is behind the surface (cosL =
-// clamp(dot(n, -Ld), 0, 1) = 0, NaN included), which zeroes both the
-// diffuse term rgb * diffuse * cosL and the specular term
-// rgb * spec^8 * cosL * shininess as long as the light colour, the diffuse
-// colour and the shininess are finite.  Skipping that shadow ray leaves a
-// sum that differs at most in the sign of a zero, which floor(f * 1e6) to an
-// integer removes, so the image is the same.  Only the fused renders skip;
-// the stage-wise shadow pass reports every ray's result.
-__device__ __forceinline__ bool light_vanishes(const rt_light& L, const rt_material& mat, f3 hp,
-                                               f3 n) {
+// The two terms shade_sample adds for light L when its shadow ray is not
+// blocked (ray-shader.cl:312-330): diffuse rgb * diffuse * cosL and specular
+// rgb * spec, with cosL = clamp(dot(n, -Ld))^2 and spec = clamp(dot(r,
+// -Ld))^8 * cosL * shininess, r the incoming direction d reflected about n.
+__device__ __forceinline__ void light_terms(const rt_light& L, const rt_material& mat, f3 hp, f3 n,
+                                            f3 d, f3& dterm, f3& sterm) {
     f3 Ld, rgb;
     light_at(L, hp, Ld, rgb);
-    const float cosL = clamp01(dot(n, neg(Ld)));
-    return cosL == 0.0f && isfinite(rgb.x) && isfinite(rgb.y) && isfinite(rgb.z) &&
-           isfinite(mat.diffuse[0]) && isfinite(mat.diffuse[1]) && isfinite(mat.diffuse[2]) &&
-           isfinite(mat.shininess);
+    const f3 diffuse = mk3(mat.diffuse[0], mat.diffuse[1], mat.diffuse[2]);
+    const float dn = dot(d, n);
+    const f3 rr = sub(d, muls(muls(n, 2.0f), dn));
+    float cosL = clamp01(dot(n, neg(Ld)));
+    cosL = cosL * cosL;
+    float spec = clamp01(dot(rr, neg(Ld)));
+    spec = spec * spec;
+    spec = spec * spec;
+    spec = spec * spec;
+    spec *= cosL * mat.shininess;
+    dterm = muls(mul(rgb, diffuse), cosL);
+    sterm = muls(rgb, spec);
+}
+
+// True when light L adds nothing to the hit's colour whether or not its
+// shadow ray is blocked: both terms of light_terms are zero (a light behind
+// the surface, cosL = 0; a surface with no diffuse colour and no shininess,
+// as the mirrors here; a black light).  Adding a zero term changes the sum
+// at most in the sign of a zero, which floor(f * 1e6) to an integer
+// removes, so skipping the shadow ray gives the same image; a NaN or
+// infinite term is never skipped.  Only the fused renders skip; the
+// stage-wise shadow pass reports every ray's result.
+__device__ __forceinline__ bool light_vanishes(const rt_light& L, const rt_material& mat, f3 hp,
+                                               f3 n, f3 d) {
+    f3 dt, st;
+    light_terms(L, mat, hp, n, d, dt, st);
+    return dt.x == 0.0f && dt.y == 0.0f && dt.z == 0.0f && st.x == 0.0f && st.y == 0.0f &&
+           st.z == 0.0f;
 }
 
 // Local Whitted term of shade_sample, as the fixed-point increments that
@@ -418,21 +437,11 @@ __device__ __forceinline__ uint3 shade_hit(const rt_lights& Ls, const rt_materia
     const f3 diffuse = mk3(mat.diffuse[0], mat.diffuse[1], mat.diffuse[2]);
     f3 val = mul(mk3(Ls.ambient[0], Ls.ambient[1], Ls.ambient[2]), diffuse);
     for (int l = 0; l < Ls.count; ++l) {
-        const rt_light& L = Ls.light[l];
-        f3 Ld, rgb;
-        light_at(L, hp, Ld, rgb);
         if (!((shadow_mask >> l) & 1u)) {
-            const float dn = dot(d, n);
-            const f3 rr = sub(d, muls(muls(n, 2.0f), dn));
-            float cosL = clamp01(dot(n, neg(Ld)));
-            cosL = cosL * cosL;
-            float spec = clamp01(dot(rr, neg(Ld)));
-            spec = spec * spec;
-            spec = spec * spec;
-            spec = spec * spec;
-            spec *= cosL * mat.shininess;
-            val = add(val, muls(mul(rgb, diffuse), cosL));
-            val = add(val, muls(rgb, spec));
+            f3 dt, st;
+            light_terms(Ls.light[l], mat, hp, n, d, dt, st);
+            val = add(val, dt);
+            val = add(val, st);
         }
     }
     val = muls(val, 1.0f - mat.reflectiveness);
@@ -579,7 +588,7 @@ __device__ __forceinline__ PixelResult render_pixel(const SceneView& S, const Bv
             const rt_material mat = S.mats[__ldg(&S.map[hit.id])];
             uint32_t mask = 0;
             for (int l = 0; l < L.count; ++l)
-                if (!light_vanishes(L.light[l], mat, hi.hp, hi.n) &&
+                if (!light_vanishes(L.light[l], mat, hi.hp, hi.n, d) &&
                     occluded<WW>(S, H, L.light[l], hi.hp, status))
                     mask |= 1u << l;
             res.shadow += (uint32_t)L.count;
