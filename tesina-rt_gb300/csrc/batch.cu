@@ -361,6 +361,7 @@ struct WarpPoolB {
     int hid[32], hv[32], hai[32], hbounce[32], hoff[33];
     unsigned hmask[32];
     unsigned char hinv[32];
+    uint8_t task[32 * RT_MAX_LIGHTS];   // shadow tasks that need a ray
     int pool_n;
 };
 }  // namespace
@@ -464,24 +465,42 @@ __global__ void __launch_bounds__(THREADS, MINB) k_render_batch_pool(BatchRender
         if (hit_ok) Q.hoff[__popc(hm & lt)] = ex - nl;
         if (lane == 0) Q.hoff[nh] = ntask;
         __syncwarp();
-        for (int t = lane; t < ntask; t += 32) {
-            int lo = 0, hi2 = nh - 1;   // the hit whose tasks contain t
-            while (lo < hi2) {
-                const int mid = (lo + hi2 + 1) >> 1;
-                if (Q.hoff[mid] <= t)
-                    lo = mid;
-                else
-                    hi2 = mid - 1;
+        // the tasks whose light adds nothing are settled without a ray
+        // (light_vanishes); the others are listed densely (hit | light << 5)
+        // and traced 32 at a time
+        int nt = 0;
+        for (int t0 = 0; t0 < ntask; t0 += 32) {
+            const int t = t0 + lane;
+            bool nd = false;
+            int lo = 0, l = 0;
+            if (t < ntask) {
+                int hi2 = nh - 1;   // the hit whose tasks contain t
+                while (lo < hi2) {
+                    const int mid = (lo + hi2 + 1) >> 1;
+                    if (Q.hoff[mid] <= t)
+                        lo = mid;
+                    else
+                        hi2 = mid - 1;
+                }
+                l = t - Q.hoff[lo];
+                const BatchView& V = A.views[Q.hv[lo]];
+                nd = !light_vanishes(V.lights->light[l],
+                                     V.scene.mats[__ldg(&V.scene.map[Q.hid[lo]])],
+                                     mk3(Q.hp[0][lo], Q.hp[1][lo], Q.hp[2][lo]),
+                                     mk3(Q.hn[0][lo], Q.hn[1][lo], Q.hn[2][lo]),
+                                     mk3(Q.hd[0][lo], Q.hd[1][lo], Q.hd[2][lo]));
             }
-            const int l = t - Q.hoff[lo];
+            const unsigned bm = __ballot_sync(0xffffffffu, nd);
+            if (nd) Q.task[nt + __popc(bm & lt)] = (uint8_t)(lo | (l << 5));
+            nt += __popc(bm);
+        }
+        __syncwarp();
+        for (int i = lane; i < nt; i += 32) {
+            const int e = Q.task[i], lo = e & 31, l = e >> 5;
             const BatchView& V = A.views[Q.hv[lo]];
             const BvhHeader H = *V.scene.hdr;
             const f3 p = mk3(Q.hp[0][lo], Q.hp[1][lo], Q.hp[2][lo]);
-            const f3 nk = mk3(Q.hn[0][lo], Q.hn[1][lo], Q.hn[2][lo]);
-            const f3 dk = mk3(Q.hd[0][lo], Q.hd[1][lo], Q.hd[2][lo]);
-            if (!light_vanishes(V.lights->light[l], V.scene.mats[__ldg(&V.scene.map[Q.hid[lo]])], p,
-                                nk, dk) &&
-                occluded<true>(V.scene, H, V.lights->light[l], p, A.status))
+            if (occluded<true>(V.scene, H, V.lights->light[l], p, A.status))
                 atomicOr(&Q.hmask[lo], 1u << l);
         }
         __syncwarp();

@@ -262,6 +262,7 @@ struct InstPool {
     int hid[32], hroot[32], hpix[32], hbounce[32];
     unsigned hmask[32];
     unsigned char hinv[32];
+    uint8_t task[32 * RT_MAX_LIGHTS];   // shadow tasks that need a ray
     int pool_n;
 };
 }  // namespace
@@ -348,16 +349,19 @@ __global__ void __launch_bounds__(128, MAXB == 6 ? 5 : RT_INST_MINB) k_render_in
         }
         __syncwarp();
         const int nl = sA.lights.count;
-        for (int t = lane; t < nh * nl; t += 32) {   // light-major, as k_render_pool
-            const int l = t / nh, k = t - l * nh;
-            const f3 p = mk3(Q.hp[0][k], Q.hp[1][k], Q.hp[2][k]);
-            const f3 nk = mk3(Q.hn[0][k], Q.hn[1][k], Q.hn[2][k]);
-            const f3 dk = mk3(Q.hd[0][k], Q.hd[1][k], Q.hd[2][k]);
-            const SceneView& Sk = sA.roots[Q.hroot[k]].scene;
-            if (!light_vanishes(sA.lights.light[l], Sk.mats[__ldg(&Sk.map[Q.hid[k]])], p, nk, dk) &&
-                occluded_multi(sA, sA.lights.light[l], p))
-                atomicOr(&Q.hmask[k], 1u << l);
-        }
+        shadow_tasks(   // light-major, as k_render_pool
+            nh, nl, Q.task,
+            [&](int k, int l) {
+                const SceneView& Sk = sA.roots[Q.hroot[k]].scene;
+                return !light_vanishes(sA.lights.light[l], Sk.mats[__ldg(&Sk.map[Q.hid[k]])],
+                                       mk3(Q.hp[0][k], Q.hp[1][k], Q.hp[2][k]),
+                                       mk3(Q.hn[0][k], Q.hn[1][k], Q.hn[2][k]),
+                                       mk3(Q.hd[0][k], Q.hd[1][k], Q.hd[2][k]));
+            },
+            [&](int k, int l) {
+                if (occluded_multi(sA, sA.lights.light[l], mk3(Q.hp[0][k], Q.hp[1][k], Q.hp[2][k])))
+                    atomicOr(&Q.hmask[k], 1u << l);
+            });
         __syncwarp();
         bool push = false, push_t = false;
         f3 np = mk3(0.f, 0.f, 0.f), nd = np, td = np;

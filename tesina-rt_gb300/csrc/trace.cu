@@ -94,6 +94,7 @@ struct WarpPool {
     float hp[3][32], hn[3][32], hd[3][32], hc[32];   // hits of the current step
     int hid[32], hpix[32], hbounce[32];
     unsigned hmask[32];
+    uint8_t task[32 * RT_MAX_LIGHTS];   // shadow tasks that need a ray
     int pool_n;
 };
 }  // namespace
@@ -185,19 +186,23 @@ __global__ void __launch_bounds__(THREADS, MINB) k_render_pool(RenderArgs a) {
         __syncwarp();
         // 3. shadow rays of every hit and light, 32 at a time
         const int nl = sL.count;
-        // light-major: neighbouring lanes trace toward the same light from
-        // neighbouring hits (coherent paths: 3 % faster on the mid-scale
-        // frame with 2 lights, 10 % on the stress pose with 3, than a hit's
-        // lights on neighbouring lanes)
-        for (int t = lane; t < nh * nl; t += 32) {
-            const int l = t / nh, k = t - l * nh;
-            const f3 p = mk3(Q.hp[0][k], Q.hp[1][k], Q.hp[2][k]);
-            const f3 nk = mk3(Q.hn[0][k], Q.hn[1][k], Q.hn[2][k]);
-            const f3 dk = mk3(Q.hd[0][k], Q.hd[1][k], Q.hd[2][k]);
-            if (!light_vanishes(sL.light[l], S.mats[__ldg(&S.map[Q.hid[k]])], p, nk, dk) &&
-                occluded(S, H, sL.light[l], p, a.status))
-                atomicOr(&Q.hmask[k], 1u << l);
-        }
+        // light-major (shadow_tasks): neighbouring lanes trace toward the same
+        // light from neighbouring hits (coherent paths: 3 % faster on the
+        // mid-scale frame with 2 lights, 10 % on the stress pose with 3, than
+        // a hit's lights on neighbouring lanes); the tasks that need a ray
+        // are traced densely
+        shadow_tasks(
+            nh, nl, Q.task,
+            [&](int k, int l) {
+                return !light_vanishes(sL.light[l], S.mats[__ldg(&S.map[Q.hid[k]])],
+                                       mk3(Q.hp[0][k], Q.hp[1][k], Q.hp[2][k]),
+                                       mk3(Q.hn[0][k], Q.hn[1][k], Q.hn[2][k]),
+                                       mk3(Q.hd[0][k], Q.hd[1][k], Q.hd[2][k]));
+            },
+            [&](int k, int l) {
+                if (occluded(S, H, sL.light[l], mk3(Q.hp[0][k], Q.hp[1][k], Q.hp[2][k]), a.status))
+                    atomicOr(&Q.hmask[k], 1u << l);
+            });
         __syncwarp();
         // 4. shading; continuing paths put their reflection ray into the pool
         bool push = false;
@@ -276,6 +281,7 @@ struct RefrPool {
     int hid[32], hpix[32], hbounce[32];
     unsigned hmask[32];
     unsigned char hinv[32];
+    uint8_t task[32 * RT_MAX_LIGHTS];   // shadow tasks that need a ray
     int pool_n;
 };
 }  // namespace
@@ -365,15 +371,18 @@ __global__ void __launch_bounds__(THREADS, MINB) k_render_pool_refr(RenderArgs a
         }
         __syncwarp();
         const int nl = sL.count;
-        for (int t = lane; t < nh * nl; t += 32) {   // light-major, as k_render_pool
-            const int l = t / nh, k = t - l * nh;
-            const f3 p = mk3(Q.hp[0][k], Q.hp[1][k], Q.hp[2][k]);
-            const f3 nk = mk3(Q.hn[0][k], Q.hn[1][k], Q.hn[2][k]);
-            const f3 dk = mk3(Q.hd[0][k], Q.hd[1][k], Q.hd[2][k]);
-            if (!light_vanishes(sL.light[l], S.mats[__ldg(&S.map[Q.hid[k]])], p, nk, dk) &&
-                occluded(S, H, sL.light[l], p, a.status))
-                atomicOr(&Q.hmask[k], 1u << l);
-        }
+        shadow_tasks(
+            nh, nl, Q.task,
+            [&](int k, int l) {
+                return !light_vanishes(sL.light[l], S.mats[__ldg(&S.map[Q.hid[k]])],
+                                       mk3(Q.hp[0][k], Q.hp[1][k], Q.hp[2][k]),
+                                       mk3(Q.hn[0][k], Q.hn[1][k], Q.hn[2][k]),
+                                       mk3(Q.hd[0][k], Q.hd[1][k], Q.hd[2][k]));
+            },
+            [&](int k, int l) {
+                if (occluded(S, H, sL.light[l], mk3(Q.hp[0][k], Q.hp[1][k], Q.hp[2][k]), a.status))
+                    atomicOr(&Q.hmask[k], 1u << l);
+            });
         __syncwarp();
         // shading; the continuing rays of each hit: reflected, refracted
         bool push_r = false, push_t = false;

@@ -430,6 +430,43 @@ __device__ __forceinline__ bool light_vanishes(const rt_light& L, const rt_mater
            st.z == 0.0f;
 }
 
+// The shadow tasks of a warp's nh hits (nh <= 32) and nl lights (nl <=
+// RT_MAX_LIGHTS), in light-major order so that neighbouring lanes trace
+// toward one light from neighbouring hits.  need(k, l) settles a task
+// without a ray when it returns false (light_vanishes); the tasks that need
+// a ray are listed densely in `list` (hit | light << 5, 32 * RT_MAX_LIGHTS
+// bytes of the warp's shared memory) and trace(k, l) runs them 32 at a
+// time, so a round of the warp traces 32 rays whatever was settled (against
+// each lane taking the tasks of its own index: 1.5 % faster on the
+// mid-scale frame, 4 % on the stress pose, equal on the small soup).  All 32
+// lanes call it.
+static_assert(RT_MAX_LIGHTS <= 8, "task list entries hold the light in 3 bits");
+template <class Need, class Trace>
+__device__ __forceinline__ void shadow_tasks(int nh, int nl, uint8_t* list, Need need, Trace trace) {
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    const int ntask = nh * nl;
+    int nt = 0;
+    for (int t0 = 0; t0 < ntask; t0 += 32) {
+        const int t = t0 + lane;
+        bool nd = false;
+        int k = 0, l = 0;
+        if (t < ntask) {
+            l = t / nh;
+            k = t - l * nh;
+            nd = need(k, l);
+        }
+        const unsigned bm = __ballot_sync(0xffffffffu, nd);
+        if (nd) list[nt + __popc(bm & lt)] = (uint8_t)(k | (l << 5));
+        nt += __popc(bm);
+    }
+    __syncwarp();
+    for (int i = lane; i < nt; i += 32) {
+        const int e = list[i];
+        trace(e & 31, e >> 5);
+    }
+}
+
 // Local Whitted term of shade_sample, as the fixed-point increments that
 // to_color_int + image[pixel] += produce (ray-shader.cl:101-109, 312-330).
 __device__ __forceinline__ uint3 shade_hit(const rt_lights& Ls, const rt_material& mat, f3 hp, f3 n,
