@@ -518,9 +518,11 @@ __global__ void __launch_bounds__(THREADS, MINB) k_render_batch_pool(BatchRender
             const rt_material mat = V.scene.mats[__ldg(&V.scene.map[Q.hid[k]])];
             const uint3 col = shade_hit(*V.lights, mat, p, n, dk, ck, Q.hmask[k]);
             const int ak = Q.hai[k];
-            atomicAdd(&A.accum[3 * (size_t)ak], col.x);
-            atomicAdd(&A.accum[3 * (size_t)ak + 1], col.y);
-            atomicAdd(&A.accum[3 * (size_t)ak + 2], col.z);
+            if (col.x | col.y | col.z) {   // a zero colour adds nothing
+                atomicAdd(&A.accum[3 * (size_t)ak], col.x);
+                atomicAdd(&A.accum[3 * (size_t)ak + 1], col.y);
+                atomicAdd(&A.accum[3 * (size_t)ak + 2], col.z);
+            }
             ++n_hits;
             n_shadow += (uint32_t)V.lights->count;
             const int bk = Q.hbounce[k];

@@ -377,9 +377,11 @@ __global__ void __launch_bounds__(128, MAXB == 6 ? 5 : RT_INST_MINB) k_render_in
             const rt_material mat = S.mats[__ldg(&S.map[Q.hid[k]])];
             const uint3 col = shade_hit(sA.lights, mat, p, n, dk, ck, Q.hmask[k]);
             const int pk = Q.hpix[k];
-            atomicAdd(&sA.accum[3 * (size_t)pk], col.x);
-            atomicAdd(&sA.accum[3 * (size_t)pk + 1], col.y);
-            atomicAdd(&sA.accum[3 * (size_t)pk + 2], col.z);
+            if (col.x | col.y | col.z) {   // a zero colour adds nothing
+                atomicAdd(&sA.accum[3 * (size_t)pk], col.x);
+                atomicAdd(&sA.accum[3 * (size_t)pk + 1], col.y);
+                atomicAdd(&sA.accum[3 * (size_t)pk + 2], col.z);
+            }
             ++n_hits;
             n_shadow += (uint32_t)nl;
             const int bk = Q.hbounce[k];

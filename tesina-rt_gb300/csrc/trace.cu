@@ -218,9 +218,11 @@ __global__ void __launch_bounds__(THREADS, MINB) k_render_pool(RenderArgs a) {
             const rt_material mat = S.mats[__ldg(&S.map[Q.hid[k]])];
             const uint3 col = shade_hit(sL, mat, p, n, dk, ck, Q.hmask[k]);
             const int pk = Q.hpix[k];
-            atomicAdd(&a.accum[3 * (size_t)pk], col.x);
-            atomicAdd(&a.accum[3 * (size_t)pk + 1], col.y);
-            atomicAdd(&a.accum[3 * (size_t)pk + 2], col.z);
+            if (col.x | col.y | col.z) {   // a zero colour adds nothing
+                atomicAdd(&a.accum[3 * (size_t)pk], col.x);
+                atomicAdd(&a.accum[3 * (size_t)pk + 1], col.y);
+                atomicAdd(&a.accum[3 * (size_t)pk + 2], col.z);
+            }
             ++n_hits;
             n_shadow += (uint32_t)nl;
             const int bk = Q.hbounce[k];
@@ -398,9 +400,11 @@ __global__ void __launch_bounds__(THREADS, MINB) k_render_pool_refr(RenderArgs a
             const rt_material mat = S.mats[__ldg(&S.map[Q.hid[k]])];
             const uint3 col = shade_hit(sL, mat, p, n, dk, ck, Q.hmask[k]);
             const int pk = Q.hpix[k];
-            atomicAdd(&a.accum[3 * (size_t)pk], col.x);
-            atomicAdd(&a.accum[3 * (size_t)pk + 1], col.y);
-            atomicAdd(&a.accum[3 * (size_t)pk + 2], col.z);
+            if (col.x | col.y | col.z) {   // a zero colour adds nothing
+                atomicAdd(&a.accum[3 * (size_t)pk], col.x);
+                atomicAdd(&a.accum[3 * (size_t)pk + 1], col.y);
+                atomicAdd(&a.accum[3 * (size_t)pk + 2], col.z);
+            }
             ++n_hits;
             n_shadow += (uint32_t)nl;
             const int bk = Q.hbounce[k];
