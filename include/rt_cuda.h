@@ -513,7 +513,10 @@ RT_API int32_t rt_server_get_stats(rt_server* server, rt_server_stats* stats);
 RT_API int32_t rt_server_reset_stats(rt_server* server);
 
 /* End-to-end convenience: host vertices in, host image out, synchronous:
- * optional vertex update -> LBVH build -> render -> RGBA8 to host. */
+ * optional vertex update -> LBVH build -> render -> RGBA8 to host.  The
+ * normals, which only the render reads, are uploaded on a stream of the
+ * context's own beside the positions and the build; pinned host buffers make
+ * the copies asynchronous. */
 RT_API int32_t rt_render_host(rt_ctx* ctx, rt_scene* scene, const float* h_pos4, const float* h_nrm4,
                        uint32_t vertex_count, const rt_bvh_cfg* cfg, const rt_camera* cam,
                        int32_t width, int32_t height, int32_t max_bounces, uint8_t* h_rgba,

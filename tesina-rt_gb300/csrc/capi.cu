@@ -405,6 +405,13 @@ int32_t rt_shutdown(rt_ctx* c) {
             if (kv.second.first) cudaFree(kv.second.first);
     dfree(c->d_out);
     dfree(c->d_stats);
+    if (c->host_side) {
+        cudaStreamSynchronize(c->host_side);
+        cudaStreamDestroy(c->host_side);
+    }
+    if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+    if (c->ev_join) cudaEventDestroy(c->ev_join);
+    if (c->h_status) cudaFreeHost(c->h_status);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return RT_OK;
@@ -1207,12 +1214,32 @@ int32_t rt_render_host(rt_ctx* c, rt_scene* s, const float* pos4, const float* n
     if (!c || !s || !cam || !h_rgba) return fail(RT_ERR_INVALID, "rt_render_host: null argument");
     cudaStream_t cs = st(c, stream);
     int32_t r;
+    if (!c->host_side) {
+        CU(cudaStreamCreateWithFlags(&c->host_side, cudaStreamNonBlocking));
+        CU(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
+        CU(cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming));
+        CU(cudaMallocHost(&c->h_status, sizeof(uint32_t)));
+    }
+    const bool side_normals = pos4 && nrm4;
     if (pos4) {
-        r = rt_scene_update_vertices(c, s, pos4, nrm4, V, stream);
-        if (r) return r;
+        if (V != s->V) return fail(RT_ERR_INVALID, "vertex count %u != scene's %u", V, s->V);
+        CU(scene_write_begin(s, cs));
+        if (side_normals) {
+            // the build reads positions only: the normals go up beside it, on
+            // a stream that starts after everything queued on cs so far (the
+            // scene's earlier readers) and that the render waits for
+            CU(cudaEventRecord(c->ev_fork, cs));
+            CU(cudaStreamWaitEvent(c->host_side, c->ev_fork, 0));
+            CU(cudaMemcpyAsync(s->d_nrm, nrm4, 16 * (size_t)V, cudaMemcpyHostToDevice,
+                               c->host_side));
+            CU(cudaEventRecord(c->ev_join, c->host_side));
+        }
+        CU(cudaMemcpyAsync(s->d_pos, pos4, 16 * (size_t)V, cudaMemcpyHostToDevice, cs));
+        CU(scene_write_end(s, cs));
     }
     r = rt_bvh_build_lbvh(c, s, cfg, stream);
     if (r) return r;
+    if (side_normals) CU(cudaStreamWaitEvent(cs, c->ev_join, 0));
     const size_t bytes = 4 * (size_t)w * h;
     if (c->d_out_cap < bytes) {
         dfree(c->d_out);
@@ -1229,9 +1256,9 @@ int32_t rt_render_host(rt_ctx* c, rt_scene* s, const float* pos4, const float* n
     if (r) return r;
     CU(cudaMemcpyAsync(h_rgba, c->d_out, bytes, cudaMemcpyDeviceToHost, cs));
     if (h_stats) CU(cudaMemcpyAsync(h_stats, c->d_stats, sizeof(*h_stats), cudaMemcpyDeviceToHost, cs));
+    CU(cudaMemcpyAsync(c->h_status, c->d_status, sizeof(uint32_t), cudaMemcpyDeviceToHost, cs));
     CU(cudaStreamSynchronize(cs));
-    uint32_t bits = 0;
-    CU(cudaMemcpy(&bits, c->d_status, sizeof(bits), cudaMemcpyDeviceToHost));
+    const uint32_t bits = *c->h_status;
     if (bits & RT_DEV_TIMEOUT) return fail(RT_ERR_TIMEOUT, "rt_render_host: device wait timed out");
     if (bits & RT_DEV_OVERFLOW) return fail(RT_ERR_OVERFLOW, "rt_render_host: stack overflow");
     return RT_OK;

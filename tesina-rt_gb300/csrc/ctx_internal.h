@@ -31,6 +31,11 @@ struct rt_ctx {
     uint8_t* d_out = nullptr;            // rt_render_host image staging
     size_t d_out_cap = 0;
     rt_render_stats* d_stats = nullptr;  // rt_render_host counters
+    // rt_render_host: a stream for the normal upload beside the build, the
+    // events that fork and join it, and a pinned status word
+    cudaStream_t host_side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    uint32_t* h_status = nullptr;
     float inv1e6 = 1.0f / 1e6f;
     rt_render_config render_cfg = {4, 0, 32, 32};   // variant (128 threads, 8 blocks/SM)
     int variant_occupancy[rt::kMaxRenderVariants] = {0};   // resident blocks per SM per variant
