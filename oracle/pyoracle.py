@@ -67,6 +67,7 @@ class Oracle(_Lib):
                                   [P, P, I32, I32, I32, SZ, P, P, C.c_int])
         self.build_sah_raw = b(L, "orc_build_sah", C.c_int, [P])
         self.traversal_counts_raw = b(L, "orc_traversal_counts", C.c_int, [P, P, I32, C.c_int, P])
+        self.vanishing_raw = b(L, "orc_vanishing_lights", C.c_int, [P, P, P, I32, P])
         self.sah_nodes_raw = b(L, "orc_sah_nodes", C.c_int, [P, P, P, P, P, P, P, C.POINTER(U32)])
 
     def multi(self, scene_handles, inst_scene, tr, trinv, lights):
@@ -165,6 +166,13 @@ class OracleScene:
         return {"nodes": int(out[0]), "tris": int(out[1]), "shadow_nodes": int(out[2]),
                 "shadow_tris": int(out[3]), "shadow_rays": int(out[4]),
                 "shadow_traced": int(out[5])}
+
+    def vanishing_lights(self, samples, hits):
+        """Per hit, the bitmask of lights whose shadow ray the fused renders
+        skip (both terms the light would add are zero)."""
+        m = np.zeros(samples.shape[0], np.uint32)
+        self.o.vanishing_raw(self.h, _p(samples), _p(hits), samples.shape[0], _p(m))
+        return m
 
     def sort_arrays(self):
         n = self.n

@@ -1217,6 +1217,23 @@ static bool light_vanishes(const rt_light& L, const rt_material& mat, v3 hp, v3 
            st.z == 0.0f;
 }
 
+/* Per hit, the lights whose shadow ray the fused GPU renders skip
+ * (light_vanishes, bit l for light l; 0 for a miss): a test shades with
+ * those bits flipped and expects the same image. */
+int orc_vanishing_lights(const orc_scene* s, const rt_sample* smp, const rt_hit* hits, int32_t n,
+                         uint32_t* masks) {
+    for (int32_t i = 0; i < n; ++i) {
+        masks[i] = 0;
+        if (!hits[i].hit) continue;
+        const rt_material& mat = s->mats[s->map[hits[i].id]];
+        for (int l = 0; l < s->lights.count; ++l)
+            if (light_vanishes(s->lights.light[l], mat, ld3(hits[i].hit_point), ld3(hits[i].n),
+                               ld3(smp[i].ray.dir)))
+                masks[i] |= 1u << l;
+    }
+    return 0;
+}
+
 /* Traversal work of the closest-hit rays smp[0, n) and of the shadow rays
  * of their hits toward each light: out = {interior nodes entered, triangles
  * tested} of the closest-hit traversals, the same of the shadow ones over

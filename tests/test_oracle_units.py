@@ -185,3 +185,45 @@ def test_oracle_traversal_counts(orc):
     away = pyoracle.gen_primary(orc, scenes.camera((0.0, 50.0, 0.0), (100.0, 50.0, 0.0)), 8, 8)
     assert s.traversal_counts(away) == {"nodes": 0, "tris": 0, "shadow_nodes": 0,
                                         "shadow_tris": 0, "shadow_rays": 0, "shadow_traced": 0}
+
+
+@pytest.mark.parametrize("kind", ["soup", "terrain"])
+def test_skipped_shadow_rays_do_not_change_the_image(orc, kind):
+    """The fused renders do not trace the shadow ray of a light whose two
+    shading terms are zero (behind the surface, or a surface without diffuse
+    colour and shininess).  On the oracle: flipping exactly those shadow
+    bits, for every hit, gives the same fixed-point image; and the rule
+    applies often enough to matter (back faces and the soup's mirrors)."""
+    from helpers import tiny_terrain
+    if kind == "soup":
+        sc = scenes.soup(6000, seed=12)
+        sc.lights = abi.make_lights((0.1,) * 3, [
+            dict(type=abi.RT_POINT_L, pos=(0.0, 4.0, -2.0)),
+            dict(type=abi.RT_DIR_L, dir=(0.3, -0.9, 0.3)),
+            dict(type=abi.RT_SPOT_L, pos=(2.0, 3.0, -3.0), dir=(-0.4, -0.6, 0.6), angle=0.5)])
+        cam = scenes.camera((0.0, 0.0, -4.0), (0.0, 0.0, 0.0))
+    else:
+        sc = tiny_terrain(64, 32, 6).scene(2)
+        cam = scenes.camera((0.0, 4.0, -10.0), (0.0, 0.0, 0.0))
+    s = orc.new_scene(sc)
+    s.build(30, 1, 0)
+    smp = pyoracle.gen_primary(orc, cam, 160, 160)
+    hits = s.trace(smp)
+    s.shadow(smp, hits)
+    vm = s.vanishing_lights(smp, hits)
+    assert int((vm != 0).sum()) > 200
+    img = np.zeros((160 * 160, 3), np.uint32)
+    s.shade(smp, hits, img)
+    flipped = hits.copy()
+    flipped["shadow_hit"] = (flipped["shadow_hit"].astype(np.uint32) ^ vm).astype(
+        flipped["shadow_hit"].dtype)
+    img2 = np.zeros_like(img)
+    s.shade(smp, flipped, img2)
+    assert np.array_equal(img, img2)
+    # control: flipping every light's bit does change the image
+    every = hits.copy()
+    every["shadow_hit"] = (every["shadow_hit"].astype(np.uint32) ^
+                           np.uint32((1 << sc.lights.count) - 1)).astype(every["shadow_hit"].dtype)
+    img3 = np.zeros_like(img)
+    s.shade(smp, every, img3)
+    assert not np.array_equal(img, img3)
