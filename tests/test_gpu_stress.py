@@ -37,13 +37,14 @@ def test_stress_tree(stress):
     assert int((gc["end"] - gc["start"])[leaf].max()) > 3     # equal-key leaves
 
 
-def test_stress_pose_full_frame(ctx, orc, stress):
-    """One pose rendered in full (8,294,400 primary samples, up to 6 bounces,
-    3 lights): the fixed-point image, the RGBA8 frame and the four ray
-    counters equal the oracle's."""
+@pytest.mark.parametrize("pose", [0, 3])
+def test_stress_pose_full_frame(ctx, orc, stress, pose):
+    """A pose rendered in full (8,294,400 primary samples, up to 6 bounces,
+    3 lights; pose 3 has the most reflection rays of the 8): the fixed-point
+    image, the RGBA8 frame and the four ray counters equal the oracle's."""
     wl, sc, g, o = stress
     w, h, b = wl["width"], wl["height"], wl["max_bounces"]
-    cam = wl["cameras"][0]
+    cam = wl["cameras"][pose]
     n = w * h
     rgba_d, img_d = ctx.alloc(4 * n), ctx.alloc(12 * n)
     st_d = ctx.alloc(32)
