@@ -31,9 +31,39 @@
 
 namespace rt {
 
+// Programmatic dependent launch.  The build's kernels after the first are
+// launched while their predecessor still runs (launch_dep); each waits at
+// its start for the predecessor grid to finish and its writes to be visible
+// (griddepcontrol.wait, which returns at once for a kernel launched without
+// the dependency), then lets its own successor launch.  It hides the
+// launches' latency: the mid-scale build took 0.2752-0.2772 ms against
+// 0.2802 ms without it, the 17.7 M-triangle build 2.584-2.589 against
+// 2.604-2.605 ms (three alternating runs each, one box).
+__device__ __forceinline__ void pdl_enter() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+template <typename... KArgs, typename... Args>
+static cudaError_t launch_dep(void (*kern)(KArgs...), unsigned grid, unsigned block, size_t smem,
+                              cudaStream_t s, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kern, args...);
+}
+
 __global__ void __launch_bounds__(256) k_bounds(const float4* __restrict__ pos,
                                                 const uint32_t* __restrict__ idx, uint32_t n,
                                                 uint32_t* __restrict__ bounds) {
+    pdl_enter();
     float lo[3] = {1e37f, 1e37f, 1e37f}, hi[3] = {-1e37f, -1e37f, -1e37f};
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         float tl[3], th[3];
@@ -77,6 +107,7 @@ __global__ void __launch_bounds__(256) k_morton_hist(const float4* __restrict__ 
                                                      int passes, uint32_t* __restrict__ keys,
                                                      uint32_t* __restrict__ vals,
                                                      uint32_t* __restrict__ hist) {
+    pdl_enter();
     __shared__ uint32_t sh[4][256];
     for (int i = threadIdx.x; i < 4 * 256; i += blockDim.x) (&sh[0][0])[i] = 0;
     __syncthreads();
@@ -118,6 +149,7 @@ __global__ void __launch_bounds__(SORT_THREADS, 3) k_onesweep(
     const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin, uint32_t* __restrict__ kout,
     uint32_t* __restrict__ vout, uint32_t n, int shift, const uint32_t* __restrict__ hist,
     uint32_t* __restrict__ lookback, uint32_t* __restrict__ tile_ctr, uint32_t* __restrict__ status) {
+    pdl_enter();
     __shared__ SortSmem S;
     if (threadIdx.x == 0) S.tile = atomicAdd(tile_ctr, 1u);   // tiles in launch order
     __syncthreads();
@@ -142,6 +174,7 @@ __global__ void __launch_bounds__(256) k_permute(
     const uint32_t* __restrict__ map_old, const uint32_t* __restrict__ orig_old,
     const float4* __restrict__ pos, uint32_t* __restrict__ idx_new, uint32_t* __restrict__ map_new,
     uint32_t* __restrict__ orig_new, float4* __restrict__ tris, float4* __restrict__ leafbox) {
+    pdl_enter();
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
         permute_one(i, vals, idx_old, map_old, orig_old, pos, idx_new, map_new, orig_new, tris,
                     leafbox);
@@ -176,6 +209,7 @@ __global__ void __launch_bounds__(C, C == EMIT_C0 ? RT_EMIT_MINB0 : 1) k_emit_le
     const EmitItem* __restrict__ in, const uint32_t* __restrict__ in_count, uint32_t n_in,
     EmitItem* __restrict__ out, uint32_t* __restrict__ out_count, float4* __restrict__ nodes,
     int min_leaf, uint32_t leave, BvhHeader* __restrict__ hdr, uint32_t* __restrict__ status) {
+    pdl_enter();
     extern __shared__ __align__(16) unsigned char emit_smem[];
     auto& S = *reinterpret_cast<EmitSmem<C>*>(emit_smem);
     emit_level<C>(S, blockIdx.x, n, skeys, leafbox, in, in_count, n_in, out, out_count, nodes,
@@ -216,16 +250,22 @@ static cudaError_t launch_emit(const LbvhArgs& a, uint8_t* emit_scratch, cudaStr
     }
     const uint32_t nb0 = emit_blocks0(n);
     const EmitBuffers B = emit_buffers(n, emit_scratch);
-    k_emit_level<EMIT_C0><<<nb0, EMIT_C0, sizeof(EmitSmem<EMIT_C0>), s>>>(
-        n, a.keys_sorted, a.leafbox, nullptr, nullptr, 0, B.items[0], B.counts[0], a.nodes,
-        a.min_leaf, emit_leave(0, nb0), a.hdr, a.status);
+    cudaError_t e = launch_dep(k_emit_level<EMIT_C0>, nb0, EMIT_C0, sizeof(EmitSmem<EMIT_C0>), s, n,
+                               (const uint32_t*)a.keys_sorted, (const float4*)a.leafbox,
+                               (const EmitItem*)nullptr, (const uint32_t*)nullptr, 0u, B.items[0],
+                               B.counts[0], a.nodes, a.min_leaf, emit_leave(0, nb0), a.hdr,
+                               a.status);
+    if (e) return e;
     uint32_t n_in = nb0;
     int src = 0;
     while (n_in > 1) {
         const uint32_t g = emit_next_level(n_in);
-        k_emit_level<EMIT_C1><<<g, EMIT_C1, sizeof(EmitSmem<EMIT_C1>), s>>>(
-            n, a.keys_sorted, a.leafbox, B.items[src], B.counts[src], n_in, B.items[src ^ 1],
-            B.counts[src ^ 1], a.nodes, a.min_leaf, emit_leave(1, g), a.hdr, a.status);
+        e = launch_dep(k_emit_level<EMIT_C1>, g, EMIT_C1, sizeof(EmitSmem<EMIT_C1>), s, n,
+                       (const uint32_t*)a.keys_sorted, (const float4*)a.leafbox,
+                       (const EmitItem*)B.items[src], (const uint32_t*)B.counts[src], n_in,
+                       B.items[src ^ 1], B.counts[src ^ 1], a.nodes, a.min_leaf, emit_leave(1, g),
+                       a.hdr, a.status);
+        if (e) return e;
         n_in = g;
         src ^= 1;
     }
@@ -266,8 +306,9 @@ cudaError_t lbvh_build(const LbvhArgs& a, cudaStream_t s) {
     if (e) return e;
     const int sms = a.num_sms;
     k_bounds<<<grid_for(n, 256, sms * 8), 256, 0, s>>>(a.pos, a.idx_in, n, bounds);
-    k_morton_hist<<<grid_for(n, 256, sms * 8), 256, 0, s>>>(a.pos, a.idx_in, n, bounds, a.depth,
-                                                            passes, a.keys_unsorted, a.vals0, hist);
+    e = launch_dep(k_morton_hist, grid_for(n, 256, sms * 8), 256, 0, s, a.pos, a.idx_in, n,
+                   bounds, a.depth, passes, a.keys_unsorted, a.vals0, hist);
+    if (e) return e;
     const uint32_t* kin = a.keys_unsorted;
     const uint32_t* vin = a.vals0;
     uint32_t* kbuf[2] = {a.keys1, a.keys_sorted};
@@ -275,15 +316,16 @@ cudaError_t lbvh_build(const LbvhArgs& a, cudaStream_t s) {
     for (int p = 0; p < passes; ++p) {
         // the last pass always lands in keys_sorted / vals_sorted
         const int dst = ((passes - 1 - p) & 1) ? 0 : 1;
-        k_onesweep<<<(unsigned)tiles, SORT_THREADS, 0, s>>>(kin, vin, kbuf[dst], vbuf[dst], n, 8 * p,
-                                                          hist + 256 * p, lookback + (size_t)p * tiles * 256,
-                                                          tile_ctr + p, a.status);
+        e = launch_dep(k_onesweep, (unsigned)tiles, SORT_THREADS, 0, s, kin, vin, kbuf[dst],
+                       vbuf[dst], n, 8 * p, hist + 256 * p, lookback + (size_t)p * tiles * 256,
+                       tile_ctr + p, a.status);
+        if (e) return e;
         kin = kbuf[dst];
         vin = vbuf[dst];
     }
-    k_permute<<<grid_for(n, 256, sms * 16), 256, 0, s>>>(n, a.vals_sorted, a.idx_in, a.map_in,
-                                                         a.orig_in, a.pos, a.idx_out, a.map_out,
-                                                         a.orig_out, a.tris, a.leafbox);
+    e = launch_dep(k_permute, grid_for(n, 256, sms * 16), 256, 0, s, n, a.vals_sorted, a.idx_in,
+                   a.map_in, a.orig_in, a.pos, a.idx_out, a.map_out, a.orig_out, a.tris, a.leafbox);
+    if (e) return e;
     return launch_emit(a, reinterpret_cast<uint8_t*>(a.scratch) + lbvh_emit_offset(n), s);
 }
 
