@@ -37,7 +37,9 @@ struct rt_ctx {
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     uint32_t* h_status = nullptr;
     float inv1e6 = 1.0f / 1e6f;
-    rt_render_config render_cfg = {4, 0, 32, 32};   // variant (128 threads, 8 blocks/SM)
+    // until the autotuner or the caller picks one: the pooled kernel
+    // (variant 8, k_render_pool<128, 6>) at full residency
+    rt_render_config render_cfg = {8, 0, 32, 32};
     int variant_occupancy[rt::kMaxRenderVariants] = {0};   // resident blocks per SM per variant
     int variant_carveout[rt::kMaxRenderVariants];          // shared-memory carveout set (%), -1 unset
     int smem_per_sm = 0;                            // bytes of shared memory an SM offers
