@@ -39,7 +39,12 @@ B_RAY_CLOSEST, B_RAY_SHADOW, B_SHADE = 40, 25, 48
 # dram__bytes_read.sum + dram__bytes_write.sum of one launch of a render
 # kernel on the mid-scale frame (ncu, --clock-control none), by kernel; the
 # line's roofline carries it only when the autotuner installed that kernel.
-RENDER_DRAM_BYTES = {"k_render_pool<128, 6>": (297.9 + 32.7) * 1e6}
+RENDER_DRAM_BYTES = {
+    "k_render_pool<128, 6>": (297.9 + 32.7) * 1e6,
+    "k_render_pool<128, 8>": (320.0 + 37.3) * 1e6,
+    "k_render_pool<256, 3>": (286.5 + 28.8) * 1e6,
+    "k_render_pool<256, 4>": (318.8 + 37.1) * 1e6,
+}
 
 
 def log(*a):
