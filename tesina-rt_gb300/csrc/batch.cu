@@ -243,8 +243,9 @@ __global__ void __launch_bounds__(SORT_THREADS, 4) k_batch_build(BatchBuildArgs 
     for (uint32_t g = blockIdx.x * blockDim.x + tid; g < total; g += nblk * blockDim.x) {
         const int s = find_segment(s_toff, nsc, g);
         const BatchScene& B = A.scenes[s];
-        permute_one(g - s_toff[s], B.vals_sorted, B.idx_in, B.map_in, B.orig_in, B.pos, B.idx_out,
-                    B.map_out, B.orig_out, B.tris, B.leafbox);
+        const PermuteIO P{B.vals_sorted, B.idx_in, B.map_in,  B.orig_in, B.pos,
+                          B.idx_out,     B.map_out, B.orig_out, B.tris};
+        permute_one(g - s_toff[s], P, B.leafbox);
     }
     grid.sync();
     stamp(A, 5);

@@ -29,6 +29,12 @@
 #include "lbvh_dev.cuh"
 #include "rt_internal.cuh"
 
+// The full build's level-0 emit performs the permutation itself (1), or a
+// separate k_permute stores the leaf AABBs for it (0).
+#ifndef RT_EMIT_PERMUTE
+#define RT_EMIT_PERMUTE 1
+#endif
+
 namespace rt {
 
 // Programmatic dependent launch.  The build's kernels after the first are
@@ -169,15 +175,11 @@ __global__ void __launch_bounds__(SORT_THREADS, 1) k_onesweep_wait_probe(
                                                status);
 }
 
-__global__ void __launch_bounds__(256) k_permute(
-    uint32_t n, const uint32_t* __restrict__ vals, const uint32_t* __restrict__ idx_old,
-    const uint32_t* __restrict__ map_old, const uint32_t* __restrict__ orig_old,
-    const float4* __restrict__ pos, uint32_t* __restrict__ idx_new, uint32_t* __restrict__ map_new,
-    uint32_t* __restrict__ orig_new, float4* __restrict__ tris, float4* __restrict__ leafbox) {
+__global__ void __launch_bounds__(256) k_permute(uint32_t n, PermuteIO P,
+                                                  float4* __restrict__ leafbox) {
     pdl_enter();
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        permute_one(i, vals, idx_old, map_old, orig_old, pos, idx_new, map_new, orig_new, tris,
-                    leafbox);
+        permute_one(i, P, leafbox);
 }
 
 // Per-triangle AABBs of the current vertex positions in the existing sorted
@@ -216,6 +218,19 @@ __global__ void __launch_bounds__(C, C == EMIT_C0 ? RT_EMIT_MINB0 : 1) k_emit_le
                   min_leaf, leave, hdr, status);
 }
 
+// Level 0 of a full build: each block first permutes its own triangles
+// (index buffer, material map, upload ids, triangle records) and joins them
+// with their boxes still in registers, so no leaf AABB goes through memory.
+__global__ void __launch_bounds__(EMIT_C0, RT_EMIT_MINB0) k_emit_level0_permute(
+    uint32_t n, const uint32_t* __restrict__ skeys, PermuteIO P, EmitItem* __restrict__ out,
+    uint32_t* __restrict__ out_count, float4* __restrict__ nodes, int min_leaf, uint32_t leave,
+    BvhHeader* __restrict__ hdr, uint32_t* __restrict__ status) {
+    pdl_enter();
+    extern __shared__ __align__(16) unsigned char emit_smem[];
+    auto& S = *reinterpret_cast<EmitSmem<EMIT_C0>*>(emit_smem);
+    emit_level<EMIT_C0, true>(S, blockIdx.x, n, skeys, nullptr, nullptr, nullptr, 0, out,
+                              out_count, nodes, min_leaf, leave, hdr, status, P);
+}
 
 static size_t sort_scratch_bytes(uint32_t n, int passes) {
     const size_t tiles = ((size_t)n + SORT_TILE - 1) / SORT_TILE;
@@ -226,8 +241,11 @@ static size_t emit_scratch_bytes(uint32_t n) { return emit_buffers_bytes(n); }
 
 // The emit's levels: level 0 over triangles, then levels over the items left
 // by EMIT_GROUP blocks each until a single block reaches the root.  Item
-// buffers alternate: A holds level 0, 2, ... and B level 1, 3, ....
-static cudaError_t launch_emit(const LbvhArgs& a, uint8_t* emit_scratch, cudaStream_t s) {
+// buffers alternate: A holds level 0, 2, ... and B level 1, 3, ....  With
+// `perm`, level 0 also performs the permutation (k_emit_level0_permute);
+// without, it reads the leaf AABBs a previous launch stored.
+static cudaError_t launch_emit(const LbvhArgs& a, uint8_t* emit_scratch, cudaStream_t s,
+                               const PermuteIO* perm = nullptr) {
     const uint32_t n = a.n;
     {
         // the shared-memory opt-in is a property of the kernel on each device
@@ -241,6 +259,10 @@ static cudaError_t launch_emit(const LbvhArgs& a, uint8_t* emit_scratch, cudaStr
             e = cudaFuncSetAttribute(k_emit_level<EMIT_C0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)sizeof(EmitSmem<EMIT_C0>));
             if (e == cudaSuccess)
+                e = cudaFuncSetAttribute(k_emit_level0_permute,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)sizeof(EmitSmem<EMIT_C0>));
+            if (e == cudaSuccess)
                 e = cudaFuncSetAttribute(k_emit_level<EMIT_C1>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)sizeof(EmitSmem<EMIT_C1>));
@@ -250,11 +272,14 @@ static cudaError_t launch_emit(const LbvhArgs& a, uint8_t* emit_scratch, cudaStr
     }
     const uint32_t nb0 = emit_blocks0(n);
     const EmitBuffers B = emit_buffers(n, emit_scratch);
-    cudaError_t e = launch_dep(k_emit_level<EMIT_C0>, nb0, EMIT_C0, sizeof(EmitSmem<EMIT_C0>), s, n,
-                               (const uint32_t*)a.keys_sorted, (const float4*)a.leafbox,
-                               (const EmitItem*)nullptr, (const uint32_t*)nullptr, 0u, B.items[0],
-                               B.counts[0], a.nodes, a.min_leaf, emit_leave(0, nb0), a.hdr,
-                               a.status);
+    cudaError_t e =
+        perm ? launch_dep(k_emit_level0_permute, nb0, EMIT_C0, sizeof(EmitSmem<EMIT_C0>), s, n,
+                          (const uint32_t*)a.keys_sorted, *perm, B.items[0], B.counts[0], a.nodes,
+                          a.min_leaf, emit_leave(0, nb0), a.hdr, a.status)
+             : launch_dep(k_emit_level<EMIT_C0>, nb0, EMIT_C0, sizeof(EmitSmem<EMIT_C0>), s, n,
+                          (const uint32_t*)a.keys_sorted, (const float4*)a.leafbox,
+                          (const EmitItem*)nullptr, (const uint32_t*)nullptr, 0u, B.items[0],
+                          B.counts[0], a.nodes, a.min_leaf, emit_leave(0, nb0), a.hdr, a.status);
     if (e) return e;
     uint32_t n_in = nb0;
     int src = 0;
@@ -323,10 +348,15 @@ cudaError_t lbvh_build(const LbvhArgs& a, cudaStream_t s) {
         kin = kbuf[dst];
         vin = vbuf[dst];
     }
-    e = launch_dep(k_permute, grid_for(n, 256, sms * 16), 256, 0, s, n, a.vals_sorted, a.idx_in,
-                   a.map_in, a.orig_in, a.pos, a.idx_out, a.map_out, a.orig_out, a.tris, a.leafbox);
+    const PermuteIO P{a.vals_sorted, a.idx_in,  a.map_in,   a.orig_in, a.pos,
+                      a.idx_out,     a.map_out, a.orig_out, a.tris};
+#if RT_EMIT_PERMUTE
+    return launch_emit(a, reinterpret_cast<uint8_t*>(a.scratch) + lbvh_emit_offset(n), s, &P);
+#else
+    e = launch_dep(k_permute, grid_for(n, 256, sms * 16), 256, 0, s, n, P, a.leafbox);
     if (e) return e;
     return launch_emit(a, reinterpret_cast<uint8_t*>(a.scratch) + lbvh_emit_offset(n), s);
+#endif
 }
 
 size_t radix_scratch_words(uint32_t n, int passes) {
@@ -384,10 +414,9 @@ cudaError_t radix_sort_pairs(const uint32_t* kin, const uint32_t* vin, uint32_t*
 }
 
 cudaError_t lbvh_permute(const LbvhArgs& a, const uint32_t* order, cudaStream_t s) {
-    k_permute<<<grid_for(a.n, 256, a.num_sms * 16), 256, 0, s>>>(a.n, order, a.idx_in, a.map_in,
-                                                                 a.orig_in, a.pos, a.idx_out,
-                                                                 a.map_out, a.orig_out, a.tris,
-                                                                 a.leafbox);
+    const PermuteIO P{order,     a.idx_in,  a.map_in,   a.orig_in, a.pos,
+                      a.idx_out, a.map_out, a.orig_out, a.tris};
+    k_permute<<<grid_for(a.n, 256, a.num_sms * 16), 256, 0, s>>>(a.n, P, a.leafbox);
     return cudaGetLastError();
 }
 

@@ -310,30 +310,33 @@ __device__ __forceinline__ void onesweep_tile(SortSmemT<ITEMS>& S, uint32_t tile
 }
 
 // rearrange_indices / rearrange_map (bvh-builder.cl:49-72) of sorted slot i,
-// plus the traversal's triangle record and the leaf AABB.
-__device__ __forceinline__ void permute_one(uint32_t i, const uint32_t* __restrict__ vals,
-                                            const uint32_t* __restrict__ idx_old,
-                                            const uint32_t* __restrict__ map_old,
-                                            const uint32_t* __restrict__ orig_old,
-                                            const float4* __restrict__ pos,
-                                            uint32_t* __restrict__ idx_new,
-                                            uint32_t* __restrict__ map_new,
-                                            uint32_t* __restrict__ orig_new,
-                                            float4* __restrict__ tris,
-                                            float4* __restrict__ leafbox) {
-    const uint32_t o = __ldg(&vals[i]);
-    const uint32_t a = __ldg(&idx_old[3 * (size_t)o]), b = __ldg(&idx_old[3 * (size_t)o + 1]),
-                   c = __ldg(&idx_old[3 * (size_t)o + 2]);
-    idx_new[3 * (size_t)i] = a;
-    idx_new[3 * (size_t)i + 1] = b;
-    idx_new[3 * (size_t)i + 2] = c;
-    map_new[i] = __ldg(&map_old[o]);
-    orig_new[i] = __ldg(&orig_old[o]);
-    const float4 p0 = __ldg(&pos[a]), p1 = __ldg(&pos[b]), p2 = __ldg(&pos[c]);
-    tris[3 * (size_t)i] = make_float4(p0.x, p0.y, p0.z, 0.f);
-    tris[3 * (size_t)i + 1] = make_float4(p1.x - p0.x, p1.y - p0.y, p1.z - p0.z, 0.f);
-    tris[3 * (size_t)i + 2] = make_float4(p2.x - p0.x, p2.y - p0.y, p2.z - p0.z, 0.f);
-    float4 lo, hi;
+// plus the traversal's triangle record; returns the triangle's AABB
+// (build_leaf_bbox's min / max of the three vertices).
+struct PermuteIO {
+    const uint32_t* vals;       // sorted slot -> triangle in the order before the build
+    const uint32_t* idx_old;
+    const uint32_t* map_old;
+    const uint32_t* orig_old;
+    const float4* pos;
+    uint32_t* idx_new;
+    uint32_t* map_new;
+    uint32_t* orig_new;
+    float4* tris;
+};
+
+__device__ __forceinline__ void permute_tri(uint32_t i, const PermuteIO& P, float4& lo, float4& hi) {
+    const uint32_t o = __ldg(&P.vals[i]);
+    const uint32_t a = __ldg(&P.idx_old[3 * (size_t)o]), b = __ldg(&P.idx_old[3 * (size_t)o + 1]),
+                   c = __ldg(&P.idx_old[3 * (size_t)o + 2]);
+    P.idx_new[3 * (size_t)i] = a;
+    P.idx_new[3 * (size_t)i + 1] = b;
+    P.idx_new[3 * (size_t)i + 2] = c;
+    P.map_new[i] = __ldg(&P.map_old[o]);
+    P.orig_new[i] = __ldg(&P.orig_old[o]);
+    const float4 p0 = __ldg(&P.pos[a]), p1 = __ldg(&P.pos[b]), p2 = __ldg(&P.pos[c]);
+    P.tris[3 * (size_t)i] = make_float4(p0.x, p0.y, p0.z, 0.f);
+    P.tris[3 * (size_t)i + 1] = make_float4(p1.x - p0.x, p1.y - p0.y, p1.z - p0.z, 0.f);
+    P.tris[3 * (size_t)i + 2] = make_float4(p2.x - p0.x, p2.y - p0.y, p2.z - p0.z, 0.f);
     hi.x = fmaxf(fmaxf(p0.x, p1.x), p2.x);
     hi.y = fmaxf(fmaxf(p0.y, p1.y), p2.y);
     hi.z = fmaxf(fmaxf(p0.z, p1.z), p2.z);
@@ -341,6 +344,14 @@ __device__ __forceinline__ void permute_one(uint32_t i, const uint32_t* __restri
     lo.y = fminf(fminf(p0.y, p1.y), p2.y);
     lo.z = fminf(fminf(p0.z, p1.z), p2.z);
     lo.w = hi.w = 0.f;
+}
+
+// permute_tri with the leaf AABB stored for a later emit (the many-scene
+// build and any caller of k_permute).
+__device__ __forceinline__ void permute_one(uint32_t i, const PermuteIO& P,
+                                            float4* __restrict__ leafbox) {
+    float4 lo, hi;
+    permute_tri(i, P, lo, hi);
     leafbox[2 * (size_t)i] = lo;
     leafbox[2 * (size_t)i + 1] = hi;
 }
@@ -750,7 +761,11 @@ __device__ __forceinline__ uint32_t gather_runs(EmitSmem<C>& S, const WarpItem& 
 // out[blk * EMIT_FMAX] and their number in out_count[blk].  The block stops
 // joining once `leave` runs or fewer are left (leave <= EMIT_FMAX; 32: join
 // down to one warp's runs, as the root's level must).
-template <int C>
+//
+// With PERMUTE, level 0 performs the permutation of its own triangles
+// (permute_tri with `perm`) and keeps their boxes in registers; `leafbox` is
+// then unused.
+template <int C, bool PERMUTE = false>
 __device__ __forceinline__ void emit_level(EmitSmem<C>& S, uint32_t blk, uint32_t n,
                                            const uint32_t* __restrict__ skeys,
                                            const float4* __restrict__ leafbox,
@@ -760,7 +775,8 @@ __device__ __forceinline__ void emit_level(EmitSmem<C>& S, uint32_t blk, uint32_
                                            uint32_t* __restrict__ out_count,
                                            float4* __restrict__ nodes, int min_leaf,
                                            uint32_t leave, BvhHeader* __restrict__ hdr,
-                                           uint32_t* __restrict__ status) {
+                                           uint32_t* __restrict__ status,
+                                           const PermuteIO& perm = PermuteIO{}) {
     static_assert(C % 32 == 0 && C >= EMIT_FMAX, "block size");
     const uint32_t t = threadIdx.x, lane = t & 31u, w = t >> 5;
     WarpItem it;
@@ -781,8 +797,12 @@ __device__ __forceinline__ void emit_level(EmitSmem<C>& S, uint32_t blk, uint32_
                                   : (((uint64_t)(kprev ^ k) << 32) | (uint64_t)((i - 1) ^ i));
         float4 lo = make_float4(0.f, 0.f, 0.f, 0.f), hi = lo;
         if (have) {
-            lo = leafbox[2 * (size_t)i];
-            hi = leafbox[2 * (size_t)i + 1];
+            if constexpr (PERMUTE) {
+                permute_tri(i, perm, lo, hi);
+            } else {
+                lo = leafbox[2 * (size_t)i];
+                hi = leafbox[2 * (size_t)i + 1];
+            }
         }
         it.lox = lo.x; it.loy = lo.y; it.loz = lo.z;
         it.hix = hi.x; it.hiy = hi.y; it.hiz = hi.z;
