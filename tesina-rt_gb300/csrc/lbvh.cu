@@ -34,6 +34,12 @@
 #ifndef RT_EMIT_PERMUTE
 #define RT_EMIT_PERMUTE 1
 #endif
+// The first radix pass makes the values 0..n-1 itself (1) instead of reading
+// them from a buffer k_morton_hist fills (0).
+#ifndef RT_SORT_IOTA
+#define RT_SORT_IOTA 1
+#endif
+constexpr bool kIotaVals = RT_SORT_IOTA != 0;
 
 namespace rt {
 
@@ -123,7 +129,7 @@ __global__ void __launch_bounds__(256) k_morton_hist(const float4* __restrict__ 
         tri_aabb(pos, idx, i, lo, hi);
         const uint32_t code = morton_code(P, lo, hi);
         keys[i] = code;
-        vals[i] = i;
+        if (vals) vals[i] = i;
         for (int p = 0; p < passes; ++p) atomicAdd(&sh[p][(code >> (8 * p)) & 255u], 1u);
     }
     __syncthreads();
@@ -151,7 +157,7 @@ __global__ void __launch_bounds__(256) k_radix_hist(const uint32_t* __restrict__
     }
 }
 
-__global__ void __launch_bounds__(SORT_THREADS, 3) k_onesweep(
+__global__ void __launch_bounds__(SORT_THREADS, RT_SORT_MINB) k_onesweep(
     const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin, uint32_t* __restrict__ kout,
     uint32_t* __restrict__ vout, uint32_t n, int shift, const uint32_t* __restrict__ hist,
     uint32_t* __restrict__ lookback, uint32_t* __restrict__ tile_ctr, uint32_t* __restrict__ status) {
@@ -202,11 +208,11 @@ __global__ void __launch_bounds__(256) k_refit_leaves(uint32_t n, const uint32_t
     }
 }
 
-// One level of the emit (emit_level), one block per run of items; level-0
-// blocks are kept to a register budget that lets RT_EMIT_MINB0 of them
-// share an SM.
+// One level of the emit (emit_level), one block per run of items; blocks
+// are kept to a register budget that lets RT_EMIT_MINB0 (level 0) or
+// RT_EMIT_MINB1 (above) of them share an SM.
 template <int C>
-__global__ void __launch_bounds__(C, C == EMIT_C0 ? RT_EMIT_MINB0 : 1) k_emit_level(
+__global__ void __launch_bounds__(C, C == EMIT_C0 ? RT_EMIT_MINB0 : RT_EMIT_MINB1) k_emit_level(
     uint32_t n, const uint32_t* __restrict__ skeys, const float4* __restrict__ leafbox,
     const EmitItem* __restrict__ in, const uint32_t* __restrict__ in_count, uint32_t n_in,
     EmitItem* __restrict__ out, uint32_t* __restrict__ out_count, float4* __restrict__ nodes,
@@ -332,10 +338,10 @@ cudaError_t lbvh_build(const LbvhArgs& a, cudaStream_t s) {
     const int sms = a.num_sms;
     k_bounds<<<grid_for(n, 256, sms * 8), 256, 0, s>>>(a.pos, a.idx_in, n, bounds);
     e = launch_dep(k_morton_hist, grid_for(n, 256, sms * 8), 256, 0, s, a.pos, a.idx_in, n,
-                   bounds, a.depth, passes, a.keys_unsorted, a.vals0, hist);
+                   bounds, a.depth, passes, a.keys_unsorted, kIotaVals ? nullptr : a.vals0, hist);
     if (e) return e;
     const uint32_t* kin = a.keys_unsorted;
-    const uint32_t* vin = a.vals0;
+    const uint32_t* vin = kIotaVals ? nullptr : a.vals0;
     uint32_t* kbuf[2] = {a.keys1, a.keys_sorted};
     uint32_t* vbuf[2] = {a.vals1, a.vals_sorted};
     for (int p = 0; p < passes; ++p) {

@@ -13,13 +13,19 @@
 
 namespace rt {
 
+#ifndef RT_SORT_MINB
+#define RT_SORT_MINB 3   // radix tiles resident per SM (register budget)
+#endif
 constexpr int SORT_THREADS = 256;
 constexpr int SORT_WARPS = SORT_THREADS / 32;
 constexpr int SORT_ITEMS = 16;
 constexpr int SORT_TILE = SORT_THREADS * SORT_ITEMS;   // 4096 keys per tile
 constexpr uint32_t LB_AGG = 1u << 30, LB_PREFIX = 2u << 30, LB_MASK = (1u << 30) - 1;
 constexpr uint32_t LB_SPIN_LIMIT = 1u << 22;
-constexpr int LB_WINDOW = 32;  // look-back words read per round trip
+#ifndef RT_LB_WINDOW
+#define RT_LB_WINDOW 32
+#endif
+constexpr int LB_WINDOW = RT_LB_WINDOW;  // look-back words read per round trip
 
 // float <-> order-preserving uint32 (min/max of the integers == fmin/fmax of
 // the floats for non-NaN values).
@@ -173,7 +179,8 @@ using SortSmem = SortSmemT<SORT_ITEMS>;
 // loads, ballot ranking in index order, decoupled look-back over
 // the earlier tiles of the same sequence, shared-memory staging and a
 // coalesced scatter.  Must be called by all SORT_THREADS threads of a block;
-// a tile holds SORT_THREADS * ITEMS keys.  A look-back that polls an
+// a tile holds SORT_THREADS * ITEMS keys.  A null `vin` stands for the
+// values 0, 1, 2, ... (the first pass of a build).  A look-back that polls an
 // unpublished word more than SPIN_LIMIT times gives up: it sets
 // RT_DEV_TIMEOUT in *status and goes on with the counts it has, so every
 // block ends; the tile's writes then stay inside [0, n), since a partial
@@ -201,7 +208,7 @@ __device__ __forceinline__ void onesweep_tile(SortSmemT<ITEMS>& S, uint32_t tile
         const size_t g = base + (size_t)warp * (ITEMS * 32) + j * 32 + lane;
         const bool ok = g < n;
         k[j] = ok ? __ldcs(&kin[g]) : 0xffffffffu;
-        v[j] = ok ? __ldcs(&vin[g]) : 0u;
+        v[j] = ok ? (vin ? __ldcs(&vin[g]) : (uint32_t)g) : 0u;
     }
 #pragma unroll
     for (int j = 0; j < ITEMS; ++j) {
@@ -399,13 +406,19 @@ __device__ __forceinline__ uint64_t delta(const uint32_t* __restrict__ k, uint32
 // boundaries), so chunks and levels compose.
 // ---------------------------------------------------------------------------
 constexpr int EMIT_FMAX = 128;   // items a block may leave
-constexpr int EMIT_GROUP = 8;    // blocks of one level gathered by a block of the next
+#ifndef RT_EMIT_GROUP
+#define RT_EMIT_GROUP 8
+#endif
+constexpr int EMIT_GROUP = RT_EMIT_GROUP;   // blocks of one level gathered by a block of the next
 
 #ifndef RT_EMIT_C0
 #define RT_EMIT_C0 512
 #endif
 #ifndef RT_EMIT_MINB0
-#define RT_EMIT_MINB0 2
+#define RT_EMIT_MINB0 3
+#endif
+#ifndef RT_EMIT_MINB1
+#define RT_EMIT_MINB1 1
 #endif
 #ifndef RT_EMIT_LEAVE0
 #define RT_EMIT_LEAVE0 128u   // runs a level-0 block may leave unjoined
