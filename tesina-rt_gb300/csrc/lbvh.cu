@@ -10,15 +10,21 @@
 //                   ballot ranking and decoupled look-back with a
 //                   bounded spin (replaces the bitonic network of
 //                   bvh-builder-sort.cl and bvh-builder.cpp:361-454);
-//   k_permute       rearrange_indices / rearrange_map (:49-72) fused with the
-//                   triangle records used by traversal and the leaf AABBs;
+//   k_emit_level0_permute
+//                   rearrange_indices / rearrange_map (:49-72) and the
+//                   triangle records used by traversal, fused with level 0 of
+//                   the emit, which joins the triangles with their AABBs
+//                   still in registers;
 //   k_emit_level    bottom-up build of the radix tree (Apetrei's
 //                   agglomerative formulation of Karras' tree), collapsed to
 //                   the reference's leaf rule (find_middle, :484-552), with
 //                   every AABB (build_leaf_bbox / build_node_bbox, :262-311)
 //                   computed on the way up; a few launches whose warps join
-//                   runs of 32 items with shuffles (level 0 over 512
-//                   triangles per block, then over what 8 blocks left).
+//                   runs of 32 items (level 0 over 512 triangles per block,
+//                   then over what 8 blocks left).
+//   k_permute       the permutation alone, storing leaf AABBs (the stage-wise
+//                   entry point); k_refit_leaves the leaf AABBs of the
+//                   existing order (refit).
 // The per-element work lives in lbvh_dev.cuh, shared with the many-scene
 // persistent build of batch.cu.
 #include <cuda_runtime.h>
