@@ -192,7 +192,6 @@ __global__ void __launch_bounds__(SORT_THREADS, 4) k_batch_build(BatchBuildArgs 
                 const MortonParams P = morton_params(B.bounds, B.depth);
                 const uint32_t code = morton_code(P, lo, hi);
                 B.keys_unsorted[li] = code;
-                B.vals0[li] = li;
                 for (int p = 0; p < B.passes; ++p) {
                     const uint32_t d = (code >> (8 * p)) & 255u;
                     if (single)
@@ -228,7 +227,8 @@ __global__ void __launch_bounds__(SORT_THREADS, 4) k_batch_build(BatchBuildArgs 
             const uint32_t lt = t - s_tileoff[s];
             const int dst = ((B.passes - 1 - p) & 1) ? 0 : 1;   // last pass -> sorted
             const uint32_t* kin = p == 0 ? B.keys_unsorted : (dst ? B.keys1 : B.keys_sorted);
-            const uint32_t* vin = p == 0 ? B.vals0 : (dst ? B.vals1 : B.vals_sorted);
+            // the first pass makes the identity values itself
+            const uint32_t* vin = p == 0 ? nullptr : (dst ? B.vals1 : B.vals_sorted);
             uint32_t* kout = dst ? B.keys_sorted : B.keys1;
             uint32_t* vout = dst ? B.vals_sorted : B.vals1;
             const uint32_t ntiles_s = s_tileoff[s + 1] - s_tileoff[s];
@@ -239,15 +239,7 @@ __global__ void __launch_bounds__(SORT_THREADS, 4) k_batch_build(BatchBuildArgs 
         if (p == A.passes - 1) stamp(A, 4);
     }
 
-    // ---- stage 4: permutation into sorted order ------------------------------
-    for (uint32_t g = blockIdx.x * blockDim.x + tid; g < total; g += nblk * blockDim.x) {
-        const int s = find_segment(s_toff, nsc, g);
-        const BatchScene& B = A.scenes[s];
-        const PermuteIO P{B.vals_sorted, B.idx_in, B.map_in,  B.orig_in, B.pos,
-                          B.idx_out,     B.map_out, B.orig_out, B.tris};
-        permute_one(g - s_toff[s], P, B.leafbox);
-    }
-    grid.sync();
+    // the permutation into sorted order happens in level 0 of the emit
     stamp(A, 5);
     // ---- stage 5: the emit, level by level (k_batch_emit launches) ---------
 }
@@ -255,9 +247,10 @@ __global__ void __launch_bounds__(SORT_THREADS, 4) k_batch_build(BatchBuildArgs 
 // One level of the emit over every scene that still has blocks at it: the
 // one-scene emit's blocks (emit_level, the same items, buffers and leave
 // rule), with block j of the launch taken by the scene whose range of the
-// level's blocks holds j.
+// level's blocks holds j.  The C == EMIT_C0 instance is level 0.
+static_assert(EMIT_C0 != EMIT_C1, "k_batch_emit tells level 0 by its block size");
 template <int C>
-__global__ void __launch_bounds__(C, C == EMIT_C0 ? RT_EMIT_MINB0 : 1) k_batch_emit(
+__global__ void __launch_bounds__(C, C == EMIT_C0 ? RT_EMIT_MINB0 : RT_EMIT_MINB1) k_batch_emit(
     const BatchScene* __restrict__ scenes, int count, int level, const uint32_t* __restrict__ off,
     uint32_t* __restrict__ status) {
     extern __shared__ __align__(16) unsigned char emit_smem[];
@@ -267,16 +260,21 @@ __global__ void __launch_bounds__(C, C == EMIT_C0 ? RT_EMIT_MINB0 : 1) k_batch_e
     const uint32_t job = blockIdx.x - off[s];
     const EmitBuffers E = emit_buffers(B.n, B.emit);
     uint32_t n_in = emit_blocks0(B.n);   // blocks of the level below
-    if (level == 0) {
-        emit_level<C>(S, job, B.n, B.keys_sorted, B.leafbox, nullptr, nullptr, 0, E.items[0],
-                      E.counts[0], B.nodes, B.min_leaf, emit_leave(0, n_in), B.hdr, status);
-        return;
+    if constexpr (C == EMIT_C0) {
+        // level 0 permutes its triangles into sorted order and joins them
+        // with their AABBs in registers (as k_emit_level0_permute)
+        const PermuteIO P{B.vals_sorted, B.idx_in,  B.map_in,   B.orig_in, B.pos,
+                          B.idx_out,     B.map_out, B.orig_out, B.tris};
+        emit_level<C, true>(S, job, B.n, B.keys_sorted, nullptr, nullptr, nullptr, 0, E.items[0],
+                            E.counts[0], B.nodes, B.min_leaf, emit_leave(0, n_in), B.hdr, status,
+                            P);
+    } else {
+        for (int l = 2; l <= level; ++l) n_in = emit_next_level(n_in);
+        const int src = (level - 1) & 1;
+        emit_level<C>(S, job, B.n, B.keys_sorted, nullptr, E.items[src], E.counts[src], n_in,
+                      E.items[src ^ 1], E.counts[src ^ 1], B.nodes, B.min_leaf,
+                      emit_leave(level, emit_next_level(n_in)), B.hdr, status);
     }
-    for (int l = 2; l <= level; ++l) n_in = emit_next_level(n_in);
-    const int src = (level - 1) & 1;
-    emit_level<C>(S, job, B.n, B.keys_sorted, B.leafbox, E.items[src], E.counts[src], n_in,
-                  E.items[src ^ 1], E.counts[src ^ 1], B.nodes, B.min_leaf,
-                  emit_leave(level, emit_next_level(n_in)), B.hdr, status);
 }
 
 __global__ void k_batch_stamp(unsigned long long* t) { *t = globaltimer(); }

@@ -22,13 +22,11 @@ struct BatchScene {
     uint32_t* map_out;
     uint32_t* orig_out;
     uint32_t* keys_unsorted;
-    uint32_t* vals0;
     uint32_t* keys1;
     uint32_t* vals1;
     uint32_t* keys_sorted;
     uint32_t* vals_sorted;
     float4* tris;
-    float4* leafbox;
     float4* nodes;
     BvhHeader* hdr;
     uint32_t* bounds;     // 8 words

@@ -101,13 +101,11 @@ std::vector<rt::BatchScene> scene_table(rt_batch* b) {
         B.map_out = s->d_map[s->cur ^ 1];
         B.orig_out = s->d_orig[s->cur ^ 1];
         B.keys_unsorted = s->d_keys_unsorted;
-        B.vals0 = s->d_vals0;
         B.keys1 = s->d_keys1;
         B.vals1 = s->d_vals1;
         B.keys_sorted = s->d_keys_sorted;
         B.vals_sorted = s->d_vals_sorted;
         B.tris = s->d_tris;
-        B.leafbox = s->d_leafbox;
         B.nodes = s->d_nodes;
         B.hdr = s->d_hdr;
         uint32_t* base = b->d_scratch + b->scratch_at[k];
