@@ -441,7 +441,8 @@ RT_API int32_t rt_batch_info(rt_ctx* ctx, rt_batch* batch, uint32_t* scenes,
 /* Profiling of the batched build: when enabled, the build kernel records a
  * device timestamp after each of its stages; rt_batch_stage_times returns the
  * durations in ms of: init, scene bounds, Morton + histograms, radix passes,
- * permutation, emit + refit (synchronous). */
+ * permutation (near 0: the permutation runs inside the emit's first level),
+ * emit + refit (synchronous). */
 RT_API int32_t rt_batch_profile(rt_ctx* ctx, rt_batch* batch, int32_t enable);
 RT_API int32_t rt_batch_stage_times(rt_ctx* ctx, rt_batch* batch, float ms[6]);
 
