@@ -46,6 +46,15 @@
 #define RT_SORT_IOTA 1
 #endif
 constexpr bool kIotaVals = RT_SORT_IOTA != 0;
+// Digit width of the build's radix passes: 8 (four passes for 30-bit keys)
+// or 10 (three).  The pair sort entry points always use 8.
+#ifndef RT_SORT_BITS
+#define RT_SORT_BITS 8
+#endif
+constexpr int kBuildBits = RT_SORT_BITS;
+constexpr int kBuildRadix = 1 << kBuildBits;
+constexpr int kMaxBuildPasses = (32 + kBuildBits - 1) / kBuildBits;
+static_assert(kBuildBits == 8 || kBuildBits == 10, "build digit width");
 
 namespace rt {
 
@@ -126,8 +135,8 @@ __global__ void __launch_bounds__(256) k_morton_hist(const float4* __restrict__ 
                                                      uint32_t* __restrict__ vals,
                                                      uint32_t* __restrict__ hist) {
     pdl_enter();
-    __shared__ uint32_t sh[4][256];
-    for (int i = threadIdx.x; i < 4 * 256; i += blockDim.x) (&sh[0][0])[i] = 0;
+    __shared__ uint32_t sh[kMaxBuildPasses][kBuildRadix];
+    for (int i = threadIdx.x; i < kMaxBuildPasses * kBuildRadix; i += blockDim.x) (&sh[0][0])[i] = 0;
     __syncthreads();
     const MortonParams P = morton_params(bounds, depth);
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -136,10 +145,11 @@ __global__ void __launch_bounds__(256) k_morton_hist(const float4* __restrict__ 
         const uint32_t code = morton_code(P, lo, hi);
         keys[i] = code;
         if (vals) vals[i] = i;
-        for (int p = 0; p < passes; ++p) atomicAdd(&sh[p][(code >> (8 * p)) & 255u], 1u);
+        for (int p = 0; p < passes; ++p)
+            atomicAdd(&sh[p][(code >> (kBuildBits * p)) & (uint32_t)(kBuildRadix - 1)], 1u);
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < passes * 256; i += blockDim.x) {
+    for (int i = threadIdx.x; i < passes * kBuildRadix; i += blockDim.x) {
         const uint32_t v = (&sh[0][0])[i];
         if (v) atomicAdd(&hist[i], v);
     }
@@ -163,16 +173,23 @@ __global__ void __launch_bounds__(256) k_radix_hist(const uint32_t* __restrict__
     }
 }
 
+// One radix pass of BITS-bit digits; dynamic shared memory of
+// sizeof(SortSmemT<SORT_ITEMS, BITS>).
+template <int BITS>
 __global__ void __launch_bounds__(SORT_THREADS, RT_SORT_MINB) k_onesweep(
     const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin, uint32_t* __restrict__ kout,
     uint32_t* __restrict__ vout, uint32_t n, int shift, const uint32_t* __restrict__ hist,
     uint32_t* __restrict__ lookback, uint32_t* __restrict__ tile_ctr, uint32_t* __restrict__ status) {
     pdl_enter();
-    __shared__ SortSmem S;
+    extern __shared__ __align__(16) unsigned char sort_smem[];
+    auto& S = *reinterpret_cast<SortSmemT<SORT_ITEMS, BITS>*>(sort_smem);
     if (threadIdx.x == 0) S.tile = atomicAdd(tile_ctr, 1u);   // tiles in launch order
     __syncthreads();
-    onesweep_tile(S, S.tile, kin, vin, kout, vout, n, shift, hist, lookback, status);
+    onesweep_tile<SORT_ITEMS, LB_SPIN_LIMIT, BITS>(S, S.tile, kin, vin, kout, vout, n, shift, hist,
+                                                   lookback, status);
 }
+template <int BITS>
+constexpr size_t onesweep_smem() { return sizeof(SortSmemT<SORT_ITEMS, BITS>); }
 
 // Self-test of the look-back timeout: one block sorts tile 1 of a pass
 // whose tile 0 is never launched, so its look-back word stays unpublished;
@@ -246,7 +263,8 @@ __global__ void __launch_bounds__(EMIT_C0, RT_EMIT_MINB0) k_emit_level0_permute(
 
 static size_t sort_scratch_bytes(uint32_t n, int passes) {
     const size_t tiles = ((size_t)n + SORT_TILE - 1) / SORT_TILE;
-    return (sizeof(uint32_t) * (8 + 4 * 256 + 4 + (size_t)passes * tiles * 256) + 255) & ~(size_t)255;
+    return (sizeof(uint32_t) * (8 + (size_t)kMaxBuildPasses * kBuildRadix + 4 +
+                                (size_t)passes * tiles * kBuildRadix) + 255) & ~(size_t)255;
 }
 
 static size_t emit_scratch_bytes(uint32_t n) { return emit_buffers_bytes(n); }
@@ -256,32 +274,34 @@ static size_t emit_scratch_bytes(uint32_t n) { return emit_buffers_bytes(n); }
 // buffers alternate: A holds level 0, 2, ... and B level 1, 3, ....  With
 // `perm`, level 0 also performs the permutation (k_emit_level0_permute);
 // without, it reads the leaf AABBs a previous launch stored.
+// The shared-memory opt-ins of the kernels with dynamic shared memory (a
+// property of the kernel on each device), once per device.
+static cudaError_t setup_kernels() {
+    static std::mutex mu;
+    static uint64_t done = 0;   // devices 0..63 set up
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lk(mu);
+    if (dev < 64 && ((done >> dev) & 1)) return cudaSuccess;
+    auto opt_in = [&](const void* f, size_t bytes) {
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    };
+    opt_in((const void*)k_emit_level<EMIT_C0>, sizeof(EmitSmem<EMIT_C0>));
+    opt_in((const void*)k_emit_level0_permute, sizeof(EmitSmem<EMIT_C0>));
+    opt_in((const void*)k_emit_level<EMIT_C1>, sizeof(EmitSmem<EMIT_C1>));
+    opt_in((const void*)k_onesweep<8>, onesweep_smem<8>());
+    opt_in((const void*)k_onesweep<kBuildBits>, onesweep_smem<kBuildBits>());
+    if (e != cudaSuccess) return e;
+    if (dev < 64) done |= 1ull << dev;
+    return cudaSuccess;
+}
+
 static cudaError_t launch_emit(const LbvhArgs& a, uint8_t* emit_scratch, cudaStream_t s,
                                const PermuteIO* perm = nullptr) {
     const uint32_t n = a.n;
-    {
-        // the shared-memory opt-in is a property of the kernel on each device
-        static std::mutex mu;
-        static uint64_t done = 0;   // devices 0..63 set up
-        int dev = 0;
-        cudaError_t e = cudaGetDevice(&dev);
-        if (e != cudaSuccess) return e;
-        std::lock_guard<std::mutex> lk(mu);
-        if (dev >= 64 || !((done >> dev) & 1)) {
-            e = cudaFuncSetAttribute(k_emit_level<EMIT_C0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)sizeof(EmitSmem<EMIT_C0>));
-            if (e == cudaSuccess)
-                e = cudaFuncSetAttribute(k_emit_level0_permute,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)sizeof(EmitSmem<EMIT_C0>));
-            if (e == cudaSuccess)
-                e = cudaFuncSetAttribute(k_emit_level<EMIT_C1>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)sizeof(EmitSmem<EMIT_C1>));
-            if (e != cudaSuccess) return e;
-            if (dev < 64) done |= 1ull << dev;
-        }
-    }
+    if (cudaError_t e0 = setup_kernels()) return e0;
     const uint32_t nb0 = emit_blocks0(n);
     const EmitBuffers B = emit_buffers(n, emit_scratch);
     cudaError_t e =
@@ -324,18 +344,20 @@ size_t lbvh_scratch_bytes(uint32_t n, int passes) {
     return sort_scratch_bytes(n, passes) + emit_scratch_bytes(n);
 }
 
-size_t lbvh_emit_offset(uint32_t n) { return sort_scratch_bytes(n, 4); }
+size_t lbvh_emit_offset(uint32_t n) { return sort_scratch_bytes(n, kMaxBuildPasses); }
 
 cudaError_t lbvh_build(const LbvhArgs& a, cudaStream_t s) {
     const uint32_t n = a.n;
-    const int passes = (a.depth + 7) / 8;
+    const int passes = (a.depth + kBuildBits - 1) / kBuildBits;
     const size_t tiles = ((size_t)n + SORT_TILE - 1) / SORT_TILE;
-    // scratch: bounds[8] | hist[4*256] | tile_ctr[4] | lookback[passes*tiles*256]
+    // scratch: bounds[8] | hist[passes max * radix] | tile_ctr[4] |
+    // lookback[passes * tiles * radix]
     uint32_t* bounds = a.scratch;
     uint32_t* hist = bounds + 8;
-    uint32_t* tile_ctr = hist + 4 * 256;
+    uint32_t* tile_ctr = hist + kMaxBuildPasses * kBuildRadix;
     uint32_t* lookback = tile_ctr + 4;
-    cudaError_t e;
+    cudaError_t e = setup_kernels();
+    if (e) return e;
     e = cudaMemsetAsync(a.scratch, 0, sort_scratch_bytes(n, passes), s);
     if (e) return e;
     // bounds init: lo = ordered(+big) via 0xFF.. (max), hi = 0 (min)
@@ -353,9 +375,10 @@ cudaError_t lbvh_build(const LbvhArgs& a, cudaStream_t s) {
     for (int p = 0; p < passes; ++p) {
         // the last pass always lands in keys_sorted / vals_sorted
         const int dst = ((passes - 1 - p) & 1) ? 0 : 1;
-        e = launch_dep(k_onesweep, (unsigned)tiles, SORT_THREADS, 0, s, kin, vin, kbuf[dst],
-                       vbuf[dst], n, 8 * p, hist + 256 * p, lookback + (size_t)p * tiles * 256,
-                       tile_ctr + p, a.status);
+        e = launch_dep(k_onesweep<kBuildBits>, (unsigned)tiles, SORT_THREADS,
+                       onesweep_smem<kBuildBits>(), s, kin, vin, kbuf[dst], vbuf[dst], n,
+                       kBuildBits * p, (const uint32_t*)(hist + kBuildRadix * p),
+                       lookback + (size_t)p * tiles * kBuildRadix, tile_ctr + p, a.status);
         if (e) return e;
         kin = kbuf[dst];
         vin = vbuf[dst];
@@ -406,7 +429,9 @@ cudaError_t radix_sort_pairs(const uint32_t* kin, const uint32_t* vin, uint32_t*
     uint32_t* hist = scratch;
     uint32_t* tile_ctr = hist + 4 * 256;
     uint32_t* lookback = tile_ctr + 4;
-    cudaError_t e = cudaMemsetAsync(scratch, 0, sizeof(uint32_t) * radix_scratch_words(n, passes), s);
+    cudaError_t e = setup_kernels();
+    if (e) return e;
+    e = cudaMemsetAsync(scratch, 0, sizeof(uint32_t) * radix_scratch_words(n, passes), s);
     if (e) return e;
     if (n == 0) return cudaSuccess;
     k_radix_hist<<<grid_for(n, 256, num_sms * 8), 256, 0, s>>>(kin, n, passes, hist);
@@ -416,9 +441,9 @@ cudaError_t radix_sort_pairs(const uint32_t* kin, const uint32_t* vin, uint32_t*
         const bool to_out = ((passes - 1 - p) & 1) == 0;
         uint32_t* ko = to_out ? kout : ktmp;
         uint32_t* vo = to_out ? vout : vtmp;
-        k_onesweep<<<(unsigned)tiles, SORT_THREADS, 0, s>>>(ki, vi, ko, vo, n, 8 * p, hist + 256 * p,
-                                                          lookback + (size_t)p * tiles * 256,
-                                                          tile_ctr + p, status);
+        k_onesweep<8><<<(unsigned)tiles, SORT_THREADS, onesweep_smem<8>(), s>>>(
+            ki, vi, ko, vo, n, 8 * p, hist + 256 * p, lookback + (size_t)p * tiles * 256,
+            tile_ctr + p, status);
         ki = ko;
         vi = vo;
     }

@@ -168,31 +168,33 @@ __device__ __forceinline__ uint32_t block_excl_scan_256(uint32_t v, uint32_t* s_
 #define RT_SORT_MARK(k)
 #endif
 
-template <int ITEMS>
+template <int ITEMS, int BITS = 8>
 struct SortSmemT {
+    static constexpr int RADIX = 1 << BITS;
     uint32_t keys[SORT_THREADS * ITEMS];
     uint32_t vals[SORT_THREADS * ITEMS];
-    uint32_t whist[SORT_WARPS][256];
-    uint32_t goff[256];
-    uint32_t lstart[256];
+    uint32_t whist[SORT_WARPS][RADIX];
+    uint32_t goff[RADIX];
+    uint32_t lstart[RADIX];
     uint32_t scan[SORT_WARPS];
     uint32_t tile;
 };
 using SortSmem = SortSmemT<SORT_ITEMS>;
 
-// One tile of a stable LSD radix pass (8-bit digit at `shift`): warp-striped
-// loads, ballot ranking in index order, decoupled look-back over
-// the earlier tiles of the same sequence, shared-memory staging and a
-// coalesced scatter.  Must be called by all SORT_THREADS threads of a block;
-// a tile holds SORT_THREADS * ITEMS keys.  A null `vin` stands for the
-// values 0, 1, 2, ... (the first pass of a build).  A look-back that polls an
-// unpublished word more than SPIN_LIMIT times gives up: it sets
-// RT_DEV_TIMEOUT in *status and goes on with the counts it has, so every
-// block ends; the tile's writes then stay inside [0, n), since a partial
-// prefix only lowers the scatter offsets, which start at the digit's global
-// offset.
-template <int ITEMS = SORT_ITEMS, uint32_t SPIN_LIMIT = LB_SPIN_LIMIT>
-__device__ __forceinline__ void onesweep_tile(SortSmemT<ITEMS>& S, uint32_t tile,
+// One tile of a stable LSD radix pass (BITS-bit digit at `shift`; each
+// thread owns 2^BITS / SORT_THREADS consecutive digits): warp-striped loads,
+// ballot ranking in index order, decoupled look-back over the earlier tiles
+// of the same sequence, shared-memory staging and a coalesced scatter.  Must
+// be called by all SORT_THREADS threads of a block; a tile holds
+// SORT_THREADS * ITEMS keys.  A null `vin` stands for the values 0, 1, 2, ...
+// (the first pass of a build).  A look-back that polls an unpublished word
+// more than SPIN_LIMIT times gives up: it sets RT_DEV_TIMEOUT in *status and
+// goes on with the counts it has, so every block ends; the tile's writes
+// then stay inside [0, n), since a partial prefix only lowers the scatter
+// offsets, which start at the digit's global offset.  `hist` holds the
+// pass's 2^BITS digit counts, `lookback` 2^BITS words per tile.
+template <int ITEMS = SORT_ITEMS, uint32_t SPIN_LIMIT = LB_SPIN_LIMIT, int BITS = 8>
+__device__ __forceinline__ void onesweep_tile(SortSmemT<ITEMS, BITS>& S, uint32_t tile,
                                               const uint32_t* __restrict__ kin,
                                               const uint32_t* __restrict__ vin,
                                               uint32_t* __restrict__ kout,
@@ -200,9 +202,13 @@ __device__ __forceinline__ void onesweep_tile(SortSmemT<ITEMS>& S, uint32_t tile
                                               const uint32_t* __restrict__ hist,
                                               uint32_t* __restrict__ lookback,
                                               uint32_t* __restrict__ status) {
+    constexpr int RADIX = 1 << BITS;
+    constexpr int DPT = RADIX / SORT_THREADS;   // digits per thread
+    constexpr uint32_t DMASK = (uint32_t)RADIX - 1u;
+    static_assert(DPT >= 1 && RADIX % SORT_THREADS == 0, "digits per thread");
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     RT_SORT_MARK(0);
-    for (int i = tid; i < SORT_WARPS * 256; i += SORT_THREADS) (&S.whist[0][0])[i] = 0;
+    for (int i = tid; i < SORT_WARPS * RADIX; i += SORT_THREADS) (&S.whist[0][0])[i] = 0;
     __syncthreads();
     const size_t base = (size_t)tile * (SORT_THREADS * ITEMS);
     const uint32_t lanemask_lt = (1u << lane) - 1u;
@@ -219,12 +225,12 @@ __device__ __forceinline__ void onesweep_tile(SortSmemT<ITEMS>& S, uint32_t tile
     for (int j = 0; j < ITEMS; ++j) {
         const size_t g = base + (size_t)warp * (ITEMS * 32) + j * 32 + lane;
         const bool ok = g < n;
-        const uint32_t d = (k[j] >> shift) & 255u;
+        const uint32_t d = (k[j] >> shift) & DMASK;
         // lanes holding the same digit: one ballot per digit bit (a fixed
         // cost, where a match instruction grows with the distinct digits)
         uint32_t peers = __ballot_sync(0xffffffffu, ok);
 #pragma unroll
-        for (int b = 0; b < 8; ++b) {
+        for (int b = 0; b < BITS; ++b) {
             const uint32_t bit = __ballot_sync(0xffffffffu, (d >> b) & 1u);
             peers &= ((d >> b) & 1u) ? bit : ~bit;
         }
@@ -241,18 +247,33 @@ __device__ __forceinline__ void onesweep_tile(SortSmemT<ITEMS>& S, uint32_t tile
     __syncthreads();
 
     RT_SORT_MARK(1);
-    const uint32_t dgt = tid;   // 256 threads <-> 256 digits
-    uint32_t cnt = 0;
+    // this thread's digits: tid * DPT .. tid * DPT + DPT - 1
+    const uint32_t dgt0 = (uint32_t)tid * DPT;
+    uint32_t cnt[DPT], lstart[DPT];
+    uint32_t tsum = 0;
 #pragma unroll
-    for (int w = 0; w < SORT_WARPS; ++w) {
-        const uint32_t c = S.whist[w][dgt];
-        S.whist[w][dgt] = cnt;
-        cnt += c;
+    for (int q = 0; q < DPT; ++q) {
+        uint32_t c = 0;
+#pragma unroll
+        for (int w = 0; w < SORT_WARPS; ++w) {
+            const uint32_t x = S.whist[w][dgt0 + q];
+            S.whist[w][dgt0 + q] = c;
+            c += x;
+        }
+        cnt[q] = c;
+        lstart[q] = tsum;
+        tsum += c;
     }
-    uint32_t* my = &lookback[(size_t)tile * 256 + dgt];
-    st_relaxed(my, (tile == 0 ? LB_PREFIX : LB_AGG) | cnt);   // as early as the counts are known
-    const uint32_t lstart = block_excl_scan_256(cnt, S.scan);
-    S.lstart[dgt] = lstart;
+    uint32_t* my = &lookback[(size_t)tile * RADIX + dgt0];
+#pragma unroll
+    for (int q = 0; q < DPT; ++q)   // as early as the counts are known
+        st_relaxed(my + q, (tile == 0 ? LB_PREFIX : LB_AGG) | cnt[q]);
+    const uint32_t lbase = block_excl_scan_256(tsum, S.scan);
+#pragma unroll
+    for (int q = 0; q < DPT; ++q) {
+        lstart[q] += lbase;
+        S.lstart[dgt0 + q] = lstart[q];
+    }
     __syncthreads();
     // the tile in digit order in shared memory (frees the registers of the
     // keys for the look-back's window)
@@ -260,7 +281,7 @@ __device__ __forceinline__ void onesweep_tile(SortSmemT<ITEMS>& S, uint32_t tile
     for (int j = 0; j < ITEMS; ++j) {
         const size_t g = base + (size_t)warp * (ITEMS * 32) + j * 32 + lane;
         if (g < n) {
-            const uint32_t d = (k[j] >> shift) & 255u;
+            const uint32_t d = (k[j] >> shift) & DMASK;
             const uint32_t p = S.lstart[d] + S.whist[warp][d] + rank[j];
             S.keys[p] = k[j];
             S.vals[p] = v[j];
@@ -268,51 +289,74 @@ __device__ __forceinline__ void onesweep_tile(SortSmemT<ITEMS>& S, uint32_t tile
     }
     // Decoupled look-back.  Each word holds its whole message (flag and
     // count), so relaxed accesses suffice; the words of LB_WINDOW earlier
-    // tiles are read per round trip and summed nearest first, up to the first
-    // inclusive prefix or the first tile that has not published yet.
+    // tiles are read per round trip and summed nearest first, for each digit
+    // up to its first inclusive prefix, and for all of them up to the first
+    // tile that has not published a digit still open.
     RT_SORT_MARK(2);
-    uint32_t excl = 0;
+    uint32_t excl[DPT];
+#pragma unroll
+    for (int q = 0; q < DPT; ++q) excl[q] = 0;
     if (tile > 0) {
+        constexpr uint32_t ALL = (1u << DPT) - 1u;
+        uint32_t open = ALL;   // digits without an inclusive prefix yet
         int64_t p = (int64_t)tile - 1;
         uint32_t spins = 0;
         for (;;) {
-            uint32_t w[LB_WINDOW];
+            uint32_t w[LB_WINDOW][DPT];
 #pragma unroll
-            for (int q = 0; q < LB_WINDOW; ++q)   // tile 0 is always a prefix: p - q < 0 is never summed
-                w[q] = p - q >= 0 ? ld_relaxed(&lookback[(size_t)(p - q) * 256 + dgt]) : LB_PREFIX;
+            for (int t = 0; t < LB_WINDOW; ++t)   // tile 0 is always a prefix: p - t < 0 is never summed
+#pragma unroll
+                for (int q = 0; q < DPT; ++q)
+                    w[t][q] = p - t >= 0 ? ld_relaxed(&lookback[(size_t)(p - t) * RADIX + dgt0 + q])
+                                         : LB_PREFIX;
             int used = 0;
-            bool done = false, wait = false;
+            bool wait = false;
 #pragma unroll
-            for (int q = 0; q < LB_WINDOW; ++q) {
-                const uint32_t flag = w[q] & ~LB_MASK;
-                if (!done && !wait) {
-                    if (flag == 0) {
+            for (int t = 0; t < LB_WINDOW; ++t) {
+                if (open && !wait) {
+                    bool miss = false;
+#pragma unroll
+                    for (int q = 0; q < DPT; ++q)
+                        miss |= ((open >> q) & 1u) && (w[t][q] & ~LB_MASK) == 0u;
+                    if (miss) {
                         wait = true;
                     } else {
-                        excl += w[q] & LB_MASK;
+#pragma unroll
+                        for (int q = 0; q < DPT; ++q)
+                            if ((open >> q) & 1u) {
+                                excl[q] += w[t][q] & LB_MASK;
+                                if ((w[t][q] & ~LB_MASK) == LB_PREFIX) open &= ~(1u << q);
+                            }
                         ++used;
-                        done = flag == LB_PREFIX;
                     }
                 }
             }
-            if (done) break;
+            if (!open) break;
             p -= used;
             if (wait && ++spins > SPIN_LIMIT) {
                 atomicOr(status, RT_DEV_TIMEOUT);
                 break;
             }
         }
-        st_relaxed(my, LB_PREFIX | (excl + cnt));
+#pragma unroll
+        for (int q = 0; q < DPT; ++q) st_relaxed(my + q, LB_PREFIX | (excl[q] + cnt[q]));
     }
     RT_SORT_MARK(3);
-    const uint32_t gstart = block_excl_scan_256(__ldg(&hist[dgt]), S.scan);
-    S.goff[dgt] = gstart + excl - lstart;
+    uint32_t h[DPT], hsum = 0;
+#pragma unroll
+    for (int q = 0; q < DPT; ++q) {
+        h[q] = hsum;
+        hsum += __ldg(&hist[dgt0 + q]);
+    }
+    const uint32_t gbase = block_excl_scan_256(hsum, S.scan);
+#pragma unroll
+    for (int q = 0; q < DPT; ++q) S.goff[dgt0 + q] = gbase + h[q] + excl[q] - lstart[q];
     __syncthreads();
     RT_SORT_MARK(4);
     const uint32_t valid_n = (uint32_t)min((size_t)(SORT_THREADS * ITEMS), (size_t)n - base);
     for (uint32_t i = tid; i < valid_n; i += SORT_THREADS) {
         const uint32_t key = S.keys[i];
-        const uint32_t d = (key >> shift) & 255u;
+        const uint32_t d = (key >> shift) & DMASK;
         const uint32_t dst = S.goff[d] + i;
         kout[dst] = key;
         vout[dst] = S.vals[i];
