@@ -13,6 +13,9 @@
 
 namespace rt {
 
+#ifndef RT_SORT_VEC_LOADS
+#define RT_SORT_VEC_LOADS 1   // whole tiles staged in shared memory: 0 no, 1 by 128-bit loads, 2 by bulk copy
+#endif
 #ifndef RT_SORT_MINB
 #define RT_SORT_MINB 3   // radix tiles resident per SM (register budget)
 #endif
@@ -54,6 +57,42 @@ __device__ __forceinline__ uint32_t ld_relaxed(const uint32_t* p) {
 __device__ __forceinline__ void st_relaxed(uint32_t* p, uint32_t v) {
     asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
+
+// A shared-memory mbarrier and the 1-D bulk copy (the TMA engine without a
+// tensor map) that completes on it.
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_inval(uint64_t* bar) {
+    asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+                 "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok) : "r"(smem_addr(bar)), "r"(parity) : "memory");
+    return ok != 0;
+}
+// global -> shared, `bytes` a multiple of 16, both addresses 16-byte aligned
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+        ::"r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(bar)) : "memory");
+}
+__device__ __forceinline__ void fence_proxy_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+constexpr uint32_t BULK_WAIT_LIMIT = 1u << 22;   // polls of a bulk copy's mbarrier
 // atomicAdd with acquire-release ordering at GPU scope: the caller's earlier
 // writes are visible to whoever reads the counter's new value, and the
 // caller sees everything released by earlier adders.
@@ -169,13 +208,14 @@ __device__ __forceinline__ uint32_t block_excl_scan_256(uint32_t v, uint32_t* s_
 #endif
 
 template <int ITEMS, int BITS = 8>
-struct SortSmemT {
+struct __align__(16) SortSmemT {
     static constexpr int RADIX = 1 << BITS;
     uint32_t keys[SORT_THREADS * ITEMS];
     uint32_t vals[SORT_THREADS * ITEMS];
     uint32_t whist[SORT_WARPS][RADIX];
     uint32_t goff[RADIX];
     uint32_t lstart[RADIX];
+    uint64_t bar;   // the bulk tile load's mbarrier
     uint32_t scan[SORT_WARPS];
     uint32_t tile;
 };
@@ -214,6 +254,51 @@ __device__ __forceinline__ void onesweep_tile(SortSmemT<ITEMS, BITS>& S, uint32_
     const uint32_t lanemask_lt = (1u << lane) - 1u;
 
     uint32_t k[ITEMS], v[ITEMS], rank[ITEMS];
+#if RT_SORT_VEC_LOADS
+    // a whole, 16-byte aligned tile: 128-bit loads into shared memory, then
+    // the warp-striped layout the ranking needs from there
+    const bool vec = base + (size_t)(SORT_THREADS * ITEMS) <= n &&
+                     ((reinterpret_cast<uintptr_t>(kin) | reinterpret_cast<uintptr_t>(vin)) & 15u) == 0;
+    static_assert(ITEMS % 4 == 0, "whole 128-bit words per thread");
+    if (vec) {
+#if RT_SORT_VEC_LOADS == 2
+        // one bulk copy per array, completing on the tile's mbarrier
+        constexpr uint32_t TB = SORT_THREADS * ITEMS * 4;
+        if (tid == 0) {
+            mbar_init(&S.bar);
+            fence_proxy_async_smem();   // earlier generic accesses of the buffers come first
+            mbar_arrive_expect_tx(&S.bar, vin ? 2 * TB : TB);
+            bulk_load(S.keys, kin + base, TB, &S.bar);
+            if (vin) bulk_load(S.vals, vin + base, TB, &S.bar);
+        }
+        __syncthreads();   // the barrier is initialised before anyone polls it
+        uint32_t polls = 0;
+        while (!mbar_try_wait(&S.bar, 0) && ++polls < BULK_WAIT_LIMIT) {
+        }
+        if (polls >= BULK_WAIT_LIMIT) {
+            atomicOr(status, RT_DEV_TIMEOUT);
+            while (!mbar_try_wait(&S.bar, 0) && ++polls < 2 * BULK_WAIT_LIMIT) {
+            }
+        }
+#else
+        const uint4* k4 = reinterpret_cast<const uint4*>(kin + base);
+        const uint4* v4 = reinterpret_cast<const uint4*>(vin + base);
+#pragma unroll
+        for (int j = 0; j < ITEMS / 4; ++j) {
+            const int e = j * SORT_THREADS + tid;
+            reinterpret_cast<uint4*>(S.keys)[e] = __ldcs(&k4[e]);
+            if (vin) reinterpret_cast<uint4*>(S.vals)[e] = __ldcs(&v4[e]);
+        }
+        __syncthreads();
+#endif
+#pragma unroll
+        for (int j = 0; j < ITEMS; ++j) {
+            const int e = warp * (ITEMS * 32) + j * 32 + lane;
+            k[j] = S.keys[e];
+            v[j] = vin ? S.vals[e] : (uint32_t)(base + e);
+        }
+    } else
+#endif
 #pragma unroll
     for (int j = 0; j < ITEMS; ++j) {
         const size_t g = base + (size_t)warp * (ITEMS * 32) + j * 32 + lane;
@@ -358,10 +443,15 @@ __device__ __forceinline__ void onesweep_tile(SortSmemT<ITEMS, BITS>& S, uint32_
         const uint32_t key = S.keys[i];
         const uint32_t d = (key >> shift) & DMASK;
         const uint32_t dst = S.goff[d] + i;
-        kout[dst] = key;
-        vout[dst] = S.vals[i];
+        if (dst < n) {   // always, unless a wait gave up (RT_DEV_TIMEOUT)
+            kout[dst] = key;
+            vout[dst] = S.vals[i];
+        }
     }
     __syncthreads();   // the shared buffers are reused by the next tile
+#if RT_SORT_VEC_LOADS == 2
+    if (vec && tid == 0) mbar_inval(&S.bar);
+#endif
     RT_SORT_MARK(5);
 }
 
