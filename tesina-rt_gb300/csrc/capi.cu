@@ -411,7 +411,7 @@ int32_t rt_shutdown(rt_ctx* c) {
     }
     if (c->ev_fork) cudaEventDestroy(c->ev_fork);
     if (c->ev_join) cudaEventDestroy(c->ev_join);
-    if (c->h_status) cudaFreeHost(c->h_status);
+    if (c->h_stage) cudaFreeHost(c->h_stage);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return RT_OK;
@@ -1218,23 +1218,24 @@ int32_t rt_render_host(rt_ctx* c, rt_scene* s, const float* pos4, const float* n
         CU(cudaStreamCreateWithFlags(&c->host_side, cudaStreamNonBlocking));
         CU(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
         CU(cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming));
-        CU(cudaMallocHost(&c->h_status, sizeof(uint32_t)));
+        CU(cudaMallocHost(&c->h_stage, sizeof(rt_ctx::HostStage)));
     }
     const bool side_normals = pos4 && nrm4;
     if (pos4) {
         if (V != s->V) return fail(RT_ERR_INVALID, "vertex count %u != scene's %u", V, s->V);
         CU(scene_write_begin(s, cs));
+        CU(cudaMemcpyAsync(s->d_pos, pos4, 16 * (size_t)V, cudaMemcpyHostToDevice, cs));
         if (side_normals) {
             // the build reads positions only: the normals go up beside it, on
-            // a stream that starts after everything queued on cs so far (the
-            // scene's earlier readers) and that the render waits for
+            // a stream that starts once the positions are up (the two copies
+            // would share the link and hold the build back) and that the
+            // render waits for
             CU(cudaEventRecord(c->ev_fork, cs));
             CU(cudaStreamWaitEvent(c->host_side, c->ev_fork, 0));
             CU(cudaMemcpyAsync(s->d_nrm, nrm4, 16 * (size_t)V, cudaMemcpyHostToDevice,
                                c->host_side));
             CU(cudaEventRecord(c->ev_join, c->host_side));
         }
-        CU(cudaMemcpyAsync(s->d_pos, pos4, 16 * (size_t)V, cudaMemcpyHostToDevice, cs));
         CU(scene_write_end(s, cs));
     }
     r = rt_bvh_build_lbvh(c, s, cfg, stream);
@@ -1255,10 +1256,14 @@ int32_t rt_render_host(rt_ctx* c, rt_scene* s, const float* pos4, const float* n
     r = rt_render(c, s, cam, w, h, max_bounces, c->d_out, nullptr, c->d_stats, stream);
     if (r) return r;
     CU(cudaMemcpyAsync(h_rgba, c->d_out, bytes, cudaMemcpyDeviceToHost, cs));
-    if (h_stats) CU(cudaMemcpyAsync(h_stats, c->d_stats, sizeof(*h_stats), cudaMemcpyDeviceToHost, cs));
-    CU(cudaMemcpyAsync(c->h_status, c->d_status, sizeof(uint32_t), cudaMemcpyDeviceToHost, cs));
+    if (h_stats)
+        CU(cudaMemcpyAsync(&c->h_stage->stats, c->d_stats, sizeof(rt_render_stats),
+                           cudaMemcpyDeviceToHost, cs));
+    CU(cudaMemcpyAsync(&c->h_stage->status, c->d_status, sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                       cs));
     CU(cudaStreamSynchronize(cs));
-    const uint32_t bits = *c->h_status;
+    if (h_stats) *h_stats = c->h_stage->stats;
+    const uint32_t bits = c->h_stage->status;
     if (bits & RT_DEV_TIMEOUT) return fail(RT_ERR_TIMEOUT, "rt_render_host: device wait timed out");
     if (bits & RT_DEV_OVERFLOW) return fail(RT_ERR_OVERFLOW, "rt_render_host: stack overflow");
     return RT_OK;

@@ -32,10 +32,15 @@ struct rt_ctx {
     size_t d_out_cap = 0;
     rt_render_stats* d_stats = nullptr;  // rt_render_host counters
     // rt_render_host: a stream for the normal upload beside the build, the
-    // events that fork and join it, and a pinned status word
+    // events that fork and join it, and pinned staging for the counters and
+    // the status word (read back without blocking the host before the end)
     cudaStream_t host_side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
-    uint32_t* h_status = nullptr;
+    struct HostStage {
+        rt_render_stats stats;
+        uint32_t status;
+    };
+    HostStage* h_stage = nullptr;
     float inv1e6 = 1.0f / 1e6f;
     // until the autotuner or the caller picks one: the pooled kernel
     // (variant 8, k_render_pool<128, 6>) at full residency
