@@ -45,6 +45,14 @@ RENDER_DRAM_BYTES = {
     "k_render_pool<256, 3>": (286.5 + 28.8) * 1e6,
     "k_render_pool<256, 4>": (318.8 + 37.1) * 1e6,
 }
+# the same for the stress workload (17.7 M triangles, 3840x2160, 3 lights,
+# depth 6), the mean over its 8 poses
+STRESS_RENDER_DRAM_BYTES = {
+    "k_render_pool<128, 6>": (2041.6 + 177.7) * 1e6,
+    "k_render_pool<128, 8>": (2149.0 + 209.5) * 1e6,
+    "k_render_pool<256, 3>": (1931.3 + 147.6) * 1e6,
+    "k_render_pool<256, 4>": (2148.2 + 209.5) * 1e6,
+}
 
 
 def log(*a):
@@ -339,6 +347,9 @@ def measure_stress(ctx, lib, torch, builds=5, cpu=True):
     rgba = ctx.alloc(4 * w * h)
     stats = ctx.alloc(32)
     ctx.sync()
+    rv = ctx.render_config().variant
+    vt, vm, _ = ctx.variants()[rv]
+    kname = ("k_render_pool<%d, %d>" if ctx.variant_pooled(rv) else "k_render<%d, %d>") % (vt, vm)
     t_build = []
     for k in range(2 + builds):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -402,9 +413,10 @@ def measure_stress(ctx, lib, torch, builds=5, cpu=True):
             "render_ms_per_pose": tr / len(t_render), "rays": rays, "shadow_rays": shadow,
             "mrays_s": rays / (tr * 1e-3) / 1e6,
             "mrays_all_incl_shadow": (rays + shadow) / (tr * 1e-3) / 1e6,
-            "roofline": {"kernel": "render (installed variant)", "bound": "hbm",
+            "roofline": {"kernel": kname, "bound": "hbm",
                          "achieved": render_gbs, "peak": hbm, "unit": "GB/s",
-                         "frac": render_gbs / hbm, "traffic": None, "peak_kind": kind,
+                         "frac": render_gbs / hbm,
+                         "traffic": STRESS_RENDER_DRAM_BYTES.get(kname), "peak_kind": kind,
                          "algorithmic_bytes_per_pose": render_bytes / len(t_render)},
             "e2e": {"value": e2e_rays / (sum(e2e_ms) * 1e-3) / 1e6, "unit": UNIT,
                     "h2d_bytes_per_step": 2 * 16 * V, "d2h_bytes_per_step": 4 * w * h + 32,
@@ -941,9 +953,12 @@ def run_gpu(args):
                         "ray + 25 B per shadow ray"}
     # the emit's levels: 512 triangles per level-0 block, then 8 blocks per block
     emit_levels = emit_levels_of(n_tris)
-    launches_per_frame = 7 + emit_levels + (2 if pooled else 1)
-    build_roofline = {"kernels": "k_bounds + k_morton_hist + 4x k_onesweep + k_permute + "
-                                 "%dx k_emit_level" % emit_levels, "bound": "hbm",
+    # k_bounds, k_morton_hist, 4 radix passes, the emit levels (the first
+    # one also permutes), then the render (+ k_fb_copy when pooled)
+    launches_per_frame = 6 + emit_levels + (2 if pooled else 1)
+    build_roofline = {"kernels": "k_bounds + k_morton_hist + 4x k_onesweep + "
+                                 "k_emit_level0_permute + %dx k_emit_level" % (emit_levels - 1),
+                      "bound": "hbm",
                       "achieved": build_gbs,
                       "peak": peak, "unit": "GB/s", "frac": build_gbs / peak,
                       "bytes_per_tri": B_BUILD_PER_TRI, "peak_kind": peak_kind,
