@@ -21,7 +21,10 @@ namespace rt {
 #endif
 constexpr int SORT_THREADS = 256;
 constexpr int SORT_WARPS = SORT_THREADS / 32;
-constexpr int SORT_ITEMS = 16;
+#ifndef RT_SORT_ITEMS
+#define RT_SORT_ITEMS 16   // keys per thread of a radix tile
+#endif
+constexpr int SORT_ITEMS = RT_SORT_ITEMS;
 constexpr int SORT_TILE = SORT_THREADS * SORT_ITEMS;   // 4096 keys per tile
 constexpr uint32_t LB_AGG = 1u << 30, LB_PREFIX = 2u << 30, LB_MASK = (1u << 30) - 1;
 constexpr uint32_t LB_SPIN_LIMIT = 1u << 22;
