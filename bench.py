@@ -9,9 +9,12 @@ to device) + LBVH build + render.  Metric: Mrays/s with the reference's ray
 count convention (primary + secondary rays, shadow rays not counted).
 
 Device-timed ``value``: inputs resident in HBM, CUDA events on the launching
-stream, L2 flushed (256 MiB write) between steps.  ``e2e``: the same frame
-through rt_render_host with pinned host buffers (vertex upload, build,
-render, RGBA8 download inside the timed region).
+stream, L2 flushed (256 MiB write) between steps.  ``e2e``: the same frames
+through the public host-buffer entry points with pinned host buffers (vertex
+upload, build, render, RGBA8 download inside the timed region for every
+frame): two frames in flight through rt_render_host_async /
+rt_render_host_wait on two streams with one scene copy each (``value``), and
+one frame at a time through rt_render_host (``sync_value``).
 
 --impl reference: the oracle (CPU restatement of the reference's kernels,
 point lights and several lights included) on all host cores, on a bounded
@@ -890,37 +893,117 @@ def run_gpu(args):
     # e2e through the public entry point with pinned host buffers
     pin_pos = [torch.from_numpy(p).pin_memory() for p, _ in frames]
     pin_nrm = [torch.from_numpy(n).pin_memory() for _, n in frames]
-    host_rgba = torch.empty((h * w, 4), dtype=torch.uint8).pin_memory()
+    host_rgba = [torch.empty((h * w, 4), dtype=torch.uint8).pin_memory() for _ in range(2)]
     cfg = abi.BvhCfg(30, 1)
-    hst = abi.RenderStats()
+    hst = [abi.RenderStats(), abi.RenderStats()]
 
     def e2e_step(i):
         capi.check(lib, lib.rt_render_host(ctx.h, scene.h, C.c_void_p(pin_pos[i].data_ptr()),
                                            C.c_void_p(pin_nrm[i].data_ptr()), V, C.byref(cfg),
                                            C.byref(wl["camera"]), w, h, nb,
-                                           C.c_void_p(host_rgba.data_ptr()), C.byref(hst), sh))
-        return int(hst.primary_rays + hst.secondary_rays)
+                                           C.c_void_p(host_rgba[0].data_ptr()), C.byref(hst[0]),
+                                           sh))
+        return int(hst[0].primary_rays + hst[0].secondary_rays)
 
+    # (1) one frame at a time: rt_render_host, L2 flushed between frames
     for i in range(min(args.warmup, nframes)):
         e2e_step(i)
-    e2e_ms, e2e_rays = [], 0
+    sync_ms, sync_rays = [], 0
     for k in range(args.steps):
         flush.zero(sh)
         stream.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        e2e_rays += e2e_step((args.warmup + k) % nframes)
+        sync_rays += e2e_step((args.warmup + k) % nframes)
         e1.record(stream)
         stream.synchronize()
-        e2e_ms.append(e0.elapsed_time(e1))
-    e2e_total = sum(e2e_ms)
+        sync_ms.append(e0.elapsed_time(e1))
+    # (2) two frames in flight: rt_render_host_async on two streams, each
+    # with its own copy of the scene, frame k collected after frame k + 1 is
+    # queued, so one frame's uploads and read-back overlap the other's build
+    # and render.  Each frame still uploads its vertices and reads back its
+    # image inside the timed region.  Consecutive frames use different scene
+    # copies: a frame's buffers were last touched two frames before, with the
+    # other copy's frame (a working set of about 250 MB, twice the L2) between.
+    scene2 = capi.Scene(ctx, ter.scene(0))
+    pair = [scene, scene2]
+    stream2 = torch.cuda.Stream()
+    shs = [sh, C.c_void_p(stream2.cuda_stream)]
+
+    def e2e_issue(k, i):
+        j = k % 2
+        capi.check(lib, lib.rt_render_host_async(
+            ctx.h, pair[j].h, C.c_void_p(pin_pos[i].data_ptr()), C.c_void_p(pin_nrm[i].data_ptr()),
+            V, C.byref(cfg), C.byref(wl["camera"]), w, h, nb, C.c_void_p(host_rgba[j].data_ptr()),
+            C.byref(hst[j]), shs[j]))
+
+    def e2e_collect(k):
+        j = k % 2
+        ctx.render_host_wait(shs[j])
+        return int(hst[j].primary_rays + hst[j].secondary_rays)
+
+    def e2e_run(first, count):
+        rays_run = 0
+        for k in range(count):
+            e2e_issue(k, (first + k) % nframes)
+            if k:
+                rays_run += e2e_collect(k - 1)
+        return rays_run + e2e_collect(count - 1)
+
+    e2e_run(0, min(max(args.warmup, 2), nframes))
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    stream2.wait_event(e0)
+    e2e_rays = e2e_run(args.warmup, args.steps)
+    stream.wait_stream(stream2)
+    e1.record(stream)
+    stream.synchronize()
+    e2e_total = e0.elapsed_time(e1)
+    sync_total = sum(sync_ms)
+    # (3) the device-resident frame (vertex update from HBM, build, render)
+    # with the same two frames in flight and no host copies: the device-side
+    # counterpart of (2)
+    outs = [rgba, ctx.alloc(4 * w * h)]
+    pstats = [ctx.alloc(32), ctx.alloc(32)]
+
+    def dev_issue(k, i):
+        j = k % 2
+        capi.check(lib, lib.rt_scene_update_vertices_device(ctx.h, pair[j].h, dpos[i].ptr,
+                                                            dnrm[i].ptr, V, shs[j]))
+        pair[j].build(30, 1, stream=shs[j])
+        pair[j].render(wl["camera"], w, h, nb, outs[j], None, pstats[j], stream=shs[j])
+
+    for k in range(2):
+        dev_issue(k, k % nframes)
+    torch.cuda.synchronize()
+    for j in range(2):
+        pstats[j].zero(shs[j])
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    stream2.wait_event(e0)
+    for k in range(args.steps):
+        dev_issue(k, (args.warmup + k) % nframes)
+    stream.wait_stream(stream2)
+    e1.record(stream)
+    stream.synchronize()
+    pipe_total = e0.elapsed_time(e1)
+    pipe_rays = 0
+    for j in range(2):
+        st2 = pstats[j].read(np.uint64)
+        pipe_rays += int(st2[0] + st2[1])
     if world > 1:
         import torch.distributed as dist
-        t = torch.tensor([e2e_total, float(e2e_rays)], device="cuda")
-        dist.all_reduce(t[0:1], op=dist.ReduceOp.MAX)
-        dist.all_reduce(t[1:2], op=dist.ReduceOp.SUM)
-        e2e_total, e2e_rays = float(t[0]), float(t[1])
+        t = torch.tensor([e2e_total, float(e2e_rays), sync_total, float(sync_rays), pipe_total,
+                          float(pipe_rays)], device="cuda")
+        for a in range(0, 6, 2):
+            dist.all_reduce(t[a:a + 1], op=dist.ReduceOp.MAX)
+            dist.all_reduce(t[a + 1:a + 2], op=dist.ReduceOp.SUM)
+        e2e_total, e2e_rays, sync_total, sync_rays, pipe_total, pipe_rays = (float(x) for x in t)
     e2e_value = e2e_rays / (e2e_total * 1e-3) / 1e6
+    sync_value = sync_rays / (sync_total * 1e-3) / 1e6
+    pipe_value = pipe_rays / (pipe_total * 1e-3) / 1e6
 
     if rank != 0:
         if world > 1:
@@ -1036,6 +1119,9 @@ def run_gpu(args):
            "config": {"workload": wl["name"], "triangles": n_tris, "width": w, "height": h,
                       "max_bounces": nb, "lights": 2, "lbvh_depth": 30, "lbvh_min_leaf": 1,
                       "rebuild_per_frame": True, "l2": "flushed (256 MiB write) between steps",
+                      "e2e_l2": "two scene copies alternate: a frame's buffers were last touched "
+                                "two frames before, the other copy's frame (about 250 MB, twice "
+                                "the L2) between",
                       "parallelism": "replicas" if world > 1 else "single GPU"},
            "mrays_all_incl_shadow": (rays_all + shadow * world) / (total_ms * 1e-3) / 1e6,
            "lbvh_mtri_s": n_tris / (med_build * 1e-3) / 1e6,
@@ -1053,8 +1139,19 @@ def run_gpu(args):
            "sah": sah_leg,
            "e2e": {"value": e2e_value, "unit": UNIT,
                    "h2d_bytes_per_step": 2 * 16 * V,
-                   "d2h_bytes_per_step": 4 * w * h + 32,
-                   "ms_per_step": e2e_total / args.steps},
+                   "d2h_bytes_per_step": 4 * w * h + 32 + 4,
+                   "ms_per_step": e2e_total / args.steps,
+                   "mode": "two frames in flight: rt_render_host_async / rt_render_host_wait on "
+                           "two streams with one scene copy each (a frame's buffers last touched "
+                           "two frames before; each frame's upload and read-back timed)",
+                   "sync_value": sync_value,
+                   "sync_ms_per_step": statistics.median(sync_ms),
+                   "sync_mode": "rt_render_host, one frame at a time, L2 flushed between frames"},
+           "two_in_flight": {"value": pipe_value, "unit": UNIT,
+                             "ms_per_step": pipe_total / args.steps,
+                             "mode": "device-resident frames (vertex update from HBM, build, "
+                                     "render), two in flight on two streams with one scene copy "
+                                     "each, no host copies: the device-side counterpart of e2e"},
            "gpu_launches": launches_per_frame * args.steps,
            "render_config": {"variant": tuned.variant, "threads": ctx.variants()[tuned.variant][0],
                              "min_blocks_per_sm": ctx.variants()[tuned.variant][1],

@@ -516,12 +516,29 @@ RT_API int32_t rt_server_reset_stats(rt_server* server);
 /* End-to-end convenience: host vertices in, host image out, synchronous:
  * optional vertex update -> LBVH build -> render -> RGBA8 to host.  The
  * normals, which only the render reads, are uploaded on a stream of the
- * context's own beside the positions and the build; pinned host buffers make
- * the copies asynchronous. */
+ * context's own once the positions are up, beside the build; pinned host
+ * buffers make the copies asynchronous.  Equal to rt_render_host_async
+ * followed by rt_render_host_wait on the same stream. */
 RT_API int32_t rt_render_host(rt_ctx* ctx, rt_scene* scene, const float* h_pos4, const float* h_nrm4,
                        uint32_t vertex_count, const rt_bvh_cfg* cfg, const rt_camera* cam,
                        int32_t width, int32_t height, int32_t max_bounces, uint8_t* h_rgba,
                        rt_render_stats* h_stats, rt_stream s);
+/* rt_render_host without the final wait: queues the frame on stream s
+ * (uploads, build, render, image and counter read-back) and returns; the
+ * host buffers must stay untouched until rt_render_host_wait(ctx, s) returns,
+ * which synchronises s, fills h_stats and maps the device status as
+ * rt_render_host does.  One frame may be pending per stream: a second call
+ * on the same stream before the wait returns RT_ERR_INVALID.  Frames on two
+ * streams (each with its own scene, or the same scene: the scene's accesses
+ * are ordered across streams) overlap one frame's copies with the other's
+ * build and render.  No reference counterpart (the reference renders one
+ * frame at a time, src/rt/renderer.cpp:113-214). */
+RT_API int32_t rt_render_host_async(rt_ctx* ctx, rt_scene* scene, const float* h_pos4,
+                                    const float* h_nrm4, uint32_t vertex_count,
+                                    const rt_bvh_cfg* cfg, const rt_camera* cam, int32_t width,
+                                    int32_t height, int32_t max_bounces, uint8_t* h_rgba,
+                                    rt_render_stats* h_stats, rt_stream s);
+RT_API int32_t rt_render_host_wait(rt_ctx* ctx, rt_stream s);
 
 /* ------------------------------------------------------------------------ */
 /* Sort without allocation (no counterpart in the reference)                */

@@ -275,12 +275,32 @@ uint32_t* work_counter(rt_ctx* c, cudaStream_t s) {
     return p;
 }
 
+// Frees the rt_render_host state of one stream (its side stream finished).
+static void free_host_render(rt_ctx::HostRender& R) {
+    if (R.side) {
+        cudaStreamSynchronize(R.side);
+        cudaStreamDestroy(R.side);
+    }
+    if (R.fork) cudaEventDestroy(R.fork);
+    if (R.join) cudaEventDestroy(R.join);
+    if (R.d_out) cudaFree(R.d_out);
+    if (R.d_stats) cudaFree(R.d_stats);
+    if (R.h_stage) cudaFreeHost(R.h_stage);
+    R = rt_ctx::HostRender{};
+}
+
 void release_work_counter(rt_ctx* c, cudaStream_t s) {
     std::lock_guard<std::mutex> lk(c->work_mu);
     auto it = c->work_by_stream.find(s);
     if (it != c->work_by_stream.end()) {
         cudaFree(it->second);
         c->work_by_stream.erase(it);
+    }
+    auto ih = c->host_by_stream.find(s);
+    if (ih != c->host_by_stream.end()) {
+        cudaStreamSynchronize(s);
+        free_host_render(ih->second);
+        c->host_by_stream.erase(ih);
     }
     for (auto* m : {&c->accum_by_stream, &c->sec_by_stream}) {
         auto ia = m->find(s);
@@ -403,15 +423,10 @@ int32_t rt_shutdown(rt_ctx* c) {
     for (auto* m : {&c->accum_by_stream, &c->sec_by_stream})
         for (auto& kv : *m)
             if (kv.second.first) cudaFree(kv.second.first);
-    dfree(c->d_out);
-    dfree(c->d_stats);
-    if (c->host_side) {
-        cudaStreamSynchronize(c->host_side);
-        cudaStreamDestroy(c->host_side);
+    for (auto& kv : c->host_by_stream) {
+        cudaStreamSynchronize(kv.first);
+        rt::free_host_render(kv.second);
     }
-    if (c->ev_fork) cudaEventDestroy(c->ev_fork);
-    if (c->ev_join) cudaEventDestroy(c->ev_join);
-    if (c->h_stage) cudaFreeHost(c->h_stage);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return RT_OK;
@@ -1207,18 +1222,27 @@ int32_t rt_autotune_render(rt_ctx* c, rt_scene* s, const rt_camera* cam, int32_t
     return RT_OK;
 }
 
-int32_t rt_render_host(rt_ctx* c, rt_scene* s, const float* pos4, const float* nrm4, uint32_t V,
-                       const rt_bvh_cfg* cfg, const rt_camera* cam, int32_t w, int32_t h,
-                       int32_t max_bounces, uint8_t* h_rgba, rt_render_stats* h_stats,
-                       rt_stream stream) {
+int32_t rt_render_host_async(rt_ctx* c, rt_scene* s, const float* pos4, const float* nrm4,
+                             uint32_t V, const rt_bvh_cfg* cfg, const rt_camera* cam, int32_t w,
+                             int32_t h, int32_t max_bounces, uint8_t* h_rgba,
+                             rt_render_stats* h_stats, rt_stream stream) {
     if (!c || !s || !cam || !h_rgba) return fail(RT_ERR_INVALID, "rt_render_host: null argument");
     cudaStream_t cs = st(c, stream);
-    int32_t r;
-    if (!c->host_side) {
-        CU(cudaStreamCreateWithFlags(&c->host_side, cudaStreamNonBlocking));
-        CU(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
-        CU(cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming));
-        CU(cudaMallocHost(&c->h_stage, sizeof(rt_ctx::HostStage)));
+    rt_ctx::HostRender* Rp;
+    {
+        std::lock_guard<std::mutex> lk(c->work_mu);
+        Rp = &c->host_by_stream[cs];
+    }
+    rt_ctx::HostRender& R = *Rp;
+    if (R.pending)
+        return fail(RT_ERR_INVALID, "rt_render_host_async: the stream's previous frame has not "
+                                    "been collected (rt_render_host_wait)");
+    if (!R.side) {
+        CU(cudaStreamCreateWithFlags(&R.side, cudaStreamNonBlocking));
+        CU(cudaEventCreateWithFlags(&R.fork, cudaEventDisableTiming));
+        CU(cudaEventCreateWithFlags(&R.join, cudaEventDisableTiming));
+        CU(cudaMallocHost(&R.h_stage, sizeof(*R.h_stage)));
+        CU(cudaMalloc(&R.d_stats, sizeof(rt_render_stats)));
     }
     const bool side_normals = pos4 && nrm4;
     if (pos4) {
@@ -1230,43 +1254,69 @@ int32_t rt_render_host(rt_ctx* c, rt_scene* s, const float* pos4, const float* n
             // a stream that starts once the positions are up (the two copies
             // would share the link and hold the build back) and that the
             // render waits for
-            CU(cudaEventRecord(c->ev_fork, cs));
-            CU(cudaStreamWaitEvent(c->host_side, c->ev_fork, 0));
-            CU(cudaMemcpyAsync(s->d_nrm, nrm4, 16 * (size_t)V, cudaMemcpyHostToDevice,
-                               c->host_side));
-            CU(cudaEventRecord(c->ev_join, c->host_side));
+            CU(cudaEventRecord(R.fork, cs));
+            CU(cudaStreamWaitEvent(R.side, R.fork, 0));
+            CU(cudaMemcpyAsync(s->d_nrm, nrm4, 16 * (size_t)V, cudaMemcpyHostToDevice, R.side));
+            CU(cudaEventRecord(R.join, R.side));
         }
         CU(scene_write_end(s, cs));
     }
-    r = rt_bvh_build_lbvh(c, s, cfg, stream);
+    int32_t r = rt_bvh_build_lbvh(c, s, cfg, stream);
     if (r) return r;
-    if (side_normals) CU(cudaStreamWaitEvent(cs, c->ev_join, 0));
+    if (side_normals) CU(cudaStreamWaitEvent(cs, R.join, 0));
     const size_t bytes = 4 * (size_t)w * h;
-    if (c->d_out_cap < bytes) {
-        dfree(c->d_out);
-        if (cudaMalloc(&c->d_out, bytes)) {
+    if (R.out_cap < bytes) {
+        if (R.d_out) cudaFreeAsync(R.d_out, cs);
+        R.d_out = nullptr;
+        R.out_cap = 0;
+        if (cudaMallocAsync(reinterpret_cast<void**>(&R.d_out), bytes, cs)) {
             cudaGetLastError();
-            c->d_out_cap = 0;
             return fail(RT_ERR_OOM, "rt_render_host: image allocation failed");
         }
-        c->d_out_cap = bytes;
+        R.out_cap = bytes;
     }
-    if (!c->d_stats) CU(cudaMalloc(&c->d_stats, sizeof(rt_render_stats)));
-    CU(cudaMemsetAsync(c->d_stats, 0, sizeof(rt_render_stats), cs));
-    r = rt_render(c, s, cam, w, h, max_bounces, c->d_out, nullptr, c->d_stats, stream);
+    CU(cudaMemsetAsync(R.d_stats, 0, sizeof(rt_render_stats), cs));
+    r = rt_render(c, s, cam, w, h, max_bounces, R.d_out, nullptr, R.d_stats, stream);
     if (r) return r;
-    CU(cudaMemcpyAsync(h_rgba, c->d_out, bytes, cudaMemcpyDeviceToHost, cs));
+    CU(cudaMemcpyAsync(h_rgba, R.d_out, bytes, cudaMemcpyDeviceToHost, cs));
     if (h_stats)
-        CU(cudaMemcpyAsync(&c->h_stage->stats, c->d_stats, sizeof(rt_render_stats),
+        CU(cudaMemcpyAsync(&R.h_stage->stats, R.d_stats, sizeof(rt_render_stats),
                            cudaMemcpyDeviceToHost, cs));
-    CU(cudaMemcpyAsync(&c->h_stage->status, c->d_status, sizeof(uint32_t), cudaMemcpyDeviceToHost,
+    CU(cudaMemcpyAsync(&R.h_stage->status, c->d_status, sizeof(uint32_t), cudaMemcpyDeviceToHost,
                        cs));
+    R.user_stats = h_stats;
+    R.pending = true;
+    return RT_OK;
+}
+
+int32_t rt_render_host_wait(rt_ctx* c, rt_stream stream) {
+    if (!c) return fail(RT_ERR_INVALID, "rt_render_host_wait: null context");
+    cudaStream_t cs = st(c, stream);
+    rt_ctx::HostRender* Rp = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(c->work_mu);
+        auto it = c->host_by_stream.find(cs);
+        if (it != c->host_by_stream.end()) Rp = &it->second;
+    }
+    if (!Rp || !Rp->pending)
+        return fail(RT_ERR_INVALID, "rt_render_host_wait: no frame pending on this stream");
+    rt_ctx::HostRender& R = *Rp;
+    R.pending = false;
     CU(cudaStreamSynchronize(cs));
-    if (h_stats) *h_stats = c->h_stage->stats;
-    const uint32_t bits = c->h_stage->status;
+    if (R.user_stats) *R.user_stats = R.h_stage->stats;
+    const uint32_t bits = R.h_stage->status;
     if (bits & RT_DEV_TIMEOUT) return fail(RT_ERR_TIMEOUT, "rt_render_host: device wait timed out");
     if (bits & RT_DEV_OVERFLOW) return fail(RT_ERR_OVERFLOW, "rt_render_host: stack overflow");
     return RT_OK;
+}
+
+int32_t rt_render_host(rt_ctx* c, rt_scene* s, const float* pos4, const float* nrm4, uint32_t V,
+                       const rt_bvh_cfg* cfg, const rt_camera* cam, int32_t w, int32_t h,
+                       int32_t max_bounces, uint8_t* h_rgba, rt_render_stats* h_stats,
+                       rt_stream stream) {
+    const int32_t r = rt_render_host_async(c, s, pos4, nrm4, V, cfg, cam, w, h, max_bounces,
+                                           h_rgba, h_stats, stream);
+    return r ? r : rt_render_host_wait(c, stream);
 }
 
 }  // extern "C"

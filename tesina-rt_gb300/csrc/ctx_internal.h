@@ -28,19 +28,25 @@ struct rt_ctx {
     // rt_gen_secondary block offsets, per stream, with their size in bytes
     // (stream-ordered allocations)
     std::map<cudaStream_t, std::pair<uint32_t*, size_t>> sec_by_stream;
-    uint8_t* d_out = nullptr;            // rt_render_host image staging
-    size_t d_out_cap = 0;
-    rt_render_stats* d_stats = nullptr;  // rt_render_host counters
-    // rt_render_host: a stream for the normal upload beside the build, the
-    // events that fork and join it, and pinned staging for the counters and
-    // the status word (read back without blocking the host before the end)
-    cudaStream_t host_side = nullptr;
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
-    struct HostStage {
-        rt_render_stats stats;
-        uint32_t status;
+    // rt_render_host / rt_render_host_async, per stream: a stream for the
+    // normal upload beside the build and the events that fork and join it,
+    // the device image and counters, pinned staging for the counters and the
+    // status word (read back without blocking the host), and the frame that
+    // waits for rt_render_host_wait
+    struct HostRender {
+        cudaStream_t side = nullptr;
+        cudaEvent_t fork = nullptr, join = nullptr;
+        uint8_t* d_out = nullptr;
+        size_t out_cap = 0;
+        rt_render_stats* d_stats = nullptr;
+        struct Stage {
+            rt_render_stats stats;
+            uint32_t status;
+        }* h_stage = nullptr;
+        rt_render_stats* user_stats = nullptr;
+        bool pending = false;
     };
-    HostStage* h_stage = nullptr;
+    std::map<cudaStream_t, HostRender> host_by_stream;
     float inv1e6 = 1.0f / 1e6f;
     // until the autotuner or the caller picks one: the pooled kernel
     // (variant 8, k_render_pool<128, 6>) at full residency

@@ -66,6 +66,8 @@ SIGNATURES = {
     "rt_fb_copy": (I32, [P, P, P, SZ, P]),
     "rt_render": (I32, [P, P, P, I32, I32, I32, P, P, P, P]),
     "rt_render_host": (I32, [P, P, P, P, U32, P, P, I32, I32, I32, P, P, P]),
+    "rt_render_host_async": (I32, [P, P, P, P, U32, P, P, I32, I32, I32, P, P, P]),
+    "rt_render_host_wait": (I32, [P, P]),
     "rt_sort_pairs_noalloc": (I32, [P, P, P, P, P, U32, I32, P]),
     "rt_render_variants": (I32, [C.POINTER(I32)]),
     "rt_render_variant_info": (I32, [P, I32, C.POINTER(I32), C.POINTER(I32), C.POINTER(I32)]),
@@ -165,6 +167,13 @@ class Context:
 
     def sync(self, stream=None):
         check(self.lib, self.lib.rt_stream_sync(self.h, stream))
+
+    def render_host_wait(self, stream=None, raise_on_error=True):
+        """Waits for the frame rt_render_host_async queued on `stream`."""
+        r = self.lib.rt_render_host_wait(self.h, stream)
+        if raise_on_error:
+            check(self.lib, r)
+        return r
 
     def stream_create(self):
         """A new non-blocking stream of the context (rt_stream handle)."""
@@ -388,6 +397,23 @@ class Scene:
                                                 C.byref(cfg), C.byref(cam), w, h, max_bounces,
                                                 _p(rgba), C.byref(st), stream))
         return rgba, st
+
+    def render_host_async(self, cam, w, h, max_bounces, pos4=None, nrm4=None, depth=30,
+                          min_leaf=1, rgba=None, stats=None, stream=None):
+        """Queues a render_host frame on `stream` and returns (rgba, stats) at
+        once; both are filled by Context.render_host_wait(stream), and they,
+        pos4 and nrm4 must stay alive until then."""
+        if rgba is None:
+            rgba = np.zeros((h * w, 4), np.uint8)
+        if stats is None:
+            stats = abi.RenderStats()
+        cfg = abi.BvhCfg(depth, min_leaf)
+        V = pos4.shape[0] if pos4 is not None else 0
+        check(self.lib, self.lib.rt_render_host_async(self.ctx.h, self.h, _p(pos4), _p(nrm4), V,
+                                                      C.byref(cfg), C.byref(cam), w, h,
+                                                      max_bounces, _p(rgba), C.byref(stats),
+                                                      stream))
+        return rgba, stats
 
     def autotune(self, cam, w, h, max_bounces, trials=2):
         cfg = abi.RenderConfig()

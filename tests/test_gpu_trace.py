@@ -232,6 +232,50 @@ def test_render_host_e2e(ctx, orc):
     assert st.primary_rays == 128 * 128
 
 
+def test_render_host_async_pipelined(ctx):
+    """rt_render_host_async / rt_render_host_wait: frames queued on two
+    streams with two scenes, each collected after the next is queued, equal
+    the synchronous rt_render_host frames; one frame pending per stream."""
+    ter = tiny_terrain(64, 32, 6)
+    cam = scenes.camera((0.0, 4.0, -10.0), (0.0, 0.0, 0.0), aspect=1.0)
+    frames = [ter.frame_vertices(i) for i in range(5)]
+    ref = capi.Scene(ctx, ter.scene(0))
+    expect = []
+    for pos, nrm in frames:
+        rgba, st = ref.render_host(cam, 96, 96, 3, pos, nrm)
+        expect.append((rgba.copy(), st.primary_rays, st.secondary_rays))
+    streams = [ctx.stream_create(), ctx.stream_create()]
+    sc = [capi.Scene(ctx, ter.scene(0)), capi.Scene(ctx, ter.scene(0))]
+    pending = [None, None]
+    got = []
+    try:
+        for k, (pos, nrm) in enumerate(frames):
+            j = k % 2
+            if pending[j] is not None:
+                ctx.render_host_wait(streams[j])
+                got.append(pending[j])
+            rgba, st = sc[j].render_host_async(cam, 96, 96, 3, pos, nrm, stream=streams[j])
+            pending[j] = (k, rgba, st, pos, nrm)
+            if k == 0:   # a second frame on a stream with one pending is refused
+                with pytest.raises(capi.RtError):
+                    sc[0].render_host_async(cam, 96, 96, 3, pos, nrm, stream=streams[0])
+        for j in (0, 1):
+            if pending[j] is not None:
+                ctx.render_host_wait(streams[j])
+                got.append(pending[j])
+        with pytest.raises(capi.RtError):   # nothing pending
+            ctx.render_host_wait(streams[0])
+    finally:
+        for s in streams:
+            ctx.stream_destroy(s)
+    assert sorted(k for k, *_ in got) == list(range(len(frames)))
+    for k, rgba, st, _, _ in got:
+        e_rgba, e_prim, e_sec = expect[k]
+        assert np.array_equal(rgba, e_rgba), "frame %d" % k
+        assert (st.primary_rays, st.secondary_rays) == (e_prim, e_sec)
+    assert ctx.device_status() == 0
+
+
 def test_render_variants_identical(ctx, orc):
     """Every kernel variant / chunk / residency the autotuner can pick gives
     the same image; the autotuner installs and caches its choice."""
