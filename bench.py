@@ -705,7 +705,7 @@ def measure_served(ctx, rates=(2000, 1000, 300, 50), n_req=400, seed=5):
     U[3,6] aimed at the origin, pixels log-uniform 128^2..1920x1080, depth
     U{1..5}.  One burst (all requests at t=0: capacity) and Poisson streams
     at several rates, each through the served configuration (continuous
-    batching: up to 256 requests per launch, 4 launches in flight) and the
+    batching: up to 256 requests per launch, 3 launches in flight) and the
     plain per-request configuration (one rt_render launch per request, one at
     a time).  Latency = submit to image in pinned host memory, server clock;
     Mrays/s = primary+secondary rays / (last done - first submit).  Images
@@ -718,7 +718,7 @@ def measure_served(ctx, rates=(2000, 1000, 300, 50), n_req=400, seed=5):
         cache.get(s)
     log("served: %d pool + %d upload scenes made in %.1f s" % (len(wl["pool"]), len(wl["uploads"]),
                                                              time.time() - t))
-    cfgs = (("served", dict(max_views=256, max_inflight=4)), ("plain", dict(max_views=1)))
+    cfgs = (("served", dict(max_views=256, max_inflight=3)), ("plain", dict(max_views=1)))
     # warm-up: module loads, pinned staging, first launches
     warm = scenes.served_requests(24, None, seed=seed + 99)
     for _, kw in cfgs:
