@@ -1222,28 +1222,12 @@ int32_t rt_autotune_render(rt_ctx* c, rt_scene* s, const rt_camera* cam, int32_t
     return RT_OK;
 }
 
-int32_t rt_render_host_async(rt_ctx* c, rt_scene* s, const float* pos4, const float* nrm4,
-                             uint32_t V, const rt_bvh_cfg* cfg, const rt_camera* cam, int32_t w,
-                             int32_t h, int32_t max_bounces, uint8_t* h_rgba,
-                             rt_render_stats* h_stats, rt_stream stream) {
-    if (!c || !s || !cam || !h_rgba) return fail(RT_ERR_INVALID, "rt_render_host: null argument");
-    cudaStream_t cs = st(c, stream);
-    rt_ctx::HostRender* Rp;
-    {
-        std::lock_guard<std::mutex> lk(c->work_mu);
-        Rp = &c->host_by_stream[cs];
-    }
-    rt_ctx::HostRender& R = *Rp;
-    if (R.pending)
-        return fail(RT_ERR_INVALID, "rt_render_host_async: the stream's previous frame has not "
-                                    "been collected (rt_render_host_wait)");
-    if (!R.side) {
-        CU(cudaStreamCreateWithFlags(&R.side, cudaStreamNonBlocking));
-        CU(cudaEventCreateWithFlags(&R.fork, cudaEventDisableTiming));
-        CU(cudaEventCreateWithFlags(&R.join, cudaEventDisableTiming));
-        CU(cudaMallocHost(&R.h_stage, sizeof(*R.h_stage)));
-        CU(cudaMalloc(&R.d_stats, sizeof(rt_render_stats)));
-    }
+// The work of one rt_render_host frame, queued on cs (see rt_render_host_async).
+static int32_t render_host_enqueue(rt_ctx* c, rt_scene* s, rt_ctx::HostRender& R, cudaStream_t cs,
+                                   const float* pos4, const float* nrm4, uint32_t V,
+                                   const rt_bvh_cfg* cfg, const rt_camera* cam, int32_t w,
+                                   int32_t h, int32_t max_bounces, uint8_t* h_rgba,
+                                   rt_render_stats* h_stats, rt_stream stream) {
     const bool side_normals = pos4 && nrm4;
     if (pos4) {
         if (V != s->V) return fail(RT_ERR_INVALID, "vertex count %u != scene's %u", V, s->V);
@@ -1284,6 +1268,40 @@ int32_t rt_render_host_async(rt_ctx* c, rt_scene* s, const float* pos4, const fl
                            cudaMemcpyDeviceToHost, cs));
     CU(cudaMemcpyAsync(&R.h_stage->status, c->d_status, sizeof(uint32_t), cudaMemcpyDeviceToHost,
                        cs));
+    return RT_OK;
+}
+
+int32_t rt_render_host_async(rt_ctx* c, rt_scene* s, const float* pos4, const float* nrm4,
+                             uint32_t V, const rt_bvh_cfg* cfg, const rt_camera* cam, int32_t w,
+                             int32_t h, int32_t max_bounces, uint8_t* h_rgba,
+                             rt_render_stats* h_stats, rt_stream stream) {
+    if (!c || !s || !cam || !h_rgba) return fail(RT_ERR_INVALID, "rt_render_host: null argument");
+    cudaStream_t cs = st(c, stream);
+    rt_ctx::HostRender* Rp;
+    {
+        std::lock_guard<std::mutex> lk(c->work_mu);
+        Rp = &c->host_by_stream[cs];
+    }
+    rt_ctx::HostRender& R = *Rp;
+    if (R.pending)
+        return fail(RT_ERR_INVALID, "rt_render_host_async: the stream's previous frame has not "
+                                    "been collected (rt_render_host_wait)");
+    if (!R.side) {
+        CU(cudaStreamCreateWithFlags(&R.side, cudaStreamNonBlocking));
+        CU(cudaEventCreateWithFlags(&R.fork, cudaEventDisableTiming));
+        CU(cudaEventCreateWithFlags(&R.join, cudaEventDisableTiming));
+        CU(cudaMallocHost(&R.h_stage, sizeof(*R.h_stage)));
+        CU(cudaMalloc(&R.d_stats, sizeof(rt_render_stats)));
+    }
+    const int32_t r = render_host_enqueue(c, s, R, cs, pos4, nrm4, V, cfg, cam, w, h, max_bounces,
+                                          h_rgba, h_stats, stream);
+    if (r) {
+        // what was queued before the failure may still read the caller's
+        // buffers: let it finish, so that the buffers are free on return
+        cudaStreamSynchronize(R.side);
+        cudaStreamSynchronize(cs);
+        return r;
+    }
     R.user_stats = h_stats;
     R.pending = true;
     return RT_OK;
