@@ -265,6 +265,16 @@ def test_render_host_async_pipelined(ctx):
                 got.append(pending[j])
         with pytest.raises(capi.RtError):   # nothing pending
             ctx.render_host_wait(streams[0])
+        # a frame refused at the door (wrong vertex count) leaves nothing
+        # pending, and the stream takes the next frame
+        pos, nrm = frames[0]
+        with pytest.raises(capi.RtError):
+            sc[0].render_host_async(cam, 96, 96, 3, pos[:-1], nrm[:-1], stream=streams[0])
+        with pytest.raises(capi.RtError):
+            ctx.render_host_wait(streams[0])
+        rgba, st = sc[0].render_host_async(cam, 96, 96, 3, pos, nrm, stream=streams[0])
+        ctx.render_host_wait(streams[0])
+        assert np.array_equal(rgba, expect[0][0])
     finally:
         for s in streams:
             ctx.stream_destroy(s)
